@@ -1,0 +1,627 @@
+// The C ABI of include/bclbm.h: set-up of the device lattice from the
+// reference's Grid/Nodes/LbField arrays, the step loop, downloads in the
+// reference's layout, and FP64 reductions.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "bclbm.h"
+#include "bclbm_launch.h"
+
+using namespace bclbm;
+
+struct bclbm_handle {
+    int q = 0, nd = 0, nfields = 1, collision = 0, precision = 0;
+    uint32_t flags = 0;
+    bool exact = false, trt = false, flux = false;
+    int n_nodes = 0, nf = 0, nf_pad = 0, ns = 0;
+    double tau[2] = {1.0, 1.0};
+    double sigma = 0.0, beta = 0.0, mom_x = 0.0, rho_ref = 1.0, scale = 1.0;
+    double force[3] = {0.0, 0.0, 0.0};
+    std::vector<int32_t> slot_node;   // device slot -> reference node number
+    std::vector<int32_t> slot_bulk;   // device slot -> index in the bulk list
+    std::vector<int32_t> bulk;        // the bulk list
+    std::vector<int32_t> solid_node;  // extended solid index -> reference node number
+    std::vector<double> solid_cg;     // RK colour of the stored solids
+    bool bulk_contiguous = false;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void* pops[2] = {nullptr, nullptr};
+    int cur = 0;
+    bool state_post = false;          // pops[cur] holds post-collision populations
+    bool macros_valid = false;
+    int32_t* d_nbr = nullptr;
+    int32_t* d_slot_bulk = nullptr;
+    double* d_rho = nullptr;
+    double* d_vel = nullptr;
+    double* d_cg = nullptr;
+    DevParams* d_params = nullptr;
+    double* d_partials = nullptr;
+    double* d_red = nullptr;
+    double* d_gather = nullptr;
+    int32_t ghost_src[19] = {0};
+    int64_t steps_done = 0;
+    std::string last_error;
+};
+
+namespace {
+
+size_t store_bytes(int precision) {
+    switch (precision) {
+        case BCLBM_F64: return 8;
+        case BCLBM_F32: return 4;
+        default: return 2;
+    }
+}
+
+int fail(bclbm_handle* h, int code, const std::string& msg) {
+    if (h) h->last_error = msg;
+    return code;
+}
+
+#define CUDA_TRY(h, expr)                                                                           \
+    do {                                                                                            \
+        cudaError_t e_ = (expr);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            return fail((h), e_ == cudaErrorMemoryAllocation ? BCLBM_ERR_NOMEM : BCLBM_ERR_CUDA,      \
+                        std::string(#expr) + ": " + cudaGetErrorString(e_));                          \
+        }                                                                                           \
+    } while (0)
+
+int rev_dir(int Q, int q) {
+    if (Q == 9) return q == 8 ? 8 : (q + 4) % 8;
+    return q == 18 ? 18 : (q + 9) % 18;
+}
+
+uint64_t spread_bits(uint64_t v, int dims) {
+    uint64_t out = 0;
+    for (int b = 0; b < 21; ++b)
+        if (v & (1ull << b)) out |= 1ull << (b * dims);
+    return out;
+}
+
+// Everything derived from the descriptor on the host (shared by create and footprint).
+struct Plan {
+    int nf = 0, nf_pad = 0, ns = 0, nfields = 1;
+    std::vector<int32_t> slot_node, slot_bulk, solid_node, ext_of_node;
+};
+
+int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full) {
+    if (!d) { err = "null descriptor"; return BCLBM_ERR_INVALID; }
+    const int Q = d->lattice_q;
+    if (Q != 9 && Q != 19) { err = "lattice_q must be 9 or 19"; return BCLBM_ERR_INVALID; }
+    if (d->n_nodes < 2 || !d->neigh || !d->types || !d->bulk || d->n_bulk < 1) {
+        err = "n_nodes, neigh, types, n_bulk and bulk are required";
+        return BCLBM_ERR_INVALID;
+    }
+    if (d->collision < BCLBM_BGK || d->collision > BCLBM_RK) { err = "unknown collision"; return BCLBM_ERR_INVALID; }
+    if (d->precision < BCLBM_F64 || d->precision > BCLBM_BF16) { err = "unknown precision"; return BCLBM_ERR_INVALID; }
+    if ((d->flags & BCLBM_FLAG_EXACT) && d->precision != BCLBM_F64) {
+        err = "BCLBM_FLAG_EXACT needs BCLBM_F64";
+        return BCLBM_ERR_INVALID;
+    }
+    if ((d->flags & BCLBM_FLAG_SFC_ORDER) && !d->pos) { err = "BCLBM_FLAG_SFC_ORDER needs pos"; return BCLBM_ERR_INVALID; }
+    const int N = d->n_nodes;
+    const int nb = d->n_bulk;
+    if (nb >= N) { err = "n_bulk must be smaller than n_nodes"; return BCLBM_ERR_INVALID; }
+    p.nfields = d->collision == BCLBM_RK ? 2 : 1;
+    const int32_t* nbr = d->neigh;
+    const int16_t* ty = d->types;
+    for (size_t k = 0; k < static_cast<size_t>(N) * Q; ++k)
+        if (nbr[k] < 0 || nbr[k] >= N) {
+            err = "neighbour id out of range at entry " + std::to_string(k);
+            return BCLBM_ERR_TABLE;
+        }
+    std::vector<int32_t> slot_of(N, -1);
+    for (int b = 0; b < nb; ++b) {
+        const int n = d->bulk[b];
+        if (n < 1 || n >= N) { err = "bulk node out of range"; return BCLBM_ERR_INVALID; }
+        if (b > 0 && n <= d->bulk[b - 1]) { err = "bulk list must be increasing"; return BCLBM_ERR_INVALID; }
+        if (ty[n] != 2 && ty[n] != 3) { err = "bulk node " + std::to_string(n) + " is not own-rank fluid"; return BCLBM_ERR_TABLE; }
+        slot_of[n] = b;  // provisional: bulk index
+    }
+    for (int n = 1; n < N; ++n) {
+        if (ty[n] > 1 && slot_of[n] < 0) {
+            err = "fluid node " + std::to_string(n) + " missing from the bulk list";
+            return BCLBM_ERR_TABLE;
+        }
+    }
+    // device order
+    std::vector<int32_t> order(nb);
+    std::iota(order.begin(), order.end(), 0);
+    if (d->flags & BCLBM_FLAG_SFC_ORDER) {
+        const int nd = Q == 9 ? 2 : 3;
+        std::vector<uint64_t> code(nb);
+        for (int b = 0; b < nb; ++b) {
+            const int n = d->bulk[b];
+            uint64_t c = 0;
+            for (int k = 0; k < nd; ++k) {
+                const int64_t v = static_cast<int64_t>(d->pos[static_cast<size_t>(n) * nd + k]) + 1;
+                c |= spread_bits(static_cast<uint64_t>(std::max<int64_t>(v, 0)), nd) << (nd - 1 - k);
+            }
+            code[b] = c;
+        }
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return code[a] < code[b]; });
+    }
+    p.nf = nb;
+    p.nf_pad = (nb + 63) / 64 * 64;
+    p.slot_node.resize(nb);
+    p.slot_bulk.resize(nb);
+    for (int s = 0; s < nb; ++s) {
+        p.slot_bulk[s] = order[s];
+        p.slot_node[s] = d->bulk[order[s]];
+        slot_of[d->bulk[order[s]]] = s;
+    }
+    // extended numbering: fluid slots, then referenced solids in node order, then the ghost
+    p.ext_of_node.assign(N, -1);
+    for (int n = 1; n < N; ++n)
+        if (slot_of[n] >= 0) p.ext_of_node[n] = slot_of[n];
+    std::vector<char> used(N, 0);
+    for (int b = 0; b < nb; ++b) {
+        const size_t n = static_cast<size_t>(d->bulk[b]);
+        for (int q = 0; q < Q; ++q) used[nbr[n * Q + q]] = 1;
+    }
+    p.solid_node.clear();
+    for (int n = 1; n < N; ++n)
+        if (used[n] && ty[n] < 2) {
+            p.ext_of_node[n] = nb + static_cast<int>(p.solid_node.size());
+            p.solid_node.push_back(n);
+        }
+    p.ns = static_cast<int>(p.solid_node.size());
+    p.ext_of_node[0] = nb + p.ns;
+    if (!full) return BCLBM_OK;
+    // the reference streams rest populations to neighbor(rest, n); it must be n itself
+    const int R = Q - 1;
+    for (int b = 0; b < nb; ++b) {
+        const size_t n = static_cast<size_t>(d->bulk[b]);
+        if (nbr[n * Q + R] != static_cast<int32_t>(n)) {
+            err = "rest-direction neighbour of node " + std::to_string(n) + " is not the node itself";
+            return BCLBM_ERR_TABLE;
+        }
+        // pull equivalence: the fluid upstream neighbour pushes into this node, and
+        // this node's fluid downstream neighbour pulls from it (a one-to-one stream map)
+        for (int q = 0; q < R; ++q) {
+            const int y = nbr[n * Q + rev_dir(Q, q)];
+            const int t = nbr[n * Q + q];
+            if ((y != 0 && ty[y] > 1 && nbr[static_cast<size_t>(y) * Q + q] != static_cast<int32_t>(n)) ||
+                (t != 0 && ty[t] > 1 && nbr[static_cast<size_t>(t) * Q + rev_dir(Q, q)] != static_cast<int32_t>(n))) {
+                err = "neighbour table not symmetric at node " + std::to_string(n) + " direction " + std::to_string(q);
+                return BCLBM_ERR_TABLE;
+            }
+        }
+    }
+    return BCLBM_OK;
+}
+
+size_t footprint_bytes(const bclbm_desc* d, const Plan& p) {
+    const int Q = d->lattice_q, D = Q == 9 ? 2 : 3;
+    const size_t pad = static_cast<size_t>(p.nf_pad);
+    size_t b = 2 * static_cast<size_t>(p.nfields) * Q * pad * store_bytes(d->precision);  // two population buffers
+    b += static_cast<size_t>(Q - 1) * pad * 4;                                             // neighbour table
+    b += (static_cast<size_t>(p.nfields) + D) * pad * 8;                                   // macros
+    b += pad * 4;                                                                          // slot -> bulk
+    if (d->collision == BCLBM_RK) b += (static_cast<size_t>(p.nf) + p.ns + 1) * 8;         // colour field
+    b += (static_cast<size_t>(grid_for(p.nf)) * 6 + 64) * 8;                               // reduction partials
+    return b;
+}
+
+StepArgs make_args(const bclbm_handle* h) {
+    StepArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.L.nf = h->nf;
+    a.L.nf_pad = h->nf_pad;
+    a.L.ns = h->ns;
+    a.L.nbr = h->d_nbr;
+    for (int q = 0; q < 19; ++q) a.L.ghost_src[q] = h->ghost_src[q];
+    a.cg = h->d_cg;
+    a.params = h->d_params;
+    a.tau = h->tau[0];
+    a.tau_anti = h->tau[1];
+    // the reference computes 1.0 / tau and (1 - 0.5 / tau) inside its collision functions
+    a.tau_inv = 1.0 / h->tau[0];
+    a.tf = (1 - 0.5 / h->tau[0]);
+    a.tauA_inv = 1.0 / h->tau[1];
+    a.taf = (1 - 0.5 / h->tau[1]);
+    const double c2 = 1.0 / 3.0;
+    a.nu0inv = 1.0 / (c2 * (h->tau[0] - 0.5));
+    a.nu1inv = 1.0 / (c2 * (h->tau[1] - 0.5));
+    a.sigma = h->sigma;
+    a.beta = h->beta;
+    a.rho_ref = h->rho_ref;
+    a.scale = h->scale;
+    a.inv_scale = 1.0 / h->scale;
+    a.partials = h->d_partials;
+    a.n_bulk = h->nf;
+    return a;
+}
+
+__global__ void k_encode(const double* __restrict__ f, void* out, int nf, int nf_pad, int Q, int nfields,
+                         int precision, double rho_ref, double scale) {
+    // f: FP64 [nfields][Q][nf_pad] reference populations -> storage format
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf) return;
+    const size_t fs = static_cast<size_t>(Q) * nf_pad;
+    for (int q = 0; q < Q; ++q) {
+        const double w = Q == 9 ? (q == 8 ? 16.0 / 36.0 : (q % 2 == 0 ? 4.0 / 36.0 : 1.0 / 36.0))
+                                : (q == 18 ? 12.0 / 36.0 : ((q % 9) < 3 ? 2.0 / 36.0 : 1.0 / 36.0));
+        const size_t k = static_cast<size_t>(q) * nf_pad + i;
+        double v0, v1 = 0.0;
+        if (nfields == 1) {
+            v0 = (f[k] - w * rho_ref) / w * scale;
+        } else {
+            v0 = (f[k] + f[fs + k] - w * rho_ref) / w * scale;
+            v1 = (f[k] - f[fs + k]) / w * scale;
+        }
+        switch (precision) {
+            case BCLBM_F32:
+                static_cast<float*>(out)[k] = static_cast<float>(v0);
+                if (nfields == 2) static_cast<float*>(out)[fs + k] = static_cast<float>(v1);
+                break;
+            case BCLBM_F16:
+                static_cast<__half*>(out)[k] = __double2half(v0);
+                if (nfields == 2) static_cast<__half*>(out)[fs + k] = __double2half(v1);
+                break;
+            case BCLBM_BF16:
+                static_cast<__nv_bfloat16*>(out)[k] = __double2bfloat16(v0);
+                if (nfields == 2) static_cast<__nv_bfloat16*>(out)[fs + k] = __double2bfloat16(v1);
+                break;
+        }
+    }
+}
+
+void free_all(bclbm_handle* h) {
+    cudaFree(h->pops[0]);
+    cudaFree(h->pops[1]);
+    cudaFree(h->d_nbr);
+    cudaFree(h->d_slot_bulk);
+    cudaFree(h->d_rho);
+    cudaFree(h->d_vel);
+    cudaFree(h->d_cg);
+    cudaFree(h->d_params);
+    cudaFree(h->d_partials);
+    cudaFree(h->d_red);
+    cudaFree(h->d_gather);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+int run_gather(bclbm_handle* h) {
+    const size_t n = static_cast<size_t>(h->nf) * h->nfields * h->q;
+    if (!h->d_gather) CUDA_TRY(h, cudaMalloc(&h->d_gather, n * sizeof(double)));
+    StepArgs a = make_args(h);
+    a.src = h->pops[h->cur];
+    CUDA_TRY(h, launch_gather(h->q, h->precision, h->nfields, !h->state_post, a, h->d_slot_bulk, h->d_gather,
+                              h->stream));
+    return BCLBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bclbm_error(int status) {
+    switch (status) {
+        case BCLBM_OK: return "ok";
+        case BCLBM_ERR_INVALID: return "invalid argument";
+        case BCLBM_ERR_TABLE: return "inconsistent neighbour table or node types";
+        case BCLBM_ERR_NOMEM: return "out of memory";
+        case BCLBM_ERR_CUDA: return "CUDA error";
+        case BCLBM_ERR_UNSUPPORTED: return "unsupported combination";
+        case BCLBM_ERR_NONFINITE: return "non-finite populations";
+        case BCLBM_ERR_BUDGET: return "request exceeds the HBM budget";
+        case BCLBM_ERR_NOCUDA: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+const char* bclbm_last_error(const bclbm_handle* h) { return h ? h->last_error.c_str() : ""; }
+
+int64_t bclbm_launch_count(void) { return launch_counter().load(); }
+
+int bclbm_footprint(const bclbm_desc* desc, size_t* bytes) {
+    if (!bytes) return BCLBM_ERR_INVALID;
+    Plan p;
+    std::string err;
+    const int rc = validate_and_plan(desc, p, err, false);
+    if (rc) return rc;
+    *bytes = footprint_bytes(desc, p);
+    return BCLBM_OK;
+}
+
+int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
+    if (!out) return BCLBM_ERR_INVALID;
+    *out = nullptr;
+    Plan p;
+    std::string err;
+    int rc = validate_and_plan(d, p, err, true);
+    if (rc) {
+        std::fprintf(stderr, "bclbm_create: %s\n", err.c_str());
+        return rc;
+    }
+    if (!d->f_init) return BCLBM_ERR_INVALID;
+    if (d->collision == BCLBM_RK && !d->rho_init) return BCLBM_ERR_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BCLBM_ERR_NOCUDA;
+    bclbm_handle* h = new (std::nothrow) bclbm_handle();
+    if (!h) return BCLBM_ERR_NOMEM;
+    h->q = d->lattice_q;
+    h->nd = h->q == 9 ? 2 : 3;
+    h->nfields = p.nfields;
+    h->collision = d->collision;
+    h->precision = d->precision;
+    h->flags = d->flags;
+    h->exact = (d->flags & BCLBM_FLAG_EXACT) != 0 || (d->collision == BCLBM_RK && d->precision == BCLBM_F64);
+    h->trt = d->collision == BCLBM_TRT;
+    h->flux = d->collision == BCLBM_RK && d->flux_control != 0;
+    h->n_nodes = d->n_nodes;
+    h->nf = p.nf;
+    h->nf_pad = p.nf_pad;
+    h->ns = p.ns;
+    h->tau[0] = d->tau[0];
+    h->tau[1] = d->collision == BCLBM_BGK ? d->tau[0] : d->tau[1];
+    h->sigma = d->sigma;
+    h->beta = d->beta;
+    h->mom_x = d->mom_x;
+    h->rho_ref = d->rho_ref > 0 ? d->rho_ref : 1.0;
+    h->scale = d->store_scale > 0 ? d->store_scale : (d->precision == BCLBM_F16 ? 4096.0 : 1.0);
+    for (int k = 0; k < 3; ++k) h->force[k] = d->force[k];
+    h->slot_node = std::move(p.slot_node);
+    h->slot_bulk = std::move(p.slot_bulk);
+    h->bulk.assign(d->bulk, d->bulk + d->n_bulk);
+    h->solid_node = std::move(p.solid_node);
+    h->bulk_contiguous = (h->bulk.back() - h->bulk.front() + 1) == d->n_bulk;
+    cudaGetDevice(&h->device);
+
+    const int Q = h->q, D = h->nd, R = Q - 1;
+    const size_t pad = static_cast<size_t>(h->nf_pad);
+    auto cleanup = [&](int code) {
+        free_all(h);
+        delete h;
+        return code;
+    };
+#define CREATE_TRY(expr)                                                                \
+    do {                                                                                \
+        cudaError_t e_ = (expr);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            std::fprintf(stderr, "bclbm_create: %s: %s\n", #expr, cudaGetErrorString(e_)); \
+            return cleanup(e_ == cudaErrorMemoryAllocation ? BCLBM_ERR_NOMEM : BCLBM_ERR_CUDA); \
+        }                                                                               \
+    } while (0)
+
+    // extended neighbour table in device numbering
+    std::vector<int32_t> tab(static_cast<size_t>(R) * pad, static_cast<int32_t>(h->nf + h->ns));
+    for (int s = 0; s < h->nf; ++s) {
+        const size_t n = static_cast<size_t>(h->slot_node[s]);
+        for (int q = 0; q < R; ++q) tab[static_cast<size_t>(q) * pad + s] = p.ext_of_node[d->neigh[n * Q + q]];
+    }
+    // ghost sources: last bulk node (bulk order) whose neighbour along c_p is node 0
+    std::vector<int32_t> slot_of_bulk(h->nf);
+    for (int s = 0; s < h->nf; ++s) slot_of_bulk[h->slot_bulk[s]] = s;
+    for (int pdir = 0; pdir < 19; ++pdir) h->ghost_src[pdir] = 0;
+    for (int pdir = 0; pdir < R; ++pdir)
+        for (int b = h->nf - 1; b >= 0; --b)
+            if (d->neigh[static_cast<size_t>(d->bulk[b]) * Q + pdir] == 0) {
+                h->ghost_src[pdir] = slot_of_bulk[b];
+                break;
+            }
+    CREATE_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    const size_t sb = store_bytes(h->precision);
+    const size_t pop_bytes = static_cast<size_t>(h->nfields) * Q * pad * sb;
+    CREATE_TRY(cudaMalloc(&h->pops[0], pop_bytes));
+    CREATE_TRY(cudaMalloc(&h->pops[1], pop_bytes));
+    CREATE_TRY(cudaMalloc(&h->d_nbr, tab.size() * sizeof(int32_t)));
+    CREATE_TRY(cudaMalloc(&h->d_slot_bulk, pad * sizeof(int32_t)));
+    CREATE_TRY(cudaMalloc(&h->d_rho, static_cast<size_t>(h->nfields) * pad * sizeof(double)));
+    CREATE_TRY(cudaMalloc(&h->d_vel, static_cast<size_t>(D) * pad * sizeof(double)));
+    CREATE_TRY(cudaMalloc(&h->d_params, sizeof(DevParams)));
+    CREATE_TRY(cudaMalloc(&h->d_partials, (static_cast<size_t>(grid_for(h->nf)) * 6 + 64) * sizeof(double)));
+    CREATE_TRY(cudaMalloc(&h->d_red, 16 * sizeof(double)));
+    CREATE_TRY(cudaMemcpyAsync(h->d_nbr, tab.data(), tab.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    CREATE_TRY(cudaMemcpyAsync(h->d_slot_bulk, h->slot_bulk.data(), h->nf * sizeof(int32_t), cudaMemcpyHostToDevice,
+                               h->stream));
+    DevParams prm;
+    for (int k = 0; k < 3; ++k) prm.force[k] = h->force[k];
+    CREATE_TRY(cudaMemcpyAsync(h->d_params, &prm, sizeof(prm), cudaMemcpyHostToDevice, h->stream));
+
+    // colour field: fluid slots (written every step), stored solids (fixed), ghost (0)
+    if (h->collision == BCLBM_RK) {
+        const size_t ncg = static_cast<size_t>(h->nf) + h->ns + 1;
+        CREATE_TRY(cudaMalloc(&h->d_cg, ncg * sizeof(double)));
+        std::vector<double> cg(ncg, 0.0);
+        h->solid_cg.assign(h->ns, 0.0);
+        for (int k = 0; k < h->ns; ++k) {
+            const int n = h->solid_node[k];
+            if (d->types[n] == 1) {  // findSolidBndNodes (main_TWOPHASE.cpp:280-284)
+                const double r0 = d->rho_init[static_cast<size_t>(n) * 2], r1 = d->rho_init[static_cast<size_t>(n) * 2 + 1];
+                h->solid_cg[k] = (r0 - r1) / (r0 + r1);
+            }
+            cg[static_cast<size_t>(h->nf) + k] = h->solid_cg[k];
+        }
+        CREATE_TRY(cudaMemcpyAsync(h->d_cg, cg.data(), ncg * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        CREATE_TRY(cudaStreamSynchronize(h->stream));
+    }
+
+    // initial populations: reference AoS -> FP64 SoA -> storage format
+    {
+        const size_t nsoa = static_cast<size_t>(h->nfields) * Q * pad;
+        std::vector<double> soa(nsoa, 0.0);
+        const int es = h->nfields * Q;
+        for (int s = 0; s < h->nf; ++s) {
+            const size_t n = static_cast<size_t>(h->slot_node[s]);
+            for (int k = 0; k < h->nfields; ++k)
+                for (int q = 0; q < Q; ++q)
+                    soa[(static_cast<size_t>(k) * Q + q) * pad + s] = d->f_init[n * es + static_cast<size_t>(k) * Q + q];
+        }
+        if (h->precision == BCLBM_F64) {
+            CREATE_TRY(cudaMemcpyAsync(h->pops[0], soa.data(), nsoa * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+            CREATE_TRY(cudaStreamSynchronize(h->stream));
+        } else {
+            double* tmp = nullptr;
+            CREATE_TRY(cudaMalloc(&tmp, nsoa * sizeof(double)));
+            cudaError_t e = cudaMemcpyAsync(tmp, soa.data(), nsoa * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+            if (e == cudaSuccess) {
+                k_encode<<<grid_for(h->nf), kBlock, 0, h->stream>>>(tmp, h->pops[0], h->nf, h->nf_pad, Q, h->nfields,
+                                                                    h->precision, h->rho_ref, h->scale);
+                launch_counter()++;
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+            cudaFree(tmp);
+            CREATE_TRY(e);
+        }
+    }
+#undef CREATE_TRY
+    h->cur = 0;
+    h->state_post = false;
+    *out = h;
+    return BCLBM_OK;
+}
+
+int bclbm_step(bclbm_handle* h, int nsteps) {
+    if (!h || nsteps < 0) return BCLBM_ERR_INVALID;
+    if (nsteps == 0) return BCLBM_OK;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    StepArgs a = make_args(h);
+    for (int s = 0; s < nsteps; ++s) {
+        const bool local = !h->state_post;
+        const bool macros = (s == nsteps - 1);
+        a.src = h->pops[h->cur];
+        a.dst = h->pops[1 - h->cur];
+        a.rho_out = macros ? h->d_rho : nullptr;
+        a.vel_out = macros ? h->d_vel : nullptr;
+        if (h->collision != BCLBM_RK) {
+            if (h->exact) CUDA_TRY(h, launch_single_exact(h->q, h->trt, local, a, h->stream));
+            else CUDA_TRY(h, launch_single_fast(h->q, h->precision, h->trt, local, a, h->stream));
+        } else {
+            StepArgs ad = a;
+            ad.rho_out = nullptr;
+            if (h->precision == BCLBM_F64) CUDA_TRY(h, launch_rk_f64(h->q, local, h->flux, ad, h->stream, true));
+            else CUDA_TRY(h, launch_rk_shift(h->q, h->precision, local, h->flux, ad, h->stream, true));
+            if (h->flux) {
+                CUDA_TRY(h, launch_reduce_final(1, h->d_partials, grid_for(h->nf), h->d_red, false, h->stream));
+                CUDA_TRY(h, launch_flux_force(h->d_red, 1.0 / static_cast<double>(h->nf), h->mom_x, h->d_params,
+                                              h->stream));
+            }
+            if (h->precision == BCLBM_F64) CUDA_TRY(h, launch_rk_f64(h->q, local, false, a, h->stream, false));
+            else CUDA_TRY(h, launch_rk_shift(h->q, h->precision, local, false, a, h->stream, false));
+        }
+        h->cur = 1 - h->cur;
+        h->state_post = true;
+    }
+    h->macros_valid = true;
+    h->steps_done += nsteps;
+    return BCLBM_OK;
+}
+
+int bclbm_sync(bclbm_handle* h) {
+    if (!h) return BCLBM_ERR_INVALID;
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return BCLBM_OK;
+}
+
+int bclbm_download_f(bclbm_handle* h, double* f) {
+    if (!h || !f) return BCLBM_ERR_INVALID;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    int rc = run_gather(h);
+    if (rc) return rc;
+    const int es = h->nfields * h->q;
+    const size_t n = static_cast<size_t>(h->nf) * es;
+    if (h->bulk_contiguous) {
+        CUDA_TRY(h, cudaMemcpyAsync(f + static_cast<size_t>(h->bulk.front()) * es, h->d_gather, n * sizeof(double),
+                                    cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    } else {
+        std::vector<double> tmp(n);
+        CUDA_TRY(h, cudaMemcpyAsync(tmp.data(), h->d_gather, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        for (int b = 0; b < h->nf; ++b)
+            std::memcpy(f + static_cast<size_t>(h->bulk[b]) * es, tmp.data() + static_cast<size_t>(b) * es,
+                        es * sizeof(double));
+    }
+    return BCLBM_OK;
+}
+
+int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg) {
+    if (!h) return BCLBM_ERR_INVALID;
+    if (!h->macros_valid) return fail(h, BCLBM_ERR_INVALID, "no step has run yet");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    const size_t pad = static_cast<size_t>(h->nf_pad);
+    std::vector<double> r(static_cast<size_t>(h->nfields) * pad), v(static_cast<size_t>(h->nd) * pad), c;
+    CUDA_TRY(h, cudaMemcpyAsync(r.data(), h->d_rho, r.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(v.data(), h->d_vel, v.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (cg && h->collision == BCLBM_RK) {
+        c.resize(h->nf);
+        CUDA_TRY(h, cudaMemcpyAsync(c.data(), h->d_cg, c.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    for (int s = 0; s < h->nf; ++s) {
+        const size_t n = static_cast<size_t>(h->slot_node[s]);
+        if (rho)
+            for (int k = 0; k < h->nfields; ++k) rho[n * h->nfields + k] = r[k * pad + s];
+        if (vel)
+            for (int dd = 0; dd < h->nd; ++dd) vel[n * h->nd + dd] = v[dd * pad + s];
+        if (cg && h->collision == BCLBM_RK) cg[n] = c[s];
+    }
+    if (cg && h->collision == BCLBM_RK)
+        for (int k = 0; k < h->ns; ++k) cg[h->solid_node[k]] = h->solid_cg[k];
+    return BCLBM_OK;
+}
+
+int bclbm_reduce(bclbm_handle* h, bclbm_stats* out) {
+    if (!h || !out) return BCLBM_ERR_INVALID;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    StepArgs a = make_args(h);
+    a.src = h->pops[h->cur];
+    CUDA_TRY(h, launch_moments(h->q, h->precision, h->nfields, !h->state_post, a, h->stream));
+    CUDA_TRY(h, launch_reduce_final(6, h->d_partials, grid_for(h->nf), h->d_red, true, h->stream));
+    double red[6];
+    DevParams prm;
+    CUDA_TRY(h, cudaMemcpyAsync(red, h->d_red, sizeof(red), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(&prm, h->d_params, sizeof(prm), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    std::memset(out, 0, sizeof(*out));
+    out->mass[0] = red[0];
+    out->mass[1] = red[1];
+    for (int k = 0; k < 3; ++k) {
+        out->flux_fc[k] = red[2 + k];
+        out->momentum[k] = red[2 + k] + 0.5 * prm.force[k] * static_cast<double>(h->nf);
+    }
+    out->saturation = h->collision == BCLBM_RK ? red[0] / (red[0] + red[1]) : 0.0;
+    out->max_abs_f = red[5];
+    out->n_bulk = h->nf;
+    out->steps_done = h->steps_done;
+    out->nonfinite = std::isfinite(red[5]) && std::isfinite(red[0]) && std::isfinite(red[1]) ? 0 : 1;
+    return out->nonfinite ? fail(h, BCLBM_ERR_NONFINITE, "NaN or Inf in the populations") : BCLBM_OK;
+}
+
+int bclbm_set_force(bclbm_handle* h, const double force[3]) {
+    if (!h || !force) return BCLBM_ERR_INVALID;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    DevParams prm;
+    for (int k = 0; k < 3; ++k) prm.force[k] = h->force[k] = force[k];
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_params, &prm, sizeof(prm), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return BCLBM_OK;
+}
+
+int bclbm_node_perm(bclbm_handle* h, int32_t* out) {
+    if (!h || !out) return BCLBM_ERR_INVALID;
+    std::memcpy(out, h->slot_node.data(), h->slot_node.size() * sizeof(int32_t));
+    return BCLBM_OK;
+}
+
+void bclbm_destroy(bclbm_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+}
+
+}  // extern "C"

@@ -1,0 +1,159 @@
+// Restructured FP64 kernels (FMA), FP32-arithmetic kernels for the shifted
+// storage formats, the download gather and the deterministic FP64 reductions.
+#include "bclbm_launch.h"
+
+namespace bclbm {
+
+std::atomic<int64_t>& launch_counter() {
+    static std::atomic<int64_t> n{0};
+    return n;
+}
+
+__global__ void k_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params) {
+    // meanfcXGlobal /= numNodesGlobal; bodyForce.x = 2 * (setMomX - meanfcXGlobal)
+    // (src/twophase/main_TWOPHASE.cpp:301-308)
+    if (threadIdx.x == 0 && blockIdx.x == 0) params->force[0] = 2 * (mom_x - sum[0] * inv_n);
+}
+
+namespace {
+
+template <int Q, class S>
+cudaError_t single_fast_qs(bool trt, bool local, const StepArgs& a, cudaStream_t s) {
+    const int g = grid_for(a.L.nf);
+    if (trt) {
+        if (local) k_single<Q, S, 1, true, true><<<g, kBlock, 0, s>>>(a);
+        else k_single<Q, S, 1, true, false><<<g, kBlock, 0, s>>>(a);
+    } else {
+        if (local) k_single<Q, S, 1, false, true><<<g, kBlock, 0, s>>>(a);
+        else k_single<Q, S, 1, false, false><<<g, kBlock, 0, s>>>(a);
+    }
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+template <int Q>
+cudaError_t single_fast_q(int precision, bool trt, bool local, const StepArgs& a, cudaStream_t s) {
+    switch (precision) {
+        case kF64: return single_fast_qs<Q, double>(trt, local, a, s);
+        case kF32: return single_fast_qs<Q, float>(trt, local, a, s);
+        case kF16: return single_fast_qs<Q, __half>(trt, local, a, s);
+        case kBF16: return single_fast_qs<Q, __nv_bfloat16>(trt, local, a, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <int Q, class S>
+cudaError_t rk_shift_qs(bool local, bool flux, const StepArgs& a, cudaStream_t s, bool density) {
+    const int g = grid_for(a.L.nf);
+    if (density) {
+        if (local) {
+            if (flux) k_rk_density<Q, S, true, true><<<g, kBlock, 0, s>>>(a);
+            else k_rk_density<Q, S, true, false><<<g, kBlock, 0, s>>>(a);
+        } else {
+            if (flux) k_rk_density<Q, S, false, true><<<g, kBlock, 0, s>>>(a);
+            else k_rk_density<Q, S, false, false><<<g, kBlock, 0, s>>>(a);
+        }
+    } else {
+        if (local) k_rk_collide_shift<Q, S, true><<<g, kBlock, 0, s>>>(a);
+        else k_rk_collide_shift<Q, S, false><<<g, kBlock, 0, s>>>(a);
+    }
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+template <int Q>
+cudaError_t rk_shift_q(int precision, bool local, bool flux, const StepArgs& a, cudaStream_t s, bool density) {
+    switch (precision) {
+        case kF32: return rk_shift_qs<Q, float>(local, flux, a, s, density);
+        case kF16: return rk_shift_qs<Q, __half>(local, flux, a, s, density);
+        case kBF16: return rk_shift_qs<Q, __nv_bfloat16>(local, flux, a, s, density);
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <int Q, class S>
+cudaError_t gather_qs(int nfields, bool local, const StepArgs& a, const int32_t* sb, double* out, cudaStream_t s) {
+    const int g = grid_for(a.L.nf);
+    if (nfields == 1) {
+        if (local) k_gather<Q, S, 1, true><<<g, kBlock, 0, s>>>(a, sb, out);
+        else k_gather<Q, S, 1, false><<<g, kBlock, 0, s>>>(a, sb, out);
+    } else {
+        if (local) k_gather<Q, S, 2, true><<<g, kBlock, 0, s>>>(a, sb, out);
+        else k_gather<Q, S, 2, false><<<g, kBlock, 0, s>>>(a, sb, out);
+    }
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+template <int Q, class S>
+cudaError_t moments_qs(int nfields, bool local, const StepArgs& a, cudaStream_t s) {
+    const int g = grid_for(a.L.nf);
+    if (nfields == 1) {
+        if (local) k_moments<Q, S, 1, true><<<g, kBlock, 0, s>>>(a);
+        else k_moments<Q, S, 1, false><<<g, kBlock, 0, s>>>(a);
+    } else {
+        if (local) k_moments<Q, S, 2, true><<<g, kBlock, 0, s>>>(a);
+        else k_moments<Q, S, 2, false><<<g, kBlock, 0, s>>>(a);
+    }
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+#define BCLBM_BY_PRECISION(FN, Q, ...)                                   \
+    switch (precision) {                                                 \
+        case kF64: return FN<Q, double>(__VA_ARGS__);                    \
+        case kF32: return FN<Q, float>(__VA_ARGS__);                     \
+        case kF16: return FN<Q, __half>(__VA_ARGS__);                    \
+        case kBF16: return FN<Q, __nv_bfloat16>(__VA_ARGS__);            \
+    }                                                                    \
+    return cudaErrorInvalidValue;
+
+template <int Q>
+cudaError_t gather_q(int precision, int nfields, bool local, const StepArgs& a, const int32_t* sb, double* out,
+                     cudaStream_t s) {
+    BCLBM_BY_PRECISION(gather_qs, Q, nfields, local, a, sb, out, s)
+}
+
+template <int Q>
+cudaError_t moments_q(int precision, int nfields, bool local, const StepArgs& a, cudaStream_t s) {
+    BCLBM_BY_PRECISION(moments_qs, Q, nfields, local, a, s)
+}
+
+}  // namespace
+
+cudaError_t launch_single_fast(int Q, int precision, bool trt, bool local, const StepArgs& a, cudaStream_t s) {
+    return Q == 9 ? single_fast_q<9>(precision, trt, local, a, s) : single_fast_q<19>(precision, trt, local, a, s);
+}
+
+cudaError_t launch_rk_shift(int Q, int precision, bool local, bool flux, const StepArgs& a, cudaStream_t s,
+                            bool density) {
+    return Q == 9 ? rk_shift_q<9>(precision, local, flux, a, s, density)
+                  : rk_shift_q<19>(precision, local, flux, a, s, density);
+}
+
+cudaError_t launch_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params, cudaStream_t s) {
+    k_flux_force<<<1, 32, 0, s>>>(sum, inv_n, mom_x, params);
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather(int Q, int precision, int nfields, bool local, const StepArgs& a, const int32_t* slot_bulk,
+                          double* out, cudaStream_t s) {
+    return Q == 9 ? gather_q<9>(precision, nfields, local, a, slot_bulk, out, s)
+                  : gather_q<19>(precision, nfields, local, a, slot_bulk, out, s);
+}
+
+cudaError_t launch_moments(int Q, int precision, int nfields, bool local, const StepArgs& a, cudaStream_t s) {
+    return Q == 9 ? moments_q<9>(precision, nfields, local, a, s) : moments_q<19>(precision, nfields, local, a, s);
+}
+
+cudaError_t launch_reduce_final(int nv, const double* partials, int nblocks, double* out, bool max_last,
+                                cudaStream_t s) {
+    if (nv == 1) k_reduce_final<1><<<1, kBlock, 0, s>>>(partials, nblocks, out, max_last ? 1 : 0);
+    else if (nv == 6) k_reduce_final<6><<<1, kBlock, 0, s>>>(partials, nblocks, out, max_last ? 1 : 0);
+    else return cudaErrorInvalidValue;
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+}  // namespace bclbm

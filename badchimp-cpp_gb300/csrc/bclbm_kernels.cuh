@@ -1,0 +1,720 @@
+// Kernel templates of the bclbm time step.  Included by bclbm_exact.cu
+// (compiled with -fmad=false; the FP64 kernels that follow the reference's
+// expression order) and by bclbm_kernels.cu (everything else).
+//
+// One thread owns one fluid slot.  A step kernel pulls the Q populations that
+// stream into its slot (bounce-back fused, see bclbm_device.cuh), computes the
+// moments, collides, and writes the post-collision populations to its own
+// slot of the other buffer: reads are gathers along the neighbour table,
+// writes are fully coalesced rows.  The device state is therefore the
+// post-collision field G of the last step; the reference's f (post-stream,
+// post-bounce-back) is one pull of G away and is produced by k_gather on
+// download.  The first step after create reads the uploaded f directly
+// (LOCAL = true).
+#pragma once
+
+#include <math_constants.h>
+#include <type_traits>
+
+#include "bclbm_device.cuh"
+
+namespace bclbm {
+
+constexpr int kBlock = 256;
+constexpr double C2 = 1.0 / 3.0;  // DXQY::c2 = 1.0 / c2Inv
+
+struct DevParams {
+    double force[3];
+};
+
+struct StepArgs {
+    LatticeView L;
+    const void* src;        // state read by this step (G, or f when LOCAL)
+    void* dst;              // post-collision output
+    double* rho_out;        // [nfields][nf_pad] when MACROS
+    double* vel_out;        // [D][nf_pad] when MACROS
+    double* cg;             // RK: colour of [nf fluid | ns solids | ghost]
+    const DevParams* params;
+    double tau, tau_anti;   // single phase: relaxation times; RK: unused
+    double tau_inv, tf;     // exact single phase: 1/tau, 1 - 0.5/tau (host-computed like the reference)
+    double tauA_inv, taf;   // exact TRT: 1/tau_anti, 1 - 0.5/tau_anti
+    double nu0inv, nu1inv;  // RK
+    double sigma, beta;     // RK
+    double rho_ref;         // shifted storage reference density
+    double scale, inv_scale;// shifted storage scale
+    double* partials;       // per-block partial sums (flux controller)
+    int n_bulk;             // RK flux controller divisor
+};
+
+// ---------------------------------------------------------------------------
+// Reference-order helpers (exact mode).  Each mirrors one reference function
+// term by term; C++ evaluates a + b - c as (a + b) - c, as the reference does.
+// ---------------------------------------------------------------------------
+template <int Q>
+__device__ __forceinline__ void qsumc_ref(const double* d, double* r) {  // qSumC
+    if constexpr (Q == 9) {  // LBd2q9.h:170-177
+        r[0] = +d[0] + d[1] - d[3] - d[4] - d[5] + d[7];
+        r[1] = +d[1] + d[2] + d[3] - d[5] - d[6] - d[7];
+    } else {  // LBd3q19.h:182-190
+        r[0] = +d[0] + d[3] + d[4] + d[5] + d[6] - d[9] - d[12] - d[13] - d[14] - d[15];
+        r[1] = +d[1] + d[3] - d[4] + d[7] + d[8] - d[10] - d[12] + d[13] - d[16] - d[17];
+        r[2] = +d[2] + d[5] - d[6] + d[7] - d[8] - d[11] - d[14] + d[15] - d[16] + d[17];
+    }
+}
+
+template <int Q>
+__device__ __forceinline__ void cdotall_ref(const double* v, double* r) {  // cDotAll
+    if constexpr (Q == 9) {  // LBd2q9.h:128-142
+        r[0] = +v[0];
+        r[1] = +v[0] + v[1];
+        r[2] = +v[1];
+        r[3] = -v[0] + v[1];
+        r[4] = -v[0];
+        r[5] = -v[0] - v[1];
+        r[6] = -v[1];
+        r[7] = +v[0] - v[1];
+        r[8] = 0.0;
+    } else {  // LBd3q19.h:129-153
+        r[0] = +v[0];
+        r[1] = +v[1];
+        r[2] = +v[2];
+        r[3] = +v[0] + v[1];
+        r[4] = +v[0] - v[1];
+        r[5] = +v[0] + v[2];
+        r[6] = +v[0] - v[2];
+        r[7] = +v[1] + v[2];
+        r[8] = +v[1] - v[2];
+        r[9] = -v[0];
+        r[10] = -v[1];
+        r[11] = -v[2];
+        r[12] = -v[0] - v[1];
+        r[13] = -v[0] + v[1];
+        r[14] = -v[0] - v[2];
+        r[15] = -v[0] + v[2];
+        r[16] = -v[1] - v[2];
+        r[17] = -v[1] + v[2];
+        r[18] = 0.0;
+    }
+}
+
+template <int Q>
+__device__ __forceinline__ double dot_ref(const double* a, const double* b) {  // DXQY::dot
+    if constexpr (Q == 9) return a[0] * b[0] + a[1] * b[1];
+    else return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+template <int Q>
+__device__ __forceinline__ void grad_ref(const double* s, double* r) {  // DXQY::grad
+    constexpr double a = Lat<Q>::w1c2inv, b = Lat<Q>::w2c2inv;
+    if constexpr (Q == 9) {  // LBd2q9.h:144-151
+        r[0] = +a * (+s[0] - s[4]) + b * (+s[1] - s[3] - s[5] + s[7]);
+        r[1] = +a * (+s[2] - s[6]) + b * (+s[1] + s[3] - s[5] - s[7]);
+    } else {  // LBd3q19.h:155-163
+        r[0] = +a * (+s[0] - s[9]) + b * (+s[3] + s[4] + s[5] + s[6] - s[12] - s[13] - s[14] - s[15]);
+        r[1] = +a * (+s[1] - s[10]) + b * (+s[3] - s[4] + s[7] + s[8] - s[12] + s[13] - s[16] - s[17]);
+        r[2] = +a * (+s[2] - s[11]) + b * (+s[5] - s[6] + s[7] - s[8] - s[14] + s[15] - s[16] + s[17]);
+    }
+}
+
+__device__ __forceinline__ double cnorm_ref(int wclass) {  // DXQY::cNorm (SQRT2, LBglobal.h:11)
+    return wclass == 1 ? 1.0 : 1.4142135623730950488;
+}
+
+// ---------------------------------------------------------------------------
+// Population access
+// ---------------------------------------------------------------------------
+template <int Q, class S, bool LOCAL>
+__device__ __forceinline__ void load_field(const S* __restrict__ g, const LatticeView& L, int i,
+                                           typename Store<S>::T* v) {
+    constexpr int R = Lat<Q>::REST;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if (q == R || LOCAL) {
+            v[q] = g[static_cast<size_t>(q) * L.nf_pad + i];
+        } else {
+            const int y = __ldg(L.nbr + static_cast<size_t>(Lat<Q>::rev(q)) * L.nf_pad + i);
+            v[q] = pull_raw<Q, S>(g, L, q, y, i);
+        }
+    }
+}
+
+// Converts raw stored values to the compute representation: f itself (F64),
+// or the deviation f - w rho_ref (shifted formats).
+template <int Q, class S, class C>
+__device__ __forceinline__ void decode(const typename Store<S>::T* v, C* f, C inv_scale) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if constexpr (Store<S>::shifted) f[q] = static_cast<C>(Store<S>::val(v[q])) * (static_cast<C>(Lat<Q>::w(q)) * inv_scale);
+        else f[q] = static_cast<C>(v[q]);
+    }
+}
+
+template <int Q, class S, class C>
+__device__ __forceinline__ void encode_store(S* __restrict__ out, size_t nf_pad, int i, const C* f, C scale) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if constexpr (Store<S>::shifted) Store<S>::store(out + q * nf_pad + i, static_cast<float>(f[q] * (scale / static_cast<C>(Lat<Q>::w(q)))));
+        else out[q * nf_pad + i] = static_cast<double>(f[q]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Single-phase collision, exact reference order (std_case/main.cpp:112-133)
+// ---------------------------------------------------------------------------
+template <int Q, bool TRT>
+__device__ __forceinline__ void collide_exact(double* f, const double* F, const StepArgs& a, double& rho_o,
+                                              double* vel_o) {
+    constexpr int D = Lat<Q>::D;
+    double rho = 0.0;  // calcRho -> qSum
+#pragma unroll
+    for (int q = 0; q < Q; ++q) rho += f[q];
+    double j[D], vel[D];
+    qsumc_ref<Q>(f, j);
+#pragma unroll
+    for (int d = 0; d < D; ++d) vel[d] = (j[d] + 0.5 * F[d]) / rho;  // calcVel (LBmacroscopic.h:85)
+    rho_o = rho;
+#pragma unroll
+    for (int d = 0; d < D; ++d) vel_o[d] = vel[d];
+    const double u2 = dot_ref<Q>(vel, vel);
+    double cu[Q], cF[Q];
+    cdotall_ref<Q>(vel, cu);
+    const double uF = dot_ref<Q>(vel, F);
+    cdotall_ref<Q>(F, cF);
+    double post[Q];
+    if constexpr (!TRT) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {  // calcOmegaBGK (LBcollision.h:43), calcDeltaOmegaF (:210)
+            const double w = Lat<Q>::w(q);
+            const double om = -a.tau_inv * (f[q] - rho * w * (1.0 + 3.0 * cu[q] + 4.5 * (cu[q] * cu[q] - C2 * u2)));
+            const double dF = w * a.tf * (3.0 * cF[q] + 9.0 * (cF[q] * cu[q] - C2 * uF));
+            post[q] = f[q] + om + dF;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {  // calcOmegaBGKTRT (LBcollision.h:68-72), calcDeltaOmegaFTRT (:233)
+            const double w = Lat<Q>::w(q);
+            const int r = Lat<Q>::rev(q);
+            const double fs = 0.5 * (f[q] + f[r]);
+            const double fa = 0.5 * (f[q] - f[r]);
+            const double om = -a.tau_inv * (fs - rho * w * (1.0 + 4.5 * (cu[q] * cu[q] - C2 * u2))) -
+                              a.tauA_inv * (fa - rho * w * 3.0 * cu[q]);
+            const double dF = w * 1.0 * (a.taf * 3.0 * cF[q] + a.tf * 9.0 * (cF[q] * cu[q] - C2 * uF));
+            post[q] = f[q] + om + dF;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[q] = post[q];
+}
+
+// ---------------------------------------------------------------------------
+// Single-phase collision, restructured (FMA) in compute type C.
+// SHIFT: f holds deviations f - w rho_ref.  BGK is TRT with equal rates.
+// post_q  = al f_q + be f_rq + X + Y,  post_rq = al f_rq + be f_q + X - Y
+// X = oms w (rho (1 + 4.5 cu^2 - 1.5 u^2) [shifted: rho' + rho(4.5cu^2 - 1.5u^2)]) + w tsf (9 cF cu - 3 uF)
+// Y = oma 3 w rho cu + 3 w taf cF
+// al = 1 - (oms + oma)/2, be = (oma - oms)/2; the sums are the reference's
+// calcOmegaBGK(TRT) + calcDeltaOmegaF(TRT) regrouped by direction pairs.
+// ---------------------------------------------------------------------------
+template <int Q, class C, bool TRT, bool SHIFT>
+__device__ __forceinline__ void collide_fast(C* f, const C* F, C oms, C oma, C tsf, C taf, C rho_ref, C& rho_o,
+                                             C* vel_o) {
+    constexpr int D = Lat<Q>::D, NP = Lat<Q>::NP, R = Lat<Q>::REST;
+    C p[NP], m[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        p[k] = f[k] + f[k + NP];
+        m[k] = f[k] - f[k + NP];
+    }
+    C rs = f[R];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) rs += p[k];
+    C j[3] = {C(0), C(0), C(0)};
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        if (Lat<Q>::cx(k) > 0) j[0] += m[k];
+        if (Lat<Q>::cx(k) < 0) j[0] -= m[k];
+        if (Lat<Q>::cy(k) > 0) j[1] += m[k];
+        if (Lat<Q>::cy(k) < 0) j[1] -= m[k];
+        if (D == 3 && Lat<Q>::cz(k) > 0) j[2] += m[k];
+        if (D == 3 && Lat<Q>::cz(k) < 0) j[2] -= m[k];
+    }
+    const C rho = SHIFT ? rho_ref + rs : rs;  // rs is rho' when shifted
+    const C inv = C(1) / rho;
+    C u[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) u[d] = (d < D) ? (j[d] + C(0.5) * F[d]) * inv : C(0);
+    rho_o = rho;
+#pragma unroll
+    for (int d = 0; d < D; ++d) vel_o[d] = u[d];
+    const C u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    const C uF = u[0] * F[0] + u[1] * F[1] + u[2] * F[2];
+    const C base = SHIFT ? C(-1.5) * u2 : C(1) - C(1.5) * u2;
+    const C al = C(1) - C(0.5) * (oms + oma);
+    const C be = C(0.5) * (oma - oms);
+    // per weight class constants (0 rest, 1 axis, 2 diagonal)
+    C Aw[3], Bw[3], Kw[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const C w = static_cast<C>(c == 0 ? Lat<Q>::w(R) : (c == 1 ? Lat<Q>::w(0) : Lat<Q>::w(NP - 1)));
+        Aw[c] = oms * rho * w;
+        Bw[c] = C(3) * oma * rho * w;
+        Kw[c] = C(-3) * w * tsf * uF + (SHIFT ? oms * w * rs : C(0));
+    }
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const int c = Lat<Q>::wclass(k);
+        const C w = static_cast<C>(Lat<Q>::w(k));
+        const C cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];
+        const C cF = Lat<Q>::cx(k) * F[0] + Lat<Q>::cy(k) * F[1] + Lat<Q>::cz(k) * F[2];
+        const C X = Aw[c] * (C(4.5) * cu * cu + base) + ((C(9) * w * tsf * cF) * cu + Kw[c]);
+        const C Y = Bw[c] * cu + C(3) * w * taf * cF;
+        const C fq = f[k], fr = f[k + NP];
+        if constexpr (TRT) {
+            f[k] = al * fq + (be * fr + (X + Y));
+            f[k + NP] = al * fr + (be * fq + (X - Y));
+        } else {
+            f[k] = al * fq + (X + Y);
+            f[k + NP] = al * fr + (X - Y);
+        }
+    }
+    f[R] = (C(1) - oms) * f[R] + (Aw[0] * base + Kw[0]);
+}
+
+// ---------------------------------------------------------------------------
+// k_single: one single-phase time step.
+// MODE 0: exact reference order (F64, instantiated in the -fmad=false unit)
+// MODE 1: restructured, compute in double (F64) or float (shifted formats)
+// ---------------------------------------------------------------------------
+template <int Q, class S, int MODE, bool TRT, bool LOCAL>
+__global__ void __launch_bounds__(kBlock) k_single(StepArgs a) {
+    const bool MACROS = a.rho_out != nullptr;
+    constexpr int D = Lat<Q>::D;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.L.nf) return;
+    using T = typename Store<S>::T;
+    T v[Q];
+    load_field<Q, S, LOCAL>(static_cast<const S*>(a.src), a.L, i, v);
+    S* out = static_cast<S*>(a.dst);
+    if constexpr (MODE == 0) {
+        double f[Q], F[3], rho, vel[3];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) f[q] = v[q];
+        F[0] = a.params->force[0];
+        F[1] = a.params->force[1];
+        F[2] = a.params->force[2];
+        collide_exact<Q, TRT>(f, F, a, rho, vel);
+        if (MACROS) {
+            a.rho_out[i] = rho;
+#pragma unroll
+            for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * a.L.nf_pad + i] = vel[d];
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q) out[static_cast<size_t>(q) * a.L.nf_pad + i] = f[q];
+    } else {
+        using C = typename std::conditional<std::is_same<S, double>::value, double, float>::type;
+        C f[Q], F[3], rho, vel[3];
+        decode<Q, S, C>(v, f, static_cast<C>(a.inv_scale));
+        F[0] = static_cast<C>(a.params->force[0]);
+        F[1] = static_cast<C>(a.params->force[1]);
+        F[2] = static_cast<C>(a.params->force[2]);
+        const C oms = static_cast<C>(a.tau_inv), oma = static_cast<C>(TRT ? a.tauA_inv : a.tau_inv);
+        const C tsf = static_cast<C>(a.tf), taf = static_cast<C>(TRT ? a.taf : a.tf);
+        collide_fast<Q, C, TRT, Store<S>::shifted>(f, F, oms, oma, tsf, taf, static_cast<C>(a.rho_ref), rho, vel);
+        if (MACROS) {
+            a.rho_out[i] = static_cast<double>(rho);
+#pragma unroll
+            for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * a.L.nf_pad + i] = static_cast<double>(vel[d]);
+        }
+        encode_store<Q, S, C>(out, a.L.nf_pad, i, f, static_cast<C>(a.scale));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic block reduction of NV doubles (fixed shuffle tree + fixed
+// warp order); thread 0 writes partials[blockIdx.x * NV + k].
+// ---------------------------------------------------------------------------
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double* vals, double* partials, bool max_last) {
+    __shared__ double sh[kBlock / 32][NV];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double v = vals[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double t = __shfl_down_sync(0xffffffffu, v, o);
+            v = (max_last && k == NV - 1) ? fmax(v, t) : v + t;
+        }
+        if (lane == 0) sh[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = sh[0][k];
+            for (int w = 1; w < kBlock / 32; ++w) s = (max_last && k == NV - 1) ? fmax(s, sh[w][k]) : s + sh[w][k];
+            partials[static_cast<size_t>(blockIdx.x) * NV + k] = s;
+        }
+    }
+}
+
+// Sums nblocks rows of NV partials in block order with one block; result to out[NV].
+template <int NV>
+__global__ void __launch_bounds__(kBlock) k_reduce_final(const double* __restrict__ partials, int nblocks,
+                                                        double* out, int max_last) {
+    __shared__ double sh[kBlock][NV];
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+    // thread t sums blocks t, t+256, ... in order
+    for (int b = threadIdx.x; b < nblocks; b += kBlock) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const double v = partials[static_cast<size_t>(b) * NV + k];
+            acc[k] = (max_last && k == NV - 1) ? fmax(acc[k], v) : acc[k] + v;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[threadIdx.x][k] = acc[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NV; ++k) {
+            double s = sh[0][k];
+            for (int t = 1; t < kBlock; ++t) s = (max_last && k == NV - 1) ? fmax(s, sh[t][k]) : s + sh[t][k];
+            out[k] = s;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Two-phase (Rothman-Keller) storage.
+// F64: field 0 = f0, field 1 = f1 (the reference's two LbField fields).
+// Shifted formats: field 0 = total deviation ft - w rho_ref, field 1 = the
+// colour difference (f0 - f1); both weight-normalised and scaled.  f0 and f1
+// are (ft +- (f0 - f1)) / 2.  The total carries the flow with the FP16 mantissa
+// spent on the velocity signal; the colour difference is bounded by w.
+// ---------------------------------------------------------------------------
+template <int Q, class S, bool LOCAL>
+__device__ __forceinline__ void load_rk(const S* __restrict__ g, const LatticeView& L, int i, double* f0,
+                                        double* f1, double rho_ref, double inv_scale) {
+    using T = typename Store<S>::T;
+    T v0[Q], v1[Q];
+    const size_t fs = static_cast<size_t>(Q) * L.nf_pad;
+    load_field<Q, S, LOCAL>(g, L, i, v0);
+    load_field<Q, S, LOCAL>(g + fs, L, i, v1);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if constexpr (Store<S>::shifted) {
+            const double w = Lat<Q>::w(q);
+            const double ft = w * (rho_ref + static_cast<double>(Store<S>::val(v0[q])) * inv_scale);
+            const double dc = w * (static_cast<double>(Store<S>::val(v1[q])) * inv_scale);
+            f0[q] = 0.5 * (ft + dc);
+            f1[q] = 0.5 * (ft - dc);
+        } else {
+            f0[q] = v0[q];
+            f1[q] = v1[q];
+        }
+    }
+}
+
+// PASS 1 (main_TWOPHASE.cpp:238-246): densities, colour field; FLUX adds the
+// per-block sums of qSumC(f0 + f1)[0] for the flux controller (:292-298).
+template <int Q, class S, bool LOCAL, bool FLUX>
+__global__ void __launch_bounds__(kBlock) k_rk_density(StepArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double fx = 0.0;
+    if (i < a.L.nf) {
+        using T = typename Store<S>::T;
+        const S* g = static_cast<const S*>(a.src);
+        if constexpr (!Store<S>::shifted) {
+            T v0[Q], v1[Q];
+            const size_t fs = static_cast<size_t>(Q) * a.L.nf_pad;
+            load_field<Q, S, LOCAL>(g, a.L, i, v0);
+            load_field<Q, S, LOCAL>(g + fs, a.L, i, v1);
+            double r0 = 0.0, r1 = 0.0;
+#pragma unroll
+            for (int q = 0; q < Q; ++q) r0 += v0[q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) r1 += v1[q];
+            a.cg[i] = (r0 - r1) / (r0 + r1);
+            if (FLUX) {
+                double ft[Q], j[3];
+#pragma unroll
+                for (int q = 0; q < Q; ++q) ft[q] = v0[q] + v1[q];
+                qsumc_ref<Q>(ft, j);
+                fx = j[0];
+            }
+        } else {
+            T v0[Q], v1[Q];
+            const size_t fs = static_cast<size_t>(Q) * a.L.nf_pad;
+            load_field<Q, S, LOCAL>(g, a.L, i, v0);
+            load_field<Q, S, LOCAL>(g + fs, a.L, i, v1);
+            float rs = 0.f, dr = 0.f, jx = 0.f;
+            const float isc = static_cast<float>(a.inv_scale);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const float w = static_cast<float>(Lat<Q>::w(q));
+                const float t = Store<S>::val(v0[q]) * (w * isc);
+                rs += t;
+                dr += Store<S>::val(v1[q]) * (w * isc);
+                jx += Lat<Q>::cx(q) * t;
+            }
+            const float rho = static_cast<float>(a.rho_ref) + rs;
+            a.cg[i] = static_cast<double>(dr / rho);
+            fx = jx;
+        }
+    }
+    if constexpr (FLUX) {
+        double vals[1] = {fx};
+        block_reduce_store<1>(vals, a.partials, false);
+    }
+}
+
+// Flux controller (main_TWOPHASE.cpp:301-308): force_x = 2 (mom_x - mean).
+__global__ void k_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params);
+
+// PASS 2 (main_TWOPHASE.cpp:312-376): RK collision, perturbation and
+// recolouring of F64 populations, in the reference's expression order.
+template <int Q, bool LOCAL>
+__global__ void __launch_bounds__(kBlock) k_rk_collide_f64(StepArgs a) {
+    const bool MACROS = a.rho_out != nullptr;
+    constexpr int D = Lat<Q>::D, R = Lat<Q>::REST;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.L.nf) return;
+    double f0[Q], f1[Q];
+    load_rk<Q, double, LOCAL>(static_cast<const double*>(a.src), a.L, i, f0, f1, a.rho_ref, a.inv_scale);
+    // colour at the downstream neighbours (grad, LButilities.h:12-22)
+    double sc[Q];
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) sc[q] = a.cg[__ldg(a.L.nbr + static_cast<size_t>(q) * a.L.nf_pad + i)];
+    sc[R] = a.cg[i];
+    const double F[3] = {a.params->force[0], a.params->force[1], a.params->force[2]};
+    double ft[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) ft[q] = f0[q] + f1[q];
+    double rho0 = 0.0, rho1 = 0.0;  // pass-1 densities, recomputed from the same populations
+#pragma unroll
+    for (int q = 0; q < Q; ++q) rho0 += f0[q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) rho1 += f1[q];
+    const double rho = rho0 + rho1;
+    double j[3] = {0.0, 0.0, 0.0}, vel[3] = {0.0, 0.0, 0.0};
+    qsumc_ref<Q>(ft, j);
+#pragma unroll
+    for (int d = 0; d < D; ++d) vel[d] = (j[d] + 0.5 * F[d]) / rho;
+    const double q0 = 0.0, q1 = 0.0;  // mass sources are zero (main_TWOPHASE.cpp:132-136)
+    rho0 += 0.5 * q0;
+    rho1 += 0.5 * q1;
+    const double tau = 3.0 * rho / (rho0 * a.nu0inv + rho1 * a.nu1inv) + 0.5;
+    const double uu = dot_ref<Q>(vel, vel);
+    double cu[Q], cF[Q];
+    cdotall_ref<Q>(vel, cu);
+    const double tau_inv = 1.0 / tau;
+    const double uF = dot_ref<Q>(vel, F);
+    cdotall_ref<Q>(F, cF);
+    const double tf = (1 - 0.5 / tau);
+    double G[3] = {0.0, 0.0, 0.0};
+    grad_ref<Q>(sc, G);
+    const double cgn = sqrt(dot_ref<Q>(G, G));
+    const double gs = 1.0 / (cgn + static_cast<double>(cgn < 2.220446049250313080847e-16));
+#pragma unroll
+    for (int d = 0; d < D; ++d) G[d] *= gs;
+    double cn[Q];
+    cdotall_ref<Q>(G, cn);
+    const double af = 1.125 * cgn * a.sigma / tau;  // calcDeltaOmegaST (LBcollision2phase.h:11)
+    const double rfb = a.beta * rho0 * rho1 / rho;  // calcDeltaOmegaRC (LBcollision2phase.h:74)
+    const double c0 = (rho0 / rho);
+    const double c1 = (rho1 / rho);
+    if (MACROS) {
+        a.rho_out[i] = rho0;
+        a.rho_out[static_cast<size_t>(a.L.nf_pad) + i] = rho1;
+#pragma unroll
+        for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * a.L.nf_pad + i] = vel[d];
+    }
+    double* out = static_cast<double*>(a.dst);
+    const size_t fs = static_cast<size_t>(Q) * a.L.nf_pad;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const double w = Lat<Q>::w(q);
+        const double om = -tau_inv * (ft[q] - rho * w * (1.0 + 3.0 * cu[q] + 4.5 * (cu[q] * cu[q] - C2 * uu)));
+        const double dF = w * tf * (3.0 * cF[q] + 9.0 * (cF[q] * cu[q] - C2 * uF));
+        const double e = (1.0 + 3.0 * cu[q] + 4.5 * (cu[q] * cu[q] - C2 * uu));
+        const double dQ0 = tf * q0 * w * e;
+        const double dQ1 = tf * q1 * w * e;
+        const double dST = (q == R) ? -af * Lat<Q>::B(q) : af * (w * cn[q] * cn[q] - Lat<Q>::B(q));
+        const double dRC = (q == R) ? 0.0 : rfb * w * cn[q] / cnorm_ref(Lat<Q>::wclass(q));
+        out[q * a.L.nf_pad + i] = c0 * (ft[q] + om + dF + dST) + dRC + dQ0;
+        out[fs + q * a.L.nf_pad + i] = c1 * (ft[q] + om + dF + dST) - dRC + dQ1;
+    }
+}
+
+// PASS 2 for the shifted formats, FP32 arithmetic on (total deviation ft',
+// colour difference dc).  With X_q the reference's
+// fTot + omegaBGK + deltaOmegaF + deltaOmegaST, the two outputs
+// c0 X + RC and c1 X - RC become  ft'_post = X - w rho_ref  and
+// dc_post = (c0 - c1) X + 2 RC.
+template <int Q, class S, bool LOCAL>
+__global__ void __launch_bounds__(kBlock) k_rk_collide_shift(StepArgs a) {
+    const bool MACROS = a.rho_out != nullptr;
+    constexpr int D = Lat<Q>::D, R = Lat<Q>::REST;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.L.nf) return;
+    using T = typename Store<S>::T;
+    const S* g = static_cast<const S*>(a.src);
+    const size_t fs = static_cast<size_t>(Q) * a.L.nf_pad;
+    T v0[Q], v1[Q];
+    load_field<Q, S, LOCAL>(g, a.L, i, v0);
+    load_field<Q, S, LOCAL>(g + fs, a.L, i, v1);
+    float sc[Q];
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) sc[q] = static_cast<float>(a.cg[__ldg(a.L.nbr + static_cast<size_t>(q) * a.L.nf_pad + i)]);
+    sc[R] = 0.f;
+    const float isc = static_cast<float>(a.inv_scale);
+    float ft[Q], dc[Q];
+    float rs = 0.f, dr = 0.f, j[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const float ws = static_cast<float>(Lat<Q>::w(q)) * isc;
+        ft[q] = Store<S>::val(v0[q]) * ws;
+        dc[q] = Store<S>::val(v1[q]) * ws;
+        rs += ft[q];
+        dr += dc[q];
+        j[0] += Lat<Q>::cx(q) * ft[q];
+        j[1] += Lat<Q>::cy(q) * ft[q];
+        j[2] += Lat<Q>::cz(q) * ft[q];
+    }
+    const float F[3] = {static_cast<float>(a.params->force[0]), static_cast<float>(a.params->force[1]),
+                        static_cast<float>(a.params->force[2])};
+    const float rho_ref = static_cast<float>(a.rho_ref);
+    const float rho = rho_ref + rs;
+    const float inv = 1.f / rho;
+    const float rho0 = 0.5f * (rho + dr), rho1 = 0.5f * (rho - dr);
+    float u[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) u[d] = (d < D) ? (j[d] + 0.5f * F[d]) * inv : 0.f;
+    const float om = 1.f / (3.f * rho / (rho0 * static_cast<float>(a.nu0inv) + rho1 * static_cast<float>(a.nu1inv)) + 0.5f);
+    const float tf = 1.f - 0.5f * om;
+    const float uu = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    const float uF = u[0] * F[0] + u[1] * F[1] + u[2] * F[2];
+    float G[3] = {0.f, 0.f, 0.f};
+    {
+        constexpr float ga = static_cast<float>(Lat<Q>::w1c2inv), gb = static_cast<float>(Lat<Q>::w2c2inv);
+#pragma unroll
+        for (int q = 0; q < Q - 1; ++q) {
+            const float wq = Lat<Q>::wclass(q) == 1 ? ga : gb;
+            G[0] += (wq * Lat<Q>::cx(q)) * sc[q];
+            G[1] += (wq * Lat<Q>::cy(q)) * sc[q];
+            G[2] += (wq * Lat<Q>::cz(q)) * sc[q];
+        }
+    }
+    const float cgn = sqrtf(G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
+    const float gs = 1.f / (cgn + (cgn < 1.1920929e-07f ? 1.f : 0.f));
+    const float af = 1.125f * cgn * static_cast<float>(a.sigma) * om;
+    const float rfb = static_cast<float>(a.beta) * rho0 * rho1 * inv;
+    const float dcf = dr * inv;  // c0 - c1
+    const float sc_out = static_cast<float>(a.scale);
+    S* out = static_cast<S*>(a.dst);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const float w = static_cast<float>(Lat<Q>::w(q));
+        const float cu = Lat<Q>::cx(q) * u[0] + Lat<Q>::cy(q) * u[1] + Lat<Q>::cz(q) * u[2];
+        const float cF = Lat<Q>::cx(q) * F[0] + Lat<Q>::cy(q) * F[1] + Lat<Q>::cz(q) * F[2];
+        const float cn = (Lat<Q>::cx(q) * G[0] + Lat<Q>::cy(q) * G[1] + Lat<Q>::cz(q) * G[2]) * gs;
+        // deviation of the equilibrium from w rho_ref
+        const float feq = w * (rs + rho * (3.f * cu + 4.5f * cu * cu - 1.5f * uu));
+        const float dST = (q == R) ? -af * static_cast<float>(Lat<Q>::B(q))
+                                   : af * (w * cn * cn - static_cast<float>(Lat<Q>::B(q)));
+        const float Xd = ft[q] - om * (ft[q] - feq) + w * tf * (3.f * cF + 9.f * cF * cu - 3.f * uF) + dST;
+        const float dRC = (q == R) ? 0.f : rfb * w * cn * (Lat<Q>::wclass(q) == 1 ? 1.f : 0.70710678118654752f);
+        const float X = Xd + w * rho_ref;
+        const float s = sc_out / w;
+        Store<S>::store(out + q * a.L.nf_pad + i, Xd * s);
+        Store<S>::store(out + fs + q * a.L.nf_pad + i, (dcf * X + 2.f * dRC) * s);
+    }
+    if (MACROS) {
+        a.rho_out[i] = rho0;
+        a.rho_out[static_cast<size_t>(a.L.nf_pad) + i] = rho1;
+#pragma unroll
+        for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * a.L.nf_pad + i] = u[d];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_gather: the reference's f (one pull of G, or the state itself when LOCAL),
+// decoded to FP64 and written in reference AoS order [bulk index][field][q].
+// ---------------------------------------------------------------------------
+template <int Q, class S, int NF, bool LOCAL>
+__global__ void __launch_bounds__(kBlock) k_gather(StepArgs a, const int32_t* __restrict__ slot_bulk,
+                                                   double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.L.nf) return;
+    const size_t b = static_cast<size_t>(slot_bulk[i]);
+    const S* g = static_cast<const S*>(a.src);
+    if constexpr (NF == 1) {
+        using T = typename Store<S>::T;
+        T v[Q];
+        load_field<Q, S, LOCAL>(g, a.L, i, v);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            double f;
+            if constexpr (Store<S>::shifted)
+                f = Lat<Q>::w(q) * (a.rho_ref + static_cast<double>(Store<S>::val(v[q])) * a.inv_scale);
+            else
+                f = v[q];
+            out[b * Q + q] = f;
+        }
+    } else {
+        double f0[Q], f1[Q];
+        load_rk<Q, S, LOCAL>(g, a.L, i, f0, f1, a.rho_ref, a.inv_scale);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            out[b * 2 * Q + q] = f0[q];
+            out[b * 2 * Q + Q + q] = f1[q];
+        }
+    }
+}
+
+// k_moments: per-block FP64 sums over the reference's f of
+// [mass0, mass1, fc_x, fc_y, fc_z, max|f|(last)] plus a non-finite count
+// folded into max|f| as +inf.
+template <int Q, class S, int NF, bool LOCAL>
+__global__ void __launch_bounds__(kBlock) k_moments(StepArgs a) {
+    constexpr int NV = 6;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double vals[NV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (i < a.L.nf) {
+        double f0[Q], f1[Q];
+        const S* g = static_cast<const S*>(a.src);
+        if constexpr (NF == 1) {
+            using T = typename Store<S>::T;
+            T v[Q];
+            load_field<Q, S, LOCAL>(g, a.L, i, v);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                if constexpr (Store<S>::shifted)
+                    f0[q] = Lat<Q>::w(q) * (a.rho_ref + static_cast<double>(Store<S>::val(v[q])) * a.inv_scale);
+                else
+                    f0[q] = v[q];
+                f1[q] = 0.0;
+            }
+        } else {
+            load_rk<Q, S, LOCAL>(g, a.L, i, f0, f1, a.rho_ref, a.inv_scale);
+        }
+        double mx = 0.0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const double ft = f0[q] + f1[q];
+            vals[0] += f0[q];
+            vals[1] += f1[q];
+            vals[2] += Lat<Q>::cx(q) * ft;
+            vals[3] += Lat<Q>::cy(q) * ft;
+            vals[4] += Lat<Q>::cz(q) * ft;
+            const double af = fmax(fabs(f0[q]), fabs(f1[q]));
+            mx = (af != af || isinf(af)) ? CUDART_INF : fmax(mx, af);
+        }
+        vals[5] = mx;
+    }
+    block_reduce_store<NV>(vals, a.partials, true);
+}
+
+}  // namespace bclbm

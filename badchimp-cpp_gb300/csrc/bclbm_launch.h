@@ -1,0 +1,37 @@
+// Host-side launchers of the bclbm kernels (one per kernel family).  Each
+// dispatches the run-time lattice / precision / variant choice to a template
+// instance and enqueues it on the given stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+
+#include "bclbm_kernels.cuh"
+
+namespace bclbm {
+
+enum Precision { kF64 = 0, kF32 = 1, kF16 = 2, kBF16 = 3 };
+
+inline int grid_for(int n) { return (n + kBlock - 1) / kBlock; }
+
+// process-wide count of kernel launches issued by the library
+std::atomic<int64_t>& launch_counter();
+
+// bclbm_exact.cu (-fmad=false)
+cudaError_t launch_single_exact(int Q, bool trt, bool local, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_rk_f64(int Q, bool local, bool flux, const StepArgs& a, cudaStream_t s, bool density);
+
+// bclbm_kernels.cu
+cudaError_t launch_single_fast(int Q, int precision, bool trt, bool local, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_rk_shift(int Q, int precision, bool local, bool flux, const StepArgs& a, cudaStream_t s,
+                            bool density);
+cudaError_t launch_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params, cudaStream_t s);
+cudaError_t launch_gather(int Q, int precision, int nfields, bool local, const StepArgs& a, const int32_t* slot_bulk,
+                          double* out, cudaStream_t s);
+cudaError_t launch_moments(int Q, int precision, int nfields, bool local, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_reduce_final(int nv, const double* partials, int nblocks, double* out, bool max_last,
+                                cudaStream_t s);
+
+}  // namespace bclbm

@@ -1,0 +1,225 @@
+"""Geometry: seeded porous media and the reference's sparse node numbering.
+
+Two parts:
+
+* ``sphere_pack`` / ``channel_2d`` make voxel masks (1 = fluid, 0 = solid).
+  The reference has no 3D sphere-pack generator; this one places spheres of a
+  fixed radius with centres drawn from ``numpy.random.default_rng(seed)``
+  uniformly in the box (periodic distance, overlap allowed) until the fluid
+  fraction reaches the target porosity.
+
+* ``build_lattice`` turns a mask into the arrays the reference's ``Grid`` and
+  ``Nodes`` hold after reading a ``.vtklb`` file written by
+  ``PythonScripts/vtklb.py``: the node numbering, the neighbour table
+  ``neigList_[node*nQ + q]`` (src/lbsolver/LBgrid.h:119, 160), the positions
+  ``pos_`` (LBgrid.h:120) and the node types of ``Nodes::setupNodeType``
+  (src/lbsolver/LBnodes.h:141-209).  The numbering rules restated here are the
+  single-rank case of ``vtklb.setup_processor_labels`` and
+  ``write_neighbors_fast`` (PythonScripts/vtklb.py:6-45, 84-114, 182-218):
+
+  - node 0 is the ghost node;
+  - fluid nodes are numbered 1..Nf in C order of the interior (x slowest);
+  - then every solid that is a lattice neighbour of a fluid node, in C order of
+    the array padded by a one-node rim; a periodic rim position is a separate
+    node (the rim copies the opposite interior layer, vtklb.py:97-114);
+  - a neighbour outside the padded array, or at an unlisted position, is node 0,
+    except that a rim position holding fluid maps to the interior fluid node it
+    copies (vtklb.py:34-39).
+
+Everything is plain numpy so that tables for 256^3 boxes build in seconds.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+# Lattice velocity sets in the reference's order, rest direction last
+# (src/lbsolver/LBd2q9.h:33, src/lbsolver/LBd3q19.h:33; PythonScripts/vtklb.py:171-176).
+D2Q9_C = np.array([[1, 0], [1, 1], [0, 1], [-1, 1], [-1, 0], [-1, -1], [0, -1], [1, -1], [0, 0]],
+                  dtype=np.int64)
+D3Q19_C = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0], [1, -1, 0], [1, 0, 1], [1, 0, -1],
+                    [0, 1, 1], [0, 1, -1], [-1, 0, 0], [0, -1, 0], [0, 0, -1], [-1, -1, 0],
+                    [-1, 1, 0], [-1, 0, -1], [-1, 0, 1], [0, -1, -1], [0, -1, 1], [0, 0, 0]],
+                   dtype=np.int64)
+LATTICE_C = {"D2Q9": D2Q9_C, "D3Q19": D3Q19_C}
+LATTICE_Q = {"D2Q9": 9, "D3Q19": 19}
+
+
+def lattice_name(q: int) -> str:
+    if q == 9:
+        return "D2Q9"
+    if q == 19:
+        return "D3Q19"
+    raise ValueError(f"unsupported lattice with {q} directions")
+
+
+def channel_2d(nx: int = 256, ny: int = 64) -> np.ndarray:
+    """2D channel: solid rows y=0 and y=ny-1, fluid in between (x periodic by the caller)."""
+    geo = np.ones((nx, ny), dtype=np.int8)
+    geo[:, 0] = 0
+    geo[:, ny - 1] = 0
+    return geo
+
+
+def sphere_pack(shape, radius: float, porosity: float, seed: int, max_spheres: int = 10_000_000):
+    """Periodic random pack of solid spheres; returns (mask, centres, porosity).
+
+    Spheres of radius ``radius`` (voxel ``i`` is solid when its periodic
+    distance to a centre is <= radius) are added one at a time, centres drawn
+    uniformly in the box from ``default_rng(seed)``, until the fluid fraction is
+    at most ``porosity``.
+    """
+    shape = tuple(int(n) for n in shape)
+    nd = len(shape)
+    rng = np.random.default_rng(seed)
+    solid = np.zeros(shape, dtype=bool)
+    total = solid.size
+    nsolid = 0
+    centres = []
+    r = float(radius)
+    ri = int(np.ceil(r))
+    offs = np.arange(-ri, ri + 1)
+    grids = np.meshgrid(*([offs] * nd), indexing="ij")
+    while (total - nsolid) / total > porosity:
+        if len(centres) >= max_spheres:
+            break
+        c = rng.uniform(0.0, 1.0, size=nd) * np.asarray(shape, dtype=np.float64)
+        centres.append(c)
+        base = np.floor(c).astype(np.int64)
+        d2 = np.zeros(grids[0].shape, dtype=np.float64)
+        idx = []
+        for d in range(nd):
+            p = base[d] + grids[d]
+            diff = p - c[d]
+            d2 += diff * diff
+            idx.append(np.mod(p, shape[d]))
+        inside = d2 <= r * r
+        sel = tuple(ix[inside] for ix in idx)
+        before = np.count_nonzero(solid[sel])
+        solid[sel] = True
+        nsolid += np.count_nonzero(solid[sel]) - before
+    mask = (~solid).astype(np.int8)
+    return mask, np.asarray(centres), float(np.count_nonzero(mask)) / total
+
+
+def build_lattice(geo: np.ndarray, lattice: str, periodic: str = "") -> dict:
+    """Node numbering, neighbour table, positions and node types for one rank.
+
+    ``geo`` holds 1 for fluid and 0 for solid.  Returns a dict with
+    ``neigh`` (int32 [N*Q], row 0 all zero), ``types`` (int16 [N]),
+    ``pos`` (int32 [N*nD], -1 for node 0), ``nf`` (fluid count) and ``ns``
+    (stored boundary-solid count); N = 1 + nf + ns.
+    """
+    c = LATTICE_C[lattice]
+    nq, nd = c.shape
+    geo = np.asarray(geo)
+    if geo.ndim != nd:
+        raise ValueError(f"{lattice} needs a {nd}-D geometry, got {geo.ndim}-D")
+    if not np.all((geo == 0) | (geo == 1)):
+        raise ValueError("geometry must hold 0 (solid) and 1 (fluid) only")
+    periodic = periodic.lower()
+    pshape = tuple(n + 2 for n in geo.shape)
+    interior = tuple([slice(1, -1)] * nd)
+    P = np.full(pshape, -1, dtype=np.int8)
+    P[interior] = geo
+    fluid_int = np.zeros(pshape, dtype=bool)
+    fluid_int[interior] = geo == 1
+    nf = int(np.count_nonzero(fluid_int))
+    label = np.zeros(pshape, dtype=np.int64)
+    label[fluid_int] = np.arange(1, nf + 1)
+    for d, ax in enumerate("xyz"[:nd]):
+        if ax in periodic:
+            lo = [slice(None)] * nd
+            hi = [slice(None)] * nd
+            src_lo = [slice(None)] * nd
+            src_hi = [slice(None)] * nd
+            lo[d], src_lo[d] = 0, -2
+            hi[d], src_hi[d] = -1, 1
+            P[tuple(lo)] = P[tuple(src_lo)]
+            P[tuple(hi)] = P[tuple(src_hi)]
+            label[tuple(lo)] = label[tuple(src_lo)]
+            label[tuple(hi)] = label[tuple(src_hi)]
+
+    fpos = np.nonzero(fluid_int)  # C order == label order
+    added = np.zeros(pshape, dtype=bool)
+    for v in c:
+        p = tuple(fpos[d] + v[d] for d in range(nd))
+        added[p] |= P[p] == 0
+    spos = np.nonzero(added)
+    ns = int(spos[0].size)
+    local = np.zeros(pshape, dtype=np.int64)
+    local[fpos] = np.arange(1, nf + 1)
+    local[spos] = np.arange(nf + 1, nf + ns + 1)
+
+    n_nodes = 1 + nf + ns
+    allpos = [np.concatenate([fpos[d], spos[d]]) for d in range(nd)]
+    neigh = np.zeros((n_nodes, nq), dtype=np.int32)
+    for q in range(nq):
+        p = [allpos[d] + c[q, d] for d in range(nd)]
+        ok = np.ones(allpos[0].shape, dtype=bool)
+        for d in range(nd):
+            ok &= (p[d] >= 0) & (p[d] < pshape[d])
+        pp = tuple(p[d][ok] for d in range(nd))
+        nb = local[pp]
+        img = (nb == 0) & (P[pp] == 1)
+        nb = np.where(img, label[pp], nb)
+        col = np.zeros(allpos[0].shape, dtype=np.int64)
+        col[ok] = nb
+        neigh[1:, q] = col
+    pos = np.full((n_nodes, nd), -1, dtype=np.int32)
+    for d in range(nd):
+        pos[1:, d] = allpos[d] - 1
+
+    types = node_types(neigh, nf)
+    return {"neigh": neigh.reshape(-1), "types": types, "pos": pos.reshape(-1),
+            "nf": nf, "ns": ns, "nq": nq, "nd": nd, "lattice": lattice}
+
+
+def node_types(neigh: np.ndarray, nf: int) -> np.ndarray:
+    """Nodes::setupNodeType (src/lbsolver/LBnodes.h:156-209) for one rank.
+
+    Nodes 1..nf are fluid, the rest solid, node 0 the default ghost (-1).
+    Solids are 1 with a fluid neighbour, else 0; fluids are 2 with a solid
+    neighbour (node 0 counts as solid), else 3.
+    """
+    neigh = np.asarray(neigh).reshape(-1, neigh.shape[-1] if neigh.ndim == 2 else 1)
+    n_nodes = neigh.shape[0]
+    fluid = np.zeros(n_nodes, dtype=bool)
+    fluid[1:nf + 1] = True
+    nbr_fluid = fluid[neigh]
+    types = np.zeros(n_nodes, dtype=np.int16)
+    has_fluid = nbr_fluid.any(axis=1)
+    has_solid = (~nbr_fluid).any(axis=1)
+    types[fluid] = np.where(has_solid[fluid], 2, 3)
+    solid = ~fluid
+    types[solid] = np.where(has_fluid[solid], 1, 0)
+    types[0] = -1
+    return types
+
+
+def bounce_back_links(neigh: np.ndarray, types: np.ndarray, nodes: np.ndarray, nq: int) -> list:
+    """Link classes of BoundaryHalwWayHelper (src/lbsolver/LBhalfwayhelperclass.h:128-159).
+
+    For each listed node: (node, beta, gamma, delta) with beta the unknown
+    direction of each fluid/solid pair, gamma and delta one direction of each
+    fluid/fluid and solid/solid pair, for the first nQ/2 directions in order.
+    """
+    npairs = (nq - 1) // 2
+    neigh = np.asarray(neigh).reshape(-1, nq)
+    fluid = np.asarray(types) > 1
+    out = []
+    for node in nodes:
+        beta, gamma, delta = [], [], []
+        for q in range(npairs):
+            a = fluid[neigh[node, q]]
+            b = fluid[neigh[node, q + npairs]]
+            if a and b:
+                gamma.append(q)
+            elif a:
+                beta.append(q)
+            elif b:
+                beta.append(q + npairs)
+            else:
+                delta.append(q)
+        out.append((int(node), beta, gamma, delta))
+    return out

@@ -1,0 +1,191 @@
+"""Host-side mirror of the reference lbsolver set-up, above the C ABI.
+
+The names and argument meanings follow the reference's lbsolver API so that a
+user of ``src/std_case`` / ``src/twophase`` finds the same steps:
+
+* ``Lattice``            Grid + Nodes + findBulkNodes of one rank
+                         (src/lbsolver/LBgrid.h:127-148, LBnodes.h:112-209,
+                         LBgeometry.h:11-56);
+* ``weights``            DXQY::w (src/lbsolver/LBd2q9.h:32, LBd3q19.h:32);
+* ``initiate_single``    f = w_q rho at the bulk nodes (src/std_case/main.cpp:92-96);
+* ``initiate_twophase``  rho0/rho1/wettability read as float, the wettability
+                         densities on boundary solids, and initiateLbField for
+                         both phases (src/twophase/main_TWOPHASE.cpp:156-207,
+                         src/lbsolver/LBinitiatefield.h:33-57);
+* ``Solver``             the device time step through the C ABI in
+                         ``include/bclbm.h`` (see ``native``).
+
+Arrays are numpy, in the reference's layout and numbering.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from . import geometry as _geometry
+from . import native as _native
+
+BGK, TRT, RK = 0, 1, 2
+F64, F32, F16, BF16 = 0, 1, 2, 3
+PRECISION = {"f64": F64, "f32": F32, "f16": F16, "bf16": BF16}
+FLAG_EXACT = 1
+FLAG_SFC_ORDER = 2
+
+
+def weights(nq: int) -> np.ndarray:
+    """Lattice weights in the reference's direction order, computed as the
+    reference's constexpr divisions."""
+    if nq == 9:
+        w0, w1, w2 = 16.0 / 36.0, 4.0 / 36.0, 1.0 / 36.0
+        return np.array([w1, w2, w1, w2, w1, w2, w1, w2, w0])
+    if nq == 19:
+        w0, w1, w2 = 12.0 / 36.0, 2.0 / 36.0, 1.0 / 36.0
+        return np.array([w1] * 3 + [w2] * 6 + [w1] * 3 + [w2] * 6 + [w0])
+    raise ValueError(f"unsupported lattice with {nq} directions")
+
+
+class Lattice:
+    """One rank's Grid/Nodes arrays: neighbour table, node types, positions, bulk list."""
+
+    def __init__(self, nq, neigh, types, pos=None, bulk=None, shape=None, periodic=""):
+        self.nq = int(nq)
+        self.nd = 2 if self.nq == 9 else 3
+        self.neigh = np.ascontiguousarray(neigh, dtype=np.int32).reshape(-1)
+        self.types = np.ascontiguousarray(types, dtype=np.int16)
+        self.n_nodes = int(self.types.size)
+        if self.neigh.size != self.n_nodes * self.nq:
+            raise ValueError("neighbour table size does not match the node count")
+        self.pos = None if pos is None else np.ascontiguousarray(pos, dtype=np.int32).reshape(-1)
+        if bulk is None:  # findBulkNodes: every fluid node of this rank, in node order
+            bulk = np.nonzero(self.types > 1)[0]
+        self.bulk = np.ascontiguousarray(bulk, dtype=np.int32)
+        self.shape = None if shape is None else tuple(int(n) for n in shape)
+        self.periodic = periodic
+
+    @classmethod
+    def from_geometry(cls, geo, lattice: str, periodic: str = ""):
+        lat = _geometry.build_lattice(geo, lattice, periodic)
+        return cls(lat["nq"], lat["neigh"], lat["types"], lat["pos"], shape=np.asarray(geo).shape,
+                   periodic=periodic)
+
+    @property
+    def n_bulk(self) -> int:
+        return int(self.bulk.size)
+
+    def attribute(self, values: np.ndarray) -> np.ndarray:
+        """A per-voxel attribute at every node's position, the way vtklb.py
+        writes it (periodic rim positions take the opposite interior value);
+        node 0 gets 0."""
+        values = np.asarray(values)
+        p = self.pos.reshape(-1, self.nd)
+        idx = tuple(np.mod(p[:, d], values.shape[d]) for d in range(self.nd))
+        out = values[idx].astype(values.dtype, copy=True)
+        out[0] = 0
+        return out
+
+    def solid_boundary(self) -> np.ndarray:
+        """findSolidBndNodes (src/lbsolver/LBgeometry.h:37-45)."""
+        return np.nonzero(self.types == 1)[0].astype(np.int32)
+
+
+def initiate_single(lat: Lattice, rho_node: np.ndarray) -> np.ndarray:
+    """std_case start: f(0,q,n) = w_q rho(0,n) at bulk nodes, 0 elsewhere."""
+    w = weights(lat.nq)
+    f = np.zeros((lat.n_nodes, lat.nq))
+    b = lat.bulk
+    f[b] = w[None, :] * np.asarray(rho_node, dtype=np.float64)[b][:, None]
+    return f.reshape(-1)
+
+
+def initiate_twophase(lat: Lattice, rho0_node, rho1_node, wett_node):
+    """twophase start.  Inputs are per-node attribute values (Lattice.attribute).
+
+    The reference reads rho0, rho1 and wettability as float
+    (main_TWOPHASE.cpp:158, 166, 173) and sets rho1 = 1 - wettability in float
+    arithmetic on boundary solids.  Returns (f [N*2*Q], rho [N*2]).
+    """
+    r0 = np.asarray(rho0_node).astype(np.float32).astype(np.float64)
+    r1 = np.asarray(rho1_node).astype(np.float32).astype(np.float64)
+    wt = np.asarray(wett_node).astype(np.float32)
+    sb = lat.types == 1
+    r0[sb] = wt[sb].astype(np.float64)
+    r1[sb] = (np.float32(1.0) - wt[sb]).astype(np.float64)
+    r0[0] = 0.0
+    r1[0] = 0.0
+    w = weights(lat.nq)
+    f = np.zeros((lat.n_nodes, 2, lat.nq))
+    b = lat.bulk
+    # initiateLbField with zero velocity: w_q * rho * (1 + 0) (LBinitiatefield.h:50-55)
+    f[b, 0, :] = (w[None, :] * r0[b][:, None]) * 1.0
+    f[b, 1, :] = (w[None, :] * r1[b][:, None]) * 1.0
+    rho = np.stack([r0, r1], axis=1).reshape(-1)
+    return f.reshape(-1), rho
+
+
+class Solver:
+    """One device lattice instance behind the C ABI (bclbm_create ... bclbm_destroy)."""
+
+    def __init__(self, lat: Lattice, f_init, collision=BGK, precision=F64, tau=(1.0, 1.0), force=(0.0, 0.0, 0.0),
+                 sigma=0.0, beta=0.0, flux_control=False, mom_x=0.0, rho_init=None, exact=False, sfc=False,
+                 rho_ref=1.0, store_scale=0.0):
+        if isinstance(precision, str):
+            precision = PRECISION[precision]
+        self.lat = lat
+        self.nfields = 2 if collision == RK else 1
+        flags = (FLAG_EXACT if exact else 0) | (FLAG_SFC_ORDER if sfc else 0)
+        F = np.zeros(3)
+        F[:len(force)] = force
+        self._h = _native.create(lat, np.ascontiguousarray(f_init, dtype=np.float64), collision, precision, flags,
+                                 tuple(float(t) for t in tau) + ((1.0,) if len(tau) == 1 else ()), F, sigma, beta,
+                                 int(bool(flux_control)), mom_x, rho_ref, store_scale,
+                                 None if rho_init is None else np.ascontiguousarray(rho_init, dtype=np.float64))
+
+    def step(self, nsteps: int = 1):
+        _native.check(_native.lib().bclbm_step(self._h, int(nsteps)), self._h)
+
+    def download_f(self, out=None):
+        if out is None:
+            out = np.zeros(self.lat.n_nodes * self.nfields * self.lat.nq)
+        _native.check(_native.lib().bclbm_download_f(self._h, _native.dp(out)), self._h)
+        return out
+
+    def download_macros(self):
+        rho = np.zeros(self.lat.n_nodes * self.nfields)
+        vel = np.zeros(self.lat.n_nodes * self.lat.nd)
+        cg = np.zeros(self.lat.n_nodes) if self.nfields == 2 else None
+        _native.check(_native.lib().bclbm_download_macros(self._h, _native.dp(rho), _native.dp(vel),
+                                                          _native.dp(cg)), self._h)
+        return rho, vel, cg
+
+    def reduce(self) -> dict:
+        return _native.reduce(self._h)
+
+    def set_force(self, force):
+        F = np.zeros(3)
+        F[:len(force)] = force
+        _native.check(_native.lib().bclbm_set_force(self._h, _native.dp(F)), self._h)
+
+    def node_perm(self) -> np.ndarray:
+        out = np.zeros(self.lat.n_bulk, dtype=np.int32)
+        _native.check(_native.lib().bclbm_node_perm(self._h, _native.ip(out)), self._h)
+        return out
+
+    def sync(self):
+        _native.check(_native.lib().bclbm_sync(self._h), self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _native.lib().bclbm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -1,0 +1,181 @@
+"""ctypes binding of the C ABI in include/bclbm.h (libbclbm.so, built in-tree).
+
+There is no fallback: if the shared library is missing or fails to load, every
+entry point raises.  The library is loaded from this package's folder only.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_NAME = "libbclbm.so"
+_lib = None
+
+
+class BclbmError(RuntimeError):
+    pass
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [
+        ("lattice_q", ctypes.c_int32),
+        ("n_nodes", ctypes.c_int32),
+        ("neigh", ctypes.c_void_p),
+        ("types", ctypes.c_void_p),
+        ("n_bulk", ctypes.c_int32),
+        ("bulk", ctypes.c_void_p),
+        ("pos", ctypes.c_void_p),
+        ("collision", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("flags", ctypes.c_uint32),
+        ("tau", ctypes.c_double * 2),
+        ("force", ctypes.c_double * 3),
+        ("sigma", ctypes.c_double),
+        ("beta", ctypes.c_double),
+        ("flux_control", ctypes.c_int32),
+        ("mom_x", ctypes.c_double),
+        ("rho_ref", ctypes.c_double),
+        ("store_scale", ctypes.c_double),
+        ("f_init", ctypes.c_void_p),
+        ("rho_init", ctypes.c_void_p),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("mass", ctypes.c_double * 2),
+        ("momentum", ctypes.c_double * 3),
+        ("flux_fc", ctypes.c_double * 3),
+        ("saturation", ctypes.c_double),
+        ("max_abs_f", ctypes.c_double),
+        ("n_bulk", ctypes.c_int64),
+        ("steps_done", ctypes.c_int64),
+        ("nonfinite", ctypes.c_int32),
+    ]
+
+
+EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_download_f", "bclbm_download_macros", "bclbm_reduce",
+           "bclbm_set_force", "bclbm_node_perm", "bclbm_footprint", "bclbm_sync", "bclbm_destroy", "bclbm_error",
+           "bclbm_last_error", "bclbm_launch_count"]
+
+
+def lib_path() -> Path:
+    return HERE / LIB_NAME
+
+
+def lib():
+    """Loads libbclbm.so (raising if it is absent) and declares the signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not path.exists():
+        raise BclbmError(f"{path} is missing: build it with build() (nvcc, sm_103a); there is no CPU fallback")
+    L = ctypes.CDLL(str(path))
+    vp = ctypes.c_void_p
+    L.bclbm_create.argtypes = [ctypes.POINTER(Desc), ctypes.POINTER(vp)]
+    L.bclbm_create.restype = ctypes.c_int
+    L.bclbm_step.argtypes = [vp, ctypes.c_int]
+    L.bclbm_step.restype = ctypes.c_int
+    L.bclbm_download_f.argtypes = [vp, vp]
+    L.bclbm_download_f.restype = ctypes.c_int
+    L.bclbm_download_macros.argtypes = [vp, vp, vp, vp]
+    L.bclbm_download_macros.restype = ctypes.c_int
+    L.bclbm_reduce.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.bclbm_reduce.restype = ctypes.c_int
+    L.bclbm_set_force.argtypes = [vp, vp]
+    L.bclbm_set_force.restype = ctypes.c_int
+    L.bclbm_node_perm.argtypes = [vp, vp]
+    L.bclbm_node_perm.restype = ctypes.c_int
+    L.bclbm_footprint.argtypes = [ctypes.POINTER(Desc), ctypes.POINTER(ctypes.c_size_t)]
+    L.bclbm_footprint.restype = ctypes.c_int
+    L.bclbm_sync.argtypes = [vp]
+    L.bclbm_sync.restype = ctypes.c_int
+    L.bclbm_destroy.argtypes = [vp]
+    L.bclbm_destroy.restype = None
+    L.bclbm_error.argtypes = [ctypes.c_int]
+    L.bclbm_error.restype = ctypes.c_char_p
+    L.bclbm_last_error.argtypes = [vp]
+    L.bclbm_last_error.restype = ctypes.c_char_p
+    L.bclbm_launch_count.argtypes = []
+    L.bclbm_launch_count.restype = ctypes.c_int64
+    _lib = L
+    return L
+
+
+def dp(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+ip = dp
+
+
+def check(rc: int, handle=None):
+    if rc != 0:
+        msg = lib().bclbm_error(rc).decode()
+        if handle:
+            detail = lib().bclbm_last_error(handle)
+            if detail:
+                msg += ": " + detail.decode()
+        raise BclbmError(f"bclbm status {rc}: {msg}")
+
+
+def make_desc(lat, f_init, collision, precision, flags, tau, force, sigma, beta, flux_control, mom_x, rho_ref,
+              store_scale, rho_init):
+    d = Desc()
+    d.lattice_q = lat.nq
+    d.n_nodes = lat.n_nodes
+    d.neigh = lat.neigh.ctypes.data
+    d.types = lat.types.ctypes.data
+    d.n_bulk = lat.n_bulk
+    d.bulk = lat.bulk.ctypes.data
+    d.pos = lat.pos.ctypes.data if lat.pos is not None else None
+    d.collision = int(collision)
+    d.precision = int(precision)
+    d.flags = int(flags)
+    d.tau[0], d.tau[1] = float(tau[0]), float(tau[1])
+    for k in range(3):
+        d.force[k] = float(force[k])
+    d.sigma = float(sigma)
+    d.beta = float(beta)
+    d.flux_control = int(flux_control)
+    d.mom_x = float(mom_x)
+    d.rho_ref = float(rho_ref)
+    d.store_scale = float(store_scale)
+    d.f_init = f_init.ctypes.data if f_init is not None else None
+    d.rho_init = rho_init.ctypes.data if rho_init is not None else None
+    return d
+
+
+def create(lat, f_init, collision, precision, flags, tau, force, sigma, beta, flux_control, mom_x, rho_ref,
+           store_scale, rho_init):
+    d = make_desc(lat, f_init, collision, precision, flags, tau, force, sigma, beta, flux_control, mom_x, rho_ref,
+                  store_scale, rho_init)
+    h = ctypes.c_void_p()
+    rc = lib().bclbm_create(ctypes.byref(d), ctypes.byref(h))
+    check(rc)
+    return h
+
+
+def footprint(lat, collision, precision, flags=0):
+    d = make_desc(lat, None, collision, precision, flags, (1.0, 1.0), (0.0, 0.0, 0.0), 0.0, 0.0, 0, 0.0, 1.0, 0.0,
+                  None)
+    n = ctypes.c_size_t()
+    check(lib().bclbm_footprint(ctypes.byref(d), ctypes.byref(n)))
+    return int(n.value)
+
+
+def reduce(h) -> dict:
+    s = Stats()
+    check(lib().bclbm_reduce(h, ctypes.byref(s)), h)
+    return {"mass": list(s.mass), "momentum": list(s.momentum), "flux_fc": list(s.flux_fc),
+            "saturation": s.saturation, "max_abs_f": s.max_abs_f, "n_bulk": s.n_bulk,
+            "steps_done": s.steps_done, "nonfinite": bool(s.nonfinite)}
+
+
+def launch_count() -> int:
+    return int(lib().bclbm_launch_count())

@@ -1,0 +1,140 @@
+/*
+ * bclbm: GB300-native (sm_103a) lattice-Boltzmann time step for BADChIMP.
+ *
+ * C ABI.  Plain pointers and sizes only; no exceptions cross it, nothing here
+ * calls exit().  Every function returns BCLBM_OK (0) or a negative status whose
+ * text bclbm_error() gives; bclbm_last_error() adds the detail of the last
+ * failure on a handle.
+ *
+ * The boundary replaces, in the reference's main-file time loops, the per-node
+ * collide/propagate loops, LbField::swapData, BndMpi::communicate* (a no-op at
+ * one rank) and HalfWayBounceBack::apply:
+ *   src/std_case/main.cpp:110-145         one bclbm_step(h, 1) per iteration
+ *   src/twophase/main_TWOPHASE.cpp:238-392 one bclbm_step(h, 1) per iteration
+ * Output steps (std_case/main.cpp:150-155, main_TWOPHASE.cpp:399-448) call
+ * bclbm_download_macros() into the reference's ScalarField/VectorField storage
+ * before Output::write().
+ *
+ * All host arrays passed in or out use the reference's layout and node
+ * numbering:
+ *   neigh   [N*Q]      Grid::neigList_           (src/lbsolver/LBgrid.h:119, 160, 197)
+ *   types   [N]        Nodes::nodeType_          (src/lbsolver/LBnodes.h:107, 156-209)
+ *   bulk    [n_bulk]   findBulkNodes()           (src/lbsolver/LBgeometry.h:11-21)
+ *   f       [N*nF*Q]   LbField data_             (src/lbsolver/LBfield.h:298-305)
+ *   rho     [N*nF]     ScalarField data_         (src/lbsolver/LBfield.h:92-100)
+ *   vel     [N*nD]     VectorField data_, 1 field (src/lbsolver/LBfield.h:168-175)
+ *   cg      [N]        the twophase colour field cgField (main_TWOPHASE.cpp:144, 245, 283)
+ * with N = Grid::size() (node 0 is the ghost node), Q = 9 (D2Q9) or 19 (D3Q19).
+ *
+ * A handle owns one lattice instance on the current CUDA device and a stream
+ * of its own; calls on one handle come from one host thread.  bclbm_step() is
+ * asynchronous; downloads and reductions synchronise the handle's stream.
+ */
+#ifndef BCLBM_H
+#define BCLBM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BCLBM_ABI_VERSION 1
+
+/* status codes */
+#define BCLBM_OK 0
+#define BCLBM_ERR_INVALID (-1)     /* bad argument or descriptor */
+#define BCLBM_ERR_TABLE (-2)       /* neighbour table / node types inconsistent */
+#define BCLBM_ERR_NOMEM (-3)       /* device or host allocation failed */
+#define BCLBM_ERR_CUDA (-4)        /* CUDA runtime error */
+#define BCLBM_ERR_UNSUPPORTED (-5) /* combination not built */
+#define BCLBM_ERR_NONFINITE (-6)   /* NaN/Inf found by a reduction */
+#define BCLBM_ERR_BUDGET (-7)      /* request exceeds the HBM admission budget */
+#define BCLBM_ERR_NOCUDA (-8)      /* no CUDA device visible */
+
+/* collision models */
+#define BCLBM_BGK 0 /* calcOmegaBGK + calcDeltaOmegaF          (src/lbsolver/LBcollision.h:27-46, 194-213) */
+#define BCLBM_TRT 1 /* calcOmegaBGKTRT + calcDeltaOmegaFTRT(phi=1) (LBcollision.h:50-75, 215-236) */
+#define BCLBM_RK 2  /* Rothman-Keller two-phase step of src/twophase/main_TWOPHASE.cpp:238-392 */
+
+/* population storage on the device */
+#define BCLBM_F64 0  /* plain FP64 populations, FP64 arithmetic */
+#define BCLBM_F32 1  /* FP32 shifted deviations (f - w*rho_ref)/w, FP32 arithmetic */
+#define BCLBM_F16 2  /* FP16 shifted, scaled deviations, FP32 arithmetic */
+#define BCLBM_BF16 3 /* BF16 shifted, scaled deviations, FP32 arithmetic */
+
+/* flags */
+#define BCLBM_FLAG_EXACT 1u     /* FP64 only: the reference's expression order, no FMA
+                                   contraction: results bit-identical to the reference */
+#define BCLBM_FLAG_SFC_ORDER 2u /* reorder fluid nodes along a Morton curve of their
+                                   positions (needs pos); downloads keep reference order */
+
+typedef struct {
+    int32_t lattice_q;        /* 9 or 19 */
+    int32_t n_nodes;          /* N = Grid::size() */
+    const int32_t* neigh;     /* [N*Q] */
+    const int16_t* types;     /* [N] */
+    int32_t n_bulk;           /* number of bulk (own-rank fluid) nodes */
+    const int32_t* bulk;      /* [n_bulk], increasing; every listed node has type > 1 */
+    const int32_t* pos;       /* [N*nD] Grid positions, needed for BCLBM_FLAG_SFC_ORDER, else NULL */
+    int32_t collision;        /* BCLBM_BGK | BCLBM_TRT | BCLBM_RK */
+    int32_t precision;        /* BCLBM_F64 | BCLBM_F32 | BCLBM_F16 | BCLBM_BF16 */
+    uint32_t flags;
+    double tau[2];            /* BGK: tau[0]; TRT: tau[0] symmetric, tau[1] antisymmetric;
+                                 RK: the two phase relaxation times (fluid.tau[0], fluid.tau[1]) */
+    double force[3];          /* body force (VectorField bodyForce(1,1)); unused components 0 */
+    double sigma;             /* RK: surface tension parameter A (fluid.sigma) */
+    double beta;              /* RK: recolouring parameter (fluid.beta) */
+    int32_t flux_control;     /* RK: 1 = body force x from the flux controller of
+                                 main_TWOPHASE.cpp:292-308 every step, target mom_x */
+    double mom_x;             /* RK: fluid.momx */
+    double rho_ref;           /* shifted storage: reference density of the shift (1.0 if 0) */
+    double store_scale;       /* F16/BF16: scale of the stored deviations (default if 0) */
+    const double* f_init;     /* [N*nF*Q] initial populations, nF = 2 for RK else 1 */
+    const double* rho_init;   /* RK: [N*2] densities; only the solid boundary entries (type 1)
+                                 are read (the wettability densities); else NULL */
+} bclbm_desc;
+
+typedef struct {
+    double mass[2];       /* sum over bulk nodes of rho per field (RK: per phase) */
+    double momentum[3];   /* sum over bulk nodes of rho*u = sum_q f c_q + F/2 */
+    double flux_fc[3];    /* sum over bulk nodes of sum_q f c_q (the flux controller's sum) */
+    double saturation;    /* RK: mass[0] / (mass[0] + mass[1]); else 0 */
+    double max_abs_f;     /* largest |f| over the populations (finite check) */
+    int64_t n_bulk;
+    int64_t steps_done;
+    int32_t nonfinite;    /* 1 if any NaN/Inf population was seen */
+} bclbm_stats;
+
+typedef struct bclbm_handle bclbm_handle;
+
+int bclbm_create(const bclbm_desc* desc, bclbm_handle** out);
+/* Advance nsteps time steps.  The moments of the last step's collision (the
+ * values the reference stores in rho/vel during its last node loop) are kept
+ * for bclbm_download_macros. */
+int bclbm_step(bclbm_handle* h, int nsteps);
+/* Populations after the last step (reference f after swapData + bounce-back),
+ * written into the bulk rows of a reference-layout LbField buffer [N*nF*Q];
+ * other rows are left untouched. */
+int bclbm_download_f(bclbm_handle* h, double* f);
+/* rho [N*nF], vel [N*nD], cg [N] (RK only); any may be NULL; bulk rows only. */
+int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg);
+/* FP64 reductions over the current populations (deterministic order). */
+int bclbm_reduce(bclbm_handle* h, bclbm_stats* out);
+int bclbm_set_force(bclbm_handle* h, const double force[3]);
+/* internal node order: out[i] = reference node number of device slot i, [n_bulk] */
+int bclbm_node_perm(bclbm_handle* h, int32_t* out);
+/* device bytes held by a handle created from desc (admission by HBM footprint) */
+int bclbm_footprint(const bclbm_desc* desc, size_t* bytes);
+int bclbm_sync(bclbm_handle* h);
+void bclbm_destroy(bclbm_handle* h);
+const char* bclbm_error(int status);
+const char* bclbm_last_error(const bclbm_handle* h);
+/* kernel launches issued by this process since load (for launch accounting) */
+int64_t bclbm_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

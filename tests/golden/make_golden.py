@@ -1,0 +1,271 @@
+"""Generates the golden fixtures in this folder from the reference itself.
+
+Run from the repository root where the reference sources are present:
+
+    make -C oracle ref                       # builds oracle/_ref from the reference sources
+    python tests/golden/make_golden.py [--reference PATH]
+
+For every case it writes the geometry with the reference's own
+``PythonScripts/vtklb.py`` (imported from the reference tree), runs the
+reference lbsolver through ``oracle/_ref/ref_driver_<lattice>`` and stores
+
+* the tables the reference builds from that file (neighbour table, node types,
+  positions, bulk / fluid-boundary / solid-boundary lists, half-way
+  bounce-back link classes), and
+* the reference's populations, densities, velocities (and colour field) after
+  the stated number of steps, restricted to the fluid nodes,
+
+in ``<case>.npz``.  Config 1 (the 256x64 channel) is additionally run through
+the UNMODIFIED ``src/std_case/main.cpp`` and its VTU output is compared with
+the driver's dump, which pins the driver itself.
+
+The fixtures are inputs to the tests; nothing at test time reads the
+reference tree.
+"""
+
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+
+
+def load_geometry():
+    spec = importlib.util.spec_from_file_location("bclbm_geometry", REPO / "badchimp-cpp_gb300" / "geometry.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+geometry = load_geometry()
+
+
+def read_lbfield(path):
+    with open(path, "rb") as fh:
+        nf, nq, nn = np.frombuffer(fh.read(12), dtype=np.int32)
+        data = np.frombuffer(fh.read(), dtype=np.float64)
+    return data.reshape(nn, nf, nq)
+
+
+def read_scalar(path):
+    with open(path, "rb") as fh:
+        nf, nn = np.frombuffer(fh.read(8), dtype=np.int32)
+        data = np.frombuffer(fh.read(), dtype=np.float64)
+    return data.reshape(nn, nf)
+
+
+def read_vector(path):
+    with open(path, "rb") as fh:
+        nf, nd, nn = np.frombuffer(fh.read(12), dtype=np.int32)
+        data = np.frombuffer(fh.read(), dtype=np.float64)
+    return data.reshape(nn, nf, nd)
+
+
+def read_vtu_array(path, name):
+    """One float64 DataArray of a raw-appended VTU (src/io/VTK.h:1165-1178, 730-765)."""
+    raw = Path(path).read_bytes()
+    head_end = raw.index(b'<AppendedData encoding="raw">')
+    head = raw[:head_end].decode("ascii", "replace")
+    m = re.search(r'<DataArray[^>]*Name="%s"[^>]*>' % re.escape(name), head)
+    if m is None:
+        raise KeyError(name)
+    off = int(re.search(r'offset="(\d+)"', m.group(0)).group(1))
+    start = raw.index(b"_", head_end) + 1 + off
+    nbytes = int(np.frombuffer(raw[start:start + 4], dtype=np.uint32)[0])
+    return np.frombuffer(raw[start + 4:start + 4 + nbytes], dtype=np.float64).copy()
+
+
+def write_vtklb(ref: Path, workdir: Path, mask, lattice, periodic, attrs):
+    sys.path.insert(0, str(ref / "PythonScripts"))
+    try:
+        import vtklb as vtklb_mod  # the reference's own writer
+    finally:
+        sys.path.pop(0)
+    import contextlib
+    import io
+    with contextlib.redirect_stdout(io.StringIO()):
+        vt = vtklb_mod.vtklb(np.asarray(mask, dtype=int), lattice, periodic, "tmp", str(workdir) + "/")
+        for name, arr in attrs.items():
+            vt.append_data_set(name, np.asarray(arr))
+    return workdir / "tmp0.vtklb"
+
+
+def run(cmd, cwd=None):
+    res = subprocess.run(cmd, cwd=cwd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"{cmd} failed: {res.stdout}\n{res.stderr}")
+    return res.stdout
+
+
+def two_phase_fields(mask, seed, p=0.5, wett=0.5):
+    rng = np.random.default_rng(seed)
+    red = (rng.random(mask.shape) < p).astype(np.float64)
+    rho0 = np.where(mask == 1, red, 0.0)
+    rho1 = np.where(mask == 1, 1.0 - red, 0.0)
+    return {"rho0": rho0, "rho1": rho1, "wettability": np.full(mask.shape, wett)}
+
+
+def cases():
+    """Geometries and runs.  Sizes are chosen so the oracle finishes in seconds,
+    except config 1 at its full 20,000 steps."""
+    out = []
+    # Config 1: D2Q9 channel 256x64, walls at y=0 and y=63, periodic x, tau=1, gx=1e-6.
+    ch = geometry.channel_2d(256, 64)
+    out.append(dict(name="channel_256x64", lattice="D2Q9", periodic="x", mask=ch,
+                    attrs={"init_rho": np.ones(ch.shape)},
+                    runs=[dict(tag="bgk_100", mode="single", steps=100, tau=1.0, fx=1e-6),
+                          dict(tag="bgk_20000", mode="single", steps=20000, tau=1.0, fx=1e-6)]))
+    # Small D2Q9 porous box, periodic in x and y, for the 2D two-phase path and TRT.
+    m2, _, _ = geometry.sphere_pack((40, 32), radius=4.0, porosity=0.6, seed=7)
+    out.append(dict(name="disc_40x32", lattice="D2Q9", periodic="xy", mask=m2,
+                    attrs={"init_rho": np.ones(m2.shape), **two_phase_fields(m2, 11)},
+                    runs=[dict(tag="trt_300", mode="single", steps=300, tau=0.8, tau_anti=1.125, trt=1, fx=1e-5),
+                          dict(tag="rk_200", mode="twophase", steps=200, tau0=1.0, tau1=1.0, sigma=0.01,
+                               beta=0.99, fx=1e-5)]))
+    # D3Q19 periodic sphere packs (the 256^3 / 192^3 configurations, scaled down).
+    m3, _, _ = geometry.sphere_pack((20, 20, 20), radius=4.0, porosity=0.45, seed=3)
+    out.append(dict(name="pack_20", lattice="D3Q19", periodic="xyz", mask=m3,
+                    attrs={"init_rho": np.ones(m3.shape), **two_phase_fields(m3, 5)},
+                    runs=[dict(tag="bgk_500", mode="single", steps=500, tau=0.8, fx=1e-5),
+                          dict(tag="trt_500", mode="single", steps=500, tau=0.8, tau_anti=1.125, trt=1, fx=1e-5),
+                          dict(tag="rk_100", mode="twophase", steps=100, tau0=1.0, tau1=1.0, sigma=0.01,
+                               beta=0.99, fx=1e-5),
+                          dict(tag="rkflux_60", mode="twophase", steps=60, tau0=1.0, tau1=0.7, sigma=0.01,
+                               beta=0.99, fx=0.0, momx=1e-4)]))
+    # Non-periodic D3Q19 box (x periodic only): faces without periodicity bounce back off node 0.
+    mb = np.ones((12, 10, 8), dtype=np.int8)
+    xx, yy, zz = np.indices(mb.shape)
+    mb[(xx - 6) ** 2 + (yy - 5) ** 2 + (zz - 4) ** 2 <= 6.5] = 0
+    out.append(dict(name="box_12x10x8", lattice="D3Q19", periodic="x", mask=mb,
+                    attrs={"init_rho": np.ones(mb.shape)},
+                    runs=[dict(tag="bgk_400", mode="single", steps=400, tau=0.9, fx=1e-5, fy=2e-6)]))
+    return out
+
+
+def make_case(ref: Path, case: dict, keep_dir=None):
+    lt = case["lattice"].lower()
+    drv = REPO / "oracle" / "_ref" / f"ref_driver_{lt}"
+    if not drv.exists():
+        raise SystemExit(f"{drv} missing: run 'make -C oracle ref' first")
+    work = Path(tempfile.mkdtemp(prefix="bclbm_golden_"))
+    try:
+        vtk = write_vtklb(ref, work, case["mask"], case["lattice"], case["periodic"], case["attrs"])
+        tdir = work / "tables"
+        tdir.mkdir()
+        run([str(drv), "tables", str(vtk), str(tdir)])
+        nq = geometry.LATTICE_Q[case["lattice"]]
+        nd = 2 if nq == 9 else 3
+        arrays = {
+            "mask": np.asarray(case["mask"], dtype=np.uint8),
+            "neigh": np.fromfile(tdir / "neigh.i32", dtype=np.int32),
+            "types": np.fromfile(tdir / "types.i16", dtype=np.int16),
+            "pos": np.fromfile(tdir / "pos.i32", dtype=np.int32),
+            "bulk": np.fromfile(tdir / "bulk.i32", dtype=np.int32),
+            "fluidbnd": np.fromfile(tdir / "fluidbnd.i32", dtype=np.int32),
+            "solidbnd": np.fromfile(tdir / "solidbnd.i32", dtype=np.int32),
+            "links_fluidbnd": np.fromfile(tdir / "links_fluidbnd.i32", dtype=np.int32),
+            "links_bulk": np.fromfile(tdir / "links_bulk.i32", dtype=np.int32),
+        }
+        nf = arrays["bulk"].size
+        for name, arr in case["attrs"].items():
+            arrays["attr_" + name] = np.asarray(arr, dtype=np.float64)
+        meta = {"name": case["name"], "lattice": case["lattice"], "periodic": case["periodic"],
+                "nq": nq, "nd": nd, "nf": int(nf), "n_nodes": int(arrays["types"].size), "runs": []}
+        for r in case["runs"]:
+            rdir = work / r["tag"]
+            rdir.mkdir()
+            kv = [f"{k}={v!r}" for k, v in r.items() if k not in ("tag", "mode")]
+            run([str(drv), r["mode"], str(vtk), str(rdir)] + kv)
+            f = read_lbfield(rdir / "f.lblbf")
+            rho = read_scalar(rdir / "rho.lbsca")
+            vel = read_vector(rdir / "vel.lbvec")
+            arrays[f"{r['tag']}_f"] = f[1:nf + 1].copy()
+            arrays[f"{r['tag']}_rho"] = rho[1:nf + 1].copy()
+            arrays[f"{r['tag']}_vel"] = vel[1:nf + 1].copy()
+            if r["mode"] == "twophase":
+                arrays[f"{r['tag']}_cg"] = read_scalar(rdir / "cg.lbsca")[:, 0].copy()
+                arrays[f"{r['tag']}_force"] = np.fromfile(rdir / "force.f64", dtype=np.float64)
+            meta["runs"].append({k: v for k, v in r.items()})
+        arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+        np.savez_compressed(HERE / f"{case['name']}.npz", **arrays)
+        print(f"{case['name']}: N={meta['n_nodes']} Nf={nf} runs={[r['tag'] for r in case['runs']]}")
+        if case["name"] == "channel_256x64":
+            pin_std_case(ref, vtk, work)
+    finally:
+        if keep_dir is None:
+            shutil.rmtree(work, ignore_errors=True)
+
+
+def pin_std_case(ref: Path, vtk: Path, work: Path):
+    """Runs the unmodified std_case main on config 1 and compares its VTU output
+    with the driver's dump after the same number of steps."""
+    exe = REPO / "oracle" / "_ref" / "std_case_d2q9"
+    root = work / "std_case"
+    (root / "input" / "mpi").mkdir(parents=True)
+    (root / "output").mkdir()
+    (root / "run").mkdir()
+    shutil.copy(vtk, root / "input" / "mpi" / "tmp0.vtklb")
+    n_it = 300
+    (root / "input" / "input.dat").write_text(
+        f"<iterations>\n  max {n_it}\n  write {n_it}\n<end>\n"
+        "<fluid>\n  tau 1.0\n  bodyforce 1e-6 0.0\n<end>\n")
+    run([str(exe)], cwd=root / "run")
+    vtus = sorted((root / "output").rglob("*lb_run*.vtu"))
+    last = vtus[-1]
+    rho_vtu = read_vtu_array(last, "rho")
+    vel_vtu = read_vtu_array(last, "vel").reshape(-1, 3)[:, :2]  # VTK vectors carry 3 components
+    drv = REPO / "oracle" / "_ref" / "ref_driver_d2q9"
+    ddir = work / "pin"
+    ddir.mkdir()
+    # std_case runs iterations 0..max inclusive; the moments written at the last
+    # iteration are those of the driver's last step when it runs max+1 steps.
+    run([str(drv), "single", str(root / "input" / "mpi" / "tmp0.vtklb"), str(ddir),
+         f"steps={n_it + 1}", "tau=1.0", "fx=1e-6"])
+    nf = rho_vtu.size
+    rho_d = read_scalar(ddir / "rho.lbsca")[1:nf + 1, 0]
+    vel_d = read_vector(ddir / "vel.lbvec")[1:nf + 1, 0, :]
+    if not (np.array_equal(rho_vtu, rho_d) and np.array_equal(vel_vtu, vel_d)):
+        raise SystemExit("driver does not reproduce the unmodified std_case output")
+    (HERE / "std_case_pin.json").write_text(json.dumps({
+        "what": "unmodified src/std_case/main.cpp (D2Q9) vs oracle/ref_driver.cpp, config 1 geometry",
+        "iterations": n_it, "fluid_nodes": int(nf), "rho_bit_exact": True, "vel_bit_exact": True,
+        "vtu": last.name}, indent=1) + "\n")
+    print(f"std_case pin: {last.name} rho/vel bit-exact against the driver ({nf} nodes)")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=os.environ.get("BCLBM_REFERENCE", "/root/reference"))
+    ap.add_argument("--only", default=None)
+    ap.add_argument("--pin-only", action="store_true", help="only rerun the std_case pin of config 1")
+    args = ap.parse_args()
+    ref = Path(args.reference)
+    if args.pin_only:
+        work = Path(tempfile.mkdtemp(prefix="bclbm_pin_"))
+        try:
+            ch = geometry.channel_2d(256, 64)
+            vtk = write_vtklb(ref, work, ch, "D2Q9", "x", {"init_rho": np.ones(ch.shape)})
+            pin_std_case(ref, vtk, work)
+        finally:
+            shutil.rmtree(work, ignore_errors=True)
+        return
+    for case in cases():
+        if args.only and case["name"] != args.only:
+            continue
+        make_case(ref, case)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,60 @@
+"""The in-process geometry builder against the tables the reference builds from
+vtklb.py files (bit-exact), plus generator properties."""
+
+import numpy as np
+import pytest
+
+import lbcases
+
+
+@pytest.mark.parametrize("name", lbcases.CASES)
+def test_build_lattice_matches_reference_tables(bclbm, name):
+    case = lbcases.Case(name, bclbm)
+    z = case.z
+    lat = bclbm.geometry.build_lattice(z["mask"].astype(np.int8), case.meta["lattice"], case.meta["periodic"])
+    assert lat["nf"] == case.nf
+    assert 1 + lat["nf"] + lat["ns"] == case.n_nodes
+    assert np.array_equal(lat["neigh"], z["neigh"])
+    assert np.array_equal(lat["types"], z["types"])
+    assert np.array_equal(lat["pos"], z["pos"])
+    bulk = np.nonzero(lat["types"] > 1)[0]
+    assert np.array_equal(bulk, z["bulk"])
+    assert np.array_equal(np.nonzero(lat["types"] == 2)[0], z["fluidbnd"])
+    assert np.array_equal(np.nonzero(lat["types"] == 1)[0], z["solidbnd"])
+
+
+@pytest.mark.parametrize("name", lbcases.CASES)
+@pytest.mark.parametrize("which", ["fluidbnd", "bulk"])
+def test_bounce_back_link_classes_match_reference(bclbm, name, which):
+    case = lbcases.Case(name, bclbm)
+    z = case.z
+    links = bclbm.geometry.bounce_back_links(z["neigh"], z["types"], z[which], case.nq)
+    rec = []
+    for node, beta, gamma, delta in links:
+        rec += [node, len(beta), len(gamma), len(delta)] + beta + gamma + delta
+    assert np.array_equal(np.array(rec, dtype=np.int32), z["links_" + which])
+
+
+def test_sphere_pack_is_seeded_and_hits_porosity(bclbm):
+    a, ca, pa = bclbm.geometry.sphere_pack((48, 40, 32), radius=5.0, porosity=0.4, seed=123)
+    b, cb, pb = bclbm.geometry.sphere_pack((48, 40, 32), radius=5.0, porosity=0.4, seed=123)
+    c, _, _ = bclbm.geometry.sphere_pack((48, 40, 32), radius=5.0, porosity=0.4, seed=124)
+    assert np.array_equal(a, b) and np.array_equal(ca, cb)
+    assert not np.array_equal(a, c)
+    assert pa <= 0.4 and pa > 0.37
+    assert abs(pa - a.mean()) < 1e-12
+
+
+def test_periodic_tables_are_symmetric(bclbm):
+    geo, _, _ = bclbm.geometry.sphere_pack((18, 14, 10), radius=3.0, porosity=0.5, seed=9)
+    lat = bclbm.geometry.build_lattice(geo, "D3Q19", "xyz")
+    nq, nf = lat["nq"], lat["nf"]
+    nb = lat["neigh"].reshape(-1, nq)
+    rev = [(q + 9) % 18 if q < 18 else 18 for q in range(19)]
+    types = lat["types"]
+    for x in range(1, nf + 1):
+        for q in range(18):
+            y = nb[x, rev[q]]
+            if types[y] > 1:
+                assert nb[y, q] == x
+        assert nb[x, 18] == x

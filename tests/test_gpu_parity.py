@@ -1,0 +1,162 @@
+"""GPU parity through the C ABI against the reference's own outputs.
+
+* exact FP64 step (reference expression order, no FMA): bit-identical to the
+  reference for every golden run, in reference order and in Morton order;
+  runs with the flux controller differ only through the order of the global
+  sum and stay within 1e-12;
+* restructured FP64 step (FMA): relative L2 error <= 1e-12 in f, rho and u;
+* FP32 / FP16 / BF16 shifted storage with FP32 arithmetic: errors against the
+  oracle within the storage precision's tolerance stated in each test.
+"""
+
+import numpy as np
+import pytest
+
+import lbcases
+
+pytestmark = pytest.mark.gpu
+
+RUNS = lbcases.all_runs()
+
+
+def relerr(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    n = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (n if n > 0 else 1.0)
+
+
+def make_solver(case, run, **kw):
+    L = case.L
+    f0, rho0 = case.init(run)
+    if run["mode"] == "single":
+        coll = L.TRT if run.get("trt") else L.BGK
+        tau = (run["tau"], run.get("tau_anti", run["tau"]))
+        return L.Solver(case.lat, f0, collision=coll, tau=tau, force=case.force(run), **kw)
+    return L.Solver(case.lat, f0, collision=L.RK, tau=(run["tau0"], run["tau1"]), force=case.force(run),
+                    sigma=run["sigma"], beta=run["beta"], flux_control="momx" in run, mom_x=run.get("momx", 0.0),
+                    rho_init=rho0, **kw)
+
+
+def outputs(case, run, s):
+    nfields = 2 if run["mode"] == "twophase" else 1
+    f = s.download_f(np.zeros(case.n_nodes * nfields * case.nq))
+    rho, vel, cg = s.download_macros()
+    b = case.lat.bulk
+    out = {"f": case.bulk_rows(f, nfields), "rho": rho.reshape(-1, nfields)[b], "vel": vel.reshape(-1, case.nd)[b]}
+    if cg is not None:
+        out["cg"] = cg
+    return out
+
+
+@pytest.mark.parametrize("sfc", [False, True], ids=["refOrder", "morton"])
+@pytest.mark.parametrize("name,tag", RUNS, ids=[f"{n}-{t}" for n, t in RUNS])
+def test_exact_f64_matches_reference(bclbm, gpu, name, tag, sfc):
+    case = lbcases.Case(name, bclbm)
+    run = case.runs[tag]
+    exp = case.expected(tag)
+    with make_solver(case, run, exact=True, sfc=sfc) as s:
+        s.step(run["steps"])
+        got = outputs(case, run, s)
+        perm = s.node_perm()
+    assert np.array_equal(np.sort(perm), case.lat.bulk)
+    if not sfc:
+        assert np.array_equal(perm, case.lat.bulk)
+    ef = exp["f"] if run["mode"] == "twophase" else exp["f"]
+    if "momx" in run:
+        # the flux controller's global sum runs in a different order than the reference's serial loop
+        assert relerr(got["f"], ef) <= 1e-12
+        assert relerr(got["vel"], exp["vel"][:, 0, :]) <= 1e-12
+        return
+    assert np.array_equal(got["f"], ef)
+    assert np.array_equal(got["rho"], exp["rho"])
+    assert np.array_equal(got["vel"], exp["vel"][:, 0, :])
+    if "cg" in got:
+        b = case.lat.bulk
+        assert np.array_equal(got["cg"][b], exp["cg"][b])
+
+
+SINGLE = [(n, t) for n, t in RUNS if not t.startswith("rk")]
+
+
+@pytest.mark.parametrize("name,tag", SINGLE, ids=[f"{n}-{t}" for n, t in SINGLE])
+def test_fast_f64_within_1e12(bclbm, gpu, name, tag):
+    case = lbcases.Case(name, bclbm)
+    run = case.runs[tag]
+    exp = case.expected(tag)
+    with make_solver(case, run) as s:
+        s.step(run["steps"])
+        got = outputs(case, run, s)
+    assert relerr(got["f"], exp["f"]) <= 1e-12
+    assert relerr(got["rho"], exp["rho"]) <= 1e-12
+    assert relerr(got["vel"], exp["vel"][:, 0, :]) <= 1e-12
+
+
+@pytest.mark.parametrize("prec,tol_f,tol_u", [("f32", 1e-6, 1e-4), ("f16", 5e-4, 2e-2), ("bf16", 5e-3, 1.5e-1)])
+def test_shifted_storage_single_phase(bclbm, gpu, prec, tol_f, tol_u):
+    case = lbcases.Case("pack_20", bclbm)
+    run = case.runs["bgk_500"]
+    exp = case.expected("bgk_500")
+    with make_solver(case, run, precision=prec) as s:
+        s.step(run["steps"])
+        got = outputs(case, run, s)
+        st = s.reduce()
+    assert relerr(got["f"], exp["f"]) <= tol_f
+    assert relerr(got["vel"], exp["vel"][:, 0, :]) <= tol_u
+    # mean flux (the permeability numerator) against the FP64 reference
+    jx_ref = exp["vel"][:, 0, 0].sum()
+    assert abs(got["vel"][:, 0].sum() - jx_ref) / abs(jx_ref) <= tol_u
+
+
+@pytest.mark.parametrize("prec,tol_sat,tol_u", [("f32", 1e-6, 1e-3), ("f16", 1e-3, 5e-2)])
+def test_shifted_storage_two_phase(bclbm, gpu, prec, tol_sat, tol_u):
+    case = lbcases.Case("pack_20", bclbm)
+    run = case.runs["rk_100"]
+    exp = case.expected("rk_100")
+    with make_solver(case, run, precision=prec) as s:
+        s.step(run["steps"])
+        got = outputs(case, run, s)
+        st = s.reduce()
+    sat_ref = exp["rho"][:, 0].sum() / exp["rho"].sum()
+    assert abs(st["saturation"] - sat_ref) <= tol_sat
+    assert relerr(got["vel"], exp["vel"][:, 0, :]) <= tol_u
+
+
+def test_download_before_any_step_returns_initial_state(bclbm, gpu):
+    case = lbcases.Case("box_12x10x8", bclbm)
+    run = case.runs["bgk_400"]
+    f0, _ = case.init(run)
+    for prec in ("f64", "f32"):
+        with make_solver(case, run, precision=prec) as s:
+            f = s.download_f(np.zeros_like(f0))
+        tol = 0.0 if prec == "f64" else 1e-7
+        assert relerr(case.bulk_rows(f, 1), case.bulk_rows(f0, 1)) <= tol
+
+
+def test_reduce_matches_downloaded_state(bclbm, gpu):
+    case = lbcases.Case("pack_20", bclbm)
+    run = case.runs["rk_100"]
+    with make_solver(case, run, exact=True) as s:
+        s.step(17)
+        f = s.download_f(np.zeros(case.n_nodes * 2 * case.nq))
+        st = s.reduce()
+    fr = case.bulk_rows(f, 2)
+    m = fr.sum(axis=(0, 2))
+    assert np.allclose(st["mass"], m, rtol=1e-13)
+    c = bclbm.geometry.D3Q19_C
+    fc = (fr.sum(axis=1) @ c).sum(axis=0)
+    assert np.allclose(st["flux_fc"], fc, rtol=1e-10, atol=1e-15)
+    assert st["saturation"] == pytest.approx(m[0] / m.sum(), rel=1e-13)
+    assert not st["nonfinite"] and st["steps_done"] == 17
+
+
+def test_stepping_in_pieces_equals_one_call(bclbm, gpu):
+    case = lbcases.Case("disc_40x32", bclbm)
+    run = case.runs["trt_300"]
+    with make_solver(case, run, exact=True) as a, make_solver(case, run, exact=True) as b:
+        a.step(run["steps"])
+        for _ in range(run["steps"] // 50):
+            b.step(50)
+        fa = a.download_f(np.zeros(case.n_nodes * case.nq))
+        fb = b.download_f(np.zeros(case.n_nodes * case.nq))
+    assert np.array_equal(fa, fb)
