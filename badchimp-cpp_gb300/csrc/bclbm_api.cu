@@ -483,7 +483,13 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     return BCLBM_OK;
 }
 
-int bclbm_step(bclbm_handle* h, int nsteps) {
+}  // extern "C"
+
+namespace {
+
+// The step loop.  ev (optional) receives, per step, the events around the
+// density pass (RK) and around the main step kernel: ev[4 s + 0..3].
+int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
     if (!h || nsteps < 0) return BCLBM_ERR_INVALID;
     if (nsteps == 0) return BCLBM_OK;
     CUDA_TRY(h, cudaSetDevice(h->device));
@@ -496,11 +502,14 @@ int bclbm_step(bclbm_handle* h, int nsteps) {
         a.rho_out = macros ? h->d_rho : nullptr;
         a.vel_out = macros ? h->d_vel : nullptr;
         if (h->collision != BCLBM_RK) {
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
             if (h->exact) CUDA_TRY(h, launch_single_exact(h->q, h->trt, local, a, h->stream));
             else CUDA_TRY(h, launch_single_fast(h->q, h->precision, h->trt, local, a, h->stream));
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
         } else {
             StepArgs ad = a;
             ad.rho_out = nullptr;
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 0], h->stream));
             if (h->precision == BCLBM_F64) CUDA_TRY(h, launch_rk_f64(h->q, local, h->flux, ad, h->stream, true));
             else CUDA_TRY(h, launch_rk_shift(h->q, h->precision, local, h->flux, ad, h->stream, true));
             if (h->flux) {
@@ -508,8 +517,11 @@ int bclbm_step(bclbm_handle* h, int nsteps) {
                 CUDA_TRY(h, launch_flux_force(h->d_red, 1.0 / static_cast<double>(h->nf), h->mom_x, h->d_params,
                                               h->stream));
             }
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 1], h->stream));
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
             if (h->precision == BCLBM_F64) CUDA_TRY(h, launch_rk_f64(h->q, local, false, a, h->stream, false));
             else CUDA_TRY(h, launch_rk_shift(h->q, h->precision, local, false, a, h->stream, false));
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
         }
         h->cur = 1 - h->cur;
         h->state_post = true;
@@ -517,6 +529,42 @@ int bclbm_step(bclbm_handle* h, int nsteps) {
     h->macros_valid = true;
     h->steps_done += nsteps;
     return BCLBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bclbm_step(bclbm_handle* h, int nsteps) { return step_impl(h, nsteps, nullptr); }
+
+int bclbm_step_timed(bclbm_handle* h, int nsteps, bclbm_timing* out) {
+    if (!h || !out || nsteps < 1) return BCLBM_ERR_INVALID;
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    std::vector<cudaEvent_t> ev(4 * static_cast<size_t>(nsteps) + 2, nullptr);
+    int rc = BCLBM_OK;
+    for (auto& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) rc = fail(h, BCLBM_ERR_CUDA, "cudaEventCreate failed");
+    const int64_t l0 = launch_counter().load();
+    if (rc == BCLBM_OK && cudaEventRecord(ev[0], h->stream) != cudaSuccess) rc = fail(h, BCLBM_ERR_CUDA, "event");
+    if (rc == BCLBM_OK) rc = step_impl(h, nsteps, ev.data() + 2);
+    if (rc == BCLBM_OK && cudaEventRecord(ev[1], h->stream) != cudaSuccess) rc = fail(h, BCLBM_ERR_CUDA, "event");
+    if (rc == BCLBM_OK && cudaEventSynchronize(ev[1]) != cudaSuccess) rc = fail(h, BCLBM_ERR_CUDA, "sync");
+    if (rc == BCLBM_OK) {
+        std::memset(out, 0, sizeof(*out));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        out->total_ms = ms;
+        for (int s = 0; s < nsteps; ++s) {
+            cudaEvent_t* e = ev.data() + 2 + 4 * static_cast<size_t>(s);
+            if (cudaEventElapsedTime(&ms, e[2], e[3]) == cudaSuccess) out->step_kernel_ms += ms;
+            if (h->collision == BCLBM_RK && cudaEventElapsedTime(&ms, e[0], e[1]) == cudaSuccess) out->density_ms += ms;
+        }
+        out->launches = launch_counter().load() - l0;
+        out->nsteps = nsteps;
+    }
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    return rc;
 }
 
 int bclbm_sync(bclbm_handle* h) {

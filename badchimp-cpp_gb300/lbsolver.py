@@ -143,6 +143,10 @@ class Solver:
     def step(self, nsteps: int = 1):
         _native.check(_native.lib().bclbm_step(self._h, int(nsteps)), self._h)
 
+    def step_timed(self, nsteps: int) -> dict:
+        """Steps with CUDA events on the handle's own stream (bclbm_step_timed)."""
+        return _native.step_timed(self._h, nsteps)
+
     def download_f(self, out=None):
         if out is None:
             out = np.zeros(self.lat.n_nodes * self.nfields * self.lat.nq)

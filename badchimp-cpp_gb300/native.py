@@ -58,7 +58,12 @@ class Stats(ctypes.Structure):
     ]
 
 
-EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_download_f", "bclbm_download_macros", "bclbm_reduce",
+class Timing(ctypes.Structure):
+    _fields_ = [("total_ms", ctypes.c_double), ("step_kernel_ms", ctypes.c_double),
+                ("density_ms", ctypes.c_double), ("launches", ctypes.c_int64), ("nsteps", ctypes.c_int32)]
+
+
+EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_step_timed", "bclbm_download_f", "bclbm_download_macros", "bclbm_reduce",
            "bclbm_set_force", "bclbm_node_perm", "bclbm_footprint", "bclbm_sync", "bclbm_destroy", "bclbm_error",
            "bclbm_last_error", "bclbm_launch_count"]
 
@@ -81,6 +86,8 @@ def lib():
     L.bclbm_create.restype = ctypes.c_int
     L.bclbm_step.argtypes = [vp, ctypes.c_int]
     L.bclbm_step.restype = ctypes.c_int
+    L.bclbm_step_timed.argtypes = [vp, ctypes.c_int, ctypes.POINTER(Timing)]
+    L.bclbm_step_timed.restype = ctypes.c_int
     L.bclbm_download_f.argtypes = [vp, vp]
     L.bclbm_download_f.restype = ctypes.c_int
     L.bclbm_download_macros.argtypes = [vp, vp, vp, vp]
@@ -175,6 +182,13 @@ def reduce(h) -> dict:
     return {"mass": list(s.mass), "momentum": list(s.momentum), "flux_fc": list(s.flux_fc),
             "saturation": s.saturation, "max_abs_f": s.max_abs_f, "n_bulk": s.n_bulk,
             "steps_done": s.steps_done, "nonfinite": bool(s.nonfinite)}
+
+
+def step_timed(h, nsteps: int) -> dict:
+    t = Timing()
+    check(lib().bclbm_step_timed(h, int(nsteps), ctypes.byref(t)), h)
+    return {"total_ms": t.total_ms, "step_kernel_ms": t.step_kernel_ms, "density_ms": t.density_ms,
+            "launches": int(t.launches), "nsteps": int(t.nsteps)}
 
 
 def launch_count() -> int:

@@ -1,0 +1,387 @@
+"""Benchmark of the lattice-Boltzmann time step on GB300.
+
+Workload (one bench step = one time step over every fluid node):
+  D3Q19 single phase, periodic 256^3 box of solid spheres (radius 10, seeded
+  uniform centres, overlap allowed) filled to porosity 0.40, tau = 0.8,
+  body force gx = 1e-5; BGK in plain FP64 is the headline, TRT (Lambda = 3/16)
+  and FP32 / FP16 / BF16 shifted storage are reported as variants.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+  (N > 1 under torchrun: independent replicas, one per GPU, weak scaling)
+
+value         MLUPS over all ranks, populations resident in HBM, CUDA events on
+              the library's stream, max over ranks
+e2e           the same metric through the C ABI with host buffers: create from
+              the reference-layout host arrays, K steps with a statistics
+              read-back every 50 steps, download of f / rho / u, destroy
+roofline      algorithmic bytes per launch (fluid nodes x bytes per update) over
+              the average step-kernel duration, against MEASURED_PEAKS.json
+cpu_baseline  the oracle (plain-C restatement of the reference step) on the
+              host cores, a bounded sample of steps of the same workload
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+if int(os.environ.get("WORLD_SIZE", "1")) > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
+    # one GPU per rank, seen as device 0 by torch and by libbclbm alike
+    os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("LOCAL_RANK", "0")
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "D3Q19 MLUPS, HBM GB/s; solves/s, p99 latency vs plain FP64 at ≤1e-3 perm err"
+L2_BYTES = 129 * 1024 * 1024
+# algorithmic bytes per fluid-node update, pull scheme, int32 neighbours:
+# 2 Q s_f (read + write populations) + (Q - 1) * 4 (neighbour table)
+BYTES_PER_UPDATE = {"f64": 2 * 19 * 8 + 18 * 4, "f32": 2 * 19 * 4 + 18 * 4, "f16": 2 * 19 * 2 + 18 * 4,
+                    "bf16": 2 * 19 * 2 + 18 * 4}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "of measured"
+    return 6800.0, "of fallback"
+
+
+def committed_traffic(kernel_tag: str):
+    """dram bytes per launch from the committed ncu summary (profiles/), or None."""
+    f = REPO / "profiles" / "traffic.json"
+    if not f.exists():
+        return None
+    try:
+        d = json.loads(f.read_text())
+        return d.get(kernel_tag, {}).get("traffic_bytes_per_launch")
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu_index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if parts[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(size: int, radius: float, porosity: float, seed: int):
+    import __graft_entry__ as ge
+    bclbm = ge.load()
+    t = time.time()
+    geo, centres, phi = bclbm.geometry.sphere_pack((size, size, size), radius=radius, porosity=porosity, seed=seed)
+    lat = bclbm.lbsolver.Lattice.from_geometry(geo, "D3Q19", "xyz")
+    log(f"geometry {size}^3: porosity {phi:.4f}, {len(centres)} spheres, fluid {lat.n_bulk}, "
+        f"nodes {lat.n_nodes} ({time.time() - t:.1f}s)")
+    return bclbm, lat, phi
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+        if backend == "nccl":
+            torch.cuda.set_device(0)
+    return world, rank
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_port_rate(lat, steps_target_s: float, nthreads: int, tau: float, force, max_steps: int = 1000):
+    """Oracle MLUPS on the host cores for a bounded number of steps."""
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle
+    g = oracle.OracleGrid(lat.nq, lat.neigh, lat.types, lat.bulk)
+    from importlib import import_module
+    L = import_module("bclbm").lbsolver
+    runner = oracle.SingleRunner(g, L.initiate_single(lat, np.ones(lat.n_nodes)), tau, force, nthreads=nthreads)
+    t = time.time()
+    runner.run(1)
+    one = max(time.time() - t, 1e-3)
+    steps = int(max(1, min(max_steps, steps_target_s / one)))
+    t = time.time()
+    runner.run(steps)
+    dt = time.time() - t
+    return lat.n_bulk * steps / dt / 1e6, steps, dt
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the oracle port of the reference step on all host cores."""
+    if rank != 0:
+        return
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle
+    bclbm, lat, phi = build_workload(args.size, args.radius, args.porosity, args.seed)
+    nthreads = oracle.default_threads()
+    g = oracle.OracleGrid(lat.nq, lat.neigh, lat.types, lat.bulk)
+    F = (args.gx, 0.0, 0.0)
+    runner = oracle.SingleRunner(g, bclbm.lbsolver.initiate_single(lat, np.ones(lat.n_nodes)), args.tau, F,
+                                 nthreads=nthreads)
+    for _ in range(args.warmup):
+        runner.run(1)
+    t = time.time()
+    for _ in range(args.steps):
+        runner.run(1)
+    dt = time.time() - t
+    mlups = lat.n_bulk * args.steps / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args, lat, phi, "bgk"),
+        "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": nthreads, "kind": "port",
+                         "sample": f"{args.steps} timed steps of the full workload, oracle (plain-C restatement "
+                                   f"of the reference std_case step, push + bounce-back) on {nthreads} host threads"},
+        "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, lat, phi, collision):
+    return {"workload": f"D3Q19 {collision.upper()} periodic {args.size}^3 sphere pack, radius {args.radius:g}, "
+                        f"porosity {phi:.4f} (target {args.porosity:g}), tau {args.tau:g}, gx {args.gx:g}",
+            "fluid_nodes": lat.n_bulk, "lattice_nodes": lat.n_nodes, "seed": args.seed,
+            "l2": "inputs larger than L2 (population buffers of several GB against 129 MB L2)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def time_solver(solver, steps, warmup):
+    if warmup:
+        solver.step(warmup)
+        solver.sync()
+    return solver.step_timed(steps)
+
+
+def run_mine(args, world, rank):
+    import torch
+    bclbm, lat, phi = build_workload(args.size, args.radius, args.porosity, args.seed)
+    L = bclbm.lbsolver
+    F = (args.gx, 0.0, 0.0)
+    f0 = L.initiate_single(lat, np.ones(lat.n_nodes))
+    tau_anti = 0.5 + (3.0 / 16.0) / (args.tau - 0.5)
+    peak, peak_kind = peaks()
+    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0) \
+        if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else 0
+
+    # ---- headline: plain FP64 BGK, resident in HBM -------------------------------
+    launches0 = bclbm.native.launch_count()
+    with L.Solver(lat, f0, collision=L.BGK, precision="f64", tau=(args.tau, args.tau), force=F) as s:
+        s.step(args.warmup)
+        s.sync()
+        torch.cuda.synchronize()
+        barrier(world)
+        l0 = bclbm.native.launch_count()
+        with ClockSampler(gpu_index) as clk:
+            tm = s.step_timed(args.steps)
+        launches = bclbm.native.launch_count() - l0
+        torch.cuda.synchronize()
+        barrier(world)
+        st = s.reduce()
+    total_ms = allreduce_max(world, tm["total_ms"])
+    kernel_ms = tm["step_kernel_ms"] / args.steps
+    mlups = world * lat.n_bulk * args.steps / (total_ms * 1e-3) / 1e6
+    bpu = BYTES_PER_UPDATE["f64"]
+    achieved = lat.n_bulk * bpu / (kernel_ms * 1e-3) / 1e9
+    traffic = committed_traffic("k_single_d3q19_f64_bgk")
+
+    # ---- variants ----------------------------------------------------------------
+    variants = {}
+    if not args.no_variants:
+        for tag, coll, prec in (("trt_f64", L.TRT, "f64"), ("bgk_f32", L.BGK, "f32"), ("bgk_f16", L.BGK, "f16"),
+                                ("bgk_bf16", L.BGK, "bf16"), ("bgk_f64_exact", L.BGK, "f64x")):
+            kw = dict(exact=True) if prec == "f64x" else {}
+            p = "f64" if prec == "f64x" else prec
+            with L.Solver(lat, f0, collision=coll, precision=p, tau=(args.tau, tau_anti if coll == L.TRT else args.tau),
+                          force=F, **kw) as s:
+                vsteps = max(5, args.steps // 2)
+                tv = time_solver(s, vsteps, args.warmup)
+                stv = s.reduce()
+            km = tv["step_kernel_ms"] / vsteps
+            v_mlups = lat.n_bulk * vsteps / (tv["total_ms"] * 1e-3) / 1e6
+            v_gbs = lat.n_bulk * BYTES_PER_UPDATE[p] / (km * 1e-3) / 1e9
+            variants[tag] = {"mlups": v_mlups, "kernel_ms": km, "achieved_gbs": v_gbs,
+                             "frac": v_gbs / peak, "bytes_per_update": BYTES_PER_UPDATE[p],
+                             "flux_x_after": stv["momentum"][0]}
+        if "bgk_f16" in variants:
+            variants["f16_speedup_vs_f64"] = variants["bgk_f16"]["mlups"] / mlups * world
+
+    # ---- end to end through the C ABI with host buffers -------------------------
+    torch.cuda.synchronize()
+    barrier(world)
+    host_f = np.zeros_like(f0)
+    host_rho = np.zeros(lat.n_nodes)
+    host_vel = np.zeros(lat.n_nodes * 3)
+    t = time.perf_counter()
+    with L.Solver(lat, f0, collision=L.BGK, precision="f64", tau=(args.tau, args.tau), force=F) as s:
+        done = 0
+        nred = 0
+        while done < args.steps:
+            n = min(50, args.steps - done)
+            s.step(n)
+            s.reduce()
+            nred += 1
+            done += n
+        s.download_f(host_f)
+        rho, vel, _ = s.download_macros()
+    e2e_s = time.perf_counter() - t
+    e2e_s = allreduce_max(world, e2e_s)
+    e2e_mlups = world * lat.n_bulk * args.steps / e2e_s / 1e6
+    h2d = lat.neigh.nbytes + lat.types.nbytes + lat.bulk.nbytes + f0.nbytes
+    d2h = nred * 96 + lat.n_bulk * 19 * 8 + lat.n_bulk * (1 + 3) * 8
+
+    # ---- CPU baseline: the oracle on the host cores (rank 0, N = 1) ---------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sys.path.insert(0, str(REPO / "oracle"))
+        import oracle
+        nth = oracle.default_threads()
+        rate, csteps, cdt = cpu_port_rate(lat, args.cpu_seconds, nth, args.tau, F)
+        cpu = {"value": rate, "unit": "MLUPS", "cores": nth, "kind": "port",
+               "sample": f"{csteps} steps of the same {args.size}^3 workload in {cdt:.1f}s, oracle (plain-C "
+                         f"restatement of the reference std_case step) on {nth} host threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded periodic sphere pack (numpy default_rng), no dataset",
+            "config": workload_config(args, lat, phi, "bgk"),
+            "hbm_gbs": achieved,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_single<19,double,FMA,BGK> (pull stream + fused bounce-back)",
+                         "bytes_per_update": bpu, "units_per_launch": lat.n_bulk,
+                         "kernel_ms": kernel_ms},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "e2e": {"value": e2e_mlups, "unit": "MLUPS", "h2d_bytes_per_step": h2d / args.steps,
+                    "d2h_bytes_per_step": d2h / args.steps,
+                    "path": "bclbm_create from host arrays, bclbm_step x K with bclbm_reduce every 50 steps, "
+                            "bclbm_download_f + bclbm_download_macros, bclbm_destroy"},
+            "gpu_launches": launches,
+            "launches_total": bclbm.native.launch_count() - launches0,
+            "variants": variants,
+            "check": {"mass": st["mass"][0], "flux_x": st["momentum"][0], "nonfinite": st["nonfinite"]},
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--radius", type=float, default=10.0)
+    ap.add_argument("--porosity", type=float, default=0.40)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--tau", type=float, default=0.8)
+    ap.add_argument("--gx", type=float, default=1e-5)
+    ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        import __graft_entry__ as ge
+        ge._load_build_module().build()
+        run_mine(args, world, rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -107,6 +107,14 @@ typedef struct {
     int32_t nonfinite;    /* 1 if any NaN/Inf population was seen */
 } bclbm_stats;
 
+typedef struct {
+    double total_ms;        /* CUDA events around the whole block of steps, on the handle's stream */
+    double step_kernel_ms;  /* sum over steps of the main step kernel (collide + stream) */
+    double density_ms;      /* RK: sum over steps of the density / colour pass (and flux sum) */
+    int64_t launches;       /* kernels launched by the call */
+    int32_t nsteps;
+} bclbm_timing;
+
 typedef struct bclbm_handle bclbm_handle;
 
 int bclbm_create(const bclbm_desc* desc, bclbm_handle** out);
@@ -114,6 +122,9 @@ int bclbm_create(const bclbm_desc* desc, bclbm_handle** out);
  * values the reference stores in rho/vel during its last node loop) are kept
  * for bclbm_download_macros. */
 int bclbm_step(bclbm_handle* h, int nsteps);
+/* bclbm_step with CUDA events recorded on the handle's stream around the block
+ * and around every launch of the step kernels; synchronises and fills out. */
+int bclbm_step_timed(bclbm_handle* h, int nsteps, bclbm_timing* out);
 /* Populations after the last step (reference f after swapData + bounce-back),
  * written into the bulk rows of a reference-layout LbField buffer [N*nF*Q];
  * other rows are left untouched. */

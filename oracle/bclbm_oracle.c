@@ -243,19 +243,6 @@ static void bb_slice(void* p, int begin, int end) {
     }
 }
 
-/* After an odd number of steps the state sits in the second buffer; exchange
- * the two buffers' contents so that the caller's f holds it (as swapData does
- * with the valarray storage). */
-static int swap_contents(double* a, double* b, size_t n) {
-    double* tmp = (double*)malloc(sizeof(double) * (n > 0 ? n : 1));
-    if (!tmp) return -10;
-    memcpy(tmp, a, sizeof(double) * n);
-    memcpy(a, b, sizeof(double) * n);
-    memcpy(b, tmp, sizeof(double) * n);
-    free(tmp);
-    return 0;
-}
-
 static int check_grid(const oracle_grid* g) {
     if (!g || (g->nq != 9 && g->nq != 19) || g->n_nodes < 1 || !g->neigh || !g->types || !g->bulk) return -1;
     for (size_t i = 0; i < (size_t)g->n_nodes * g->nq; ++i)
@@ -370,8 +357,7 @@ int oracle_single_run(const oracle_grid* g, int nsteps, int trt, double tau, dou
         parallel_for(bb.n, nthreads, bb_slice, &bc);
     }
     bb_free(&bb);
-    if (cur != f) return swap_contents(f, ftmp, (size_t)g->n_nodes * g->nq);
-    return 0;
+    return cur == f ? 0 : 1;
 }
 
 /* ---- twophase (src/twophase/main_TWOPHASE.cpp:238-392) ---- */
@@ -534,6 +520,5 @@ int oracle_twophase_run(const oracle_grid* g, int nsteps, double tau0, double ta
     }
     bb_free(&bb);
     free(solid);
-    if (cur != f) return swap_contents(f, ftmp, (size_t)g->n_nodes * 2 * nq);
-    return 0;
+    return cur == f ? 0 : 1;
 }

@@ -35,7 +35,9 @@ typedef struct {
 } oracle_grid;
 
 /* std_case step (src/std_case/main.cpp:110-145), BGK or TRT.
- * f, ftmp: two LbField(1, N) buffers; on return the current state is in f.
+ * f, ftmp: two LbField(1, N) buffers (swapData exchanges their roles each step).
+ * Returns 0 if the state after the last step is in f, 1 if it is in ftmp,
+ * negative on invalid input.
  * rho, vel receive the moments of the last step's collision (may be NULL).
  * trt = 0: calcOmegaBGK + calcDeltaOmegaF (LBcollision.h:27-46, 194-213).
  * trt = 1: calcOmegaBGKTRT(tau, tau_anti) + calcDeltaOmegaFTRT(phi = 1)
@@ -46,7 +48,7 @@ int oracle_single_run(const oracle_grid* g, int nsteps, int trt, double tau, dou
                       int nthreads);
 
 /* twophase step (src/twophase/main_TWOPHASE.cpp:238-392) with mass source 0.
- * f, ftmp: LbField(2, N); rho: ScalarField(2, N) holding the fixed solid
+ * f, ftmp: LbField(2, N), returned as for oracle_single_run; rho: ScalarField(2, N) holding the fixed solid
  * boundary densities on entry; cg: ScalarField(1, N), zero on entry;
  * force: in/out body force (x is overwritten by the flux controller when
  * flux_control != 0, target mom_x); force_log (may be NULL) receives the

@@ -74,27 +74,47 @@ def default_threads() -> int:
     return max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count() or 1)
 
 
+class SingleRunner:
+    """std_case loop on the oracle with reusable buffers (two LbField(1,N), rho, vel)."""
+
+    def __init__(self, g: OracleGrid, f, tau, force, trt=False, tau_anti=1.0, nthreads=1):
+        self.g = g
+        self.bufs = [np.ascontiguousarray(f, dtype=np.float64).reshape(-1).copy(), None]
+        self.bufs[1] = np.zeros_like(self.bufs[0])
+        self.rho = np.zeros(g.n_nodes)
+        self.vel = np.zeros(g.n_nodes * g.nd)
+        self.F = np.zeros(3)
+        self.F[:len(force)] = force
+        self.tau, self.tau_anti, self.trt, self.nthreads = float(tau), float(tau_anti), int(bool(trt)), int(nthreads)
+
+    @property
+    def f(self):
+        return self.bufs[0]
+
+    def run(self, nsteps):
+        rc = lib().oracle_single_run(ctypes.byref(self.g._s), int(nsteps), self.trt, self.tau, self.tau_anti,
+                                     _dp(self.F), _dp(self.bufs[0]), _dp(self.bufs[1]), _dp(self.rho),
+                                     _dp(self.vel), self.nthreads)
+        if rc < 0:
+            raise RuntimeError(f"oracle_single_run failed with {rc}")
+        if rc == 1:
+            self.bufs.reverse()
+        return self.bufs[0]
+
+
 def single_run(g: OracleGrid, f, nsteps, tau, force, trt=False, tau_anti=1.0, nthreads=1):
-    """std_case loop; f is LbField(1,N) data [N*Q] (modified in place).
+    """std_case loop from the LbField(1,N) data f [N*Q].
     Returns (f, rho [N], vel [N*nD]) with the last step's moments."""
-    f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
-    ftmp = np.zeros_like(f)
-    rho = np.zeros(g.n_nodes)
-    vel = np.zeros(g.n_nodes * g.nd)
-    F = np.zeros(3)
-    F[:len(force)] = force
-    rc = lib().oracle_single_run(ctypes.byref(g._s), int(nsteps), int(bool(trt)), float(tau), float(tau_anti),
-                                 _dp(F), _dp(f), _dp(ftmp), _dp(rho), _dp(vel), int(nthreads))
-    if rc != 0:
-        raise RuntimeError(f"oracle_single_run failed with {rc}")
-    return f, rho, vel
+    r = SingleRunner(g, f, tau, force, trt, tau_anti, nthreads)
+    r.run(nsteps)
+    return r.f, r.rho, r.vel
 
 
 def twophase_run(g: OracleGrid, f, rho, nsteps, tau0, tau1, sigma, beta, force, mom_x=None, nthreads=1):
     """twophase loop; f is LbField(2,N) data [N*2*Q], rho ScalarField(2,N) data
     with the solid boundary densities set.  Returns (f, rho, vel, cg, force_log)."""
-    f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1).copy()
-    ftmp = np.zeros_like(f)
+    bufs = [np.ascontiguousarray(f, dtype=np.float64).reshape(-1).copy(), None]
+    bufs[1] = np.zeros_like(bufs[0])
     rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(-1).copy()
     vel = np.zeros(g.n_nodes * g.nd)
     cg = np.zeros(g.n_nodes)
@@ -102,8 +122,8 @@ def twophase_run(g: OracleGrid, f, rho, nsteps, tau0, tau1, sigma, beta, force, 
     F[:len(force)] = force
     log = np.zeros(max(1, int(nsteps)))
     rc = lib().oracle_twophase_run(ctypes.byref(g._s), int(nsteps), float(tau0), float(tau1), float(sigma),
-                                   float(beta), int(mom_x is not None), float(mom_x or 0.0), _dp(F), _dp(f),
-                                   _dp(ftmp), _dp(rho), _dp(vel), _dp(cg), _dp(log), int(nthreads))
-    if rc != 0:
+                                   float(beta), int(mom_x is not None), float(mom_x or 0.0), _dp(F), _dp(bufs[0]),
+                                   _dp(bufs[1]), _dp(rho), _dp(vel), _dp(cg), _dp(log), int(nthreads))
+    if rc < 0:
         raise RuntimeError(f"oracle_twophase_run failed with {rc}")
-    return f, rho, vel, cg, log[:int(nsteps)]
+    return bufs[rc], rho, vel, cg, log[:int(nsteps)]

@@ -4,7 +4,9 @@
   reference for every golden run, in reference order and in Morton order;
   runs with the flux controller differ only through the order of the global
   sum and stay within 1e-12;
-* restructured FP64 step (FMA): relative L2 error <= 1e-12 in f, rho and u;
+* restructured FP64 step (FMA): relative L2 error <= 1e-12 in f and rho; u
+  within 1e-12 of max |u| or the reference's own rounding floor of sum_q f c_q
+  (see test_fast_f64_within_1e12);
 * FP32 / FP16 / BF16 shifted storage with FP32 arithmetic: errors against the
   oracle within the storage precision's tolerance stated in each test.
 """
@@ -89,7 +91,15 @@ def test_fast_f64_within_1e12(bclbm, gpu, name, tag):
         got = outputs(case, run, s)
     assert relerr(got["f"], exp["f"]) <= 1e-12
     assert relerr(got["rho"], exp["rho"]) <= 1e-12
-    assert relerr(got["vel"], exp["vel"][:, 0, :]) <= 1e-12
+    # u = (sum_q f c_q + F/2) / rho cancels O(0.1) terms: any summation order other
+    # than the reference's differs from it by the rounding of that sum, ~ eps max f
+    # per step whatever |u| is, and these roundings random-walk over the steps
+    # (the reference's own u_y in the 256x64 channel, exactly 0 in exact
+    # arithmetic, has grown to 7e-15 after 20,000 steps).  The bound is 1e-12
+    # relative to max |u|, or 8 eps max f sqrt(steps) when that floor is larger.
+    eu = exp["vel"][:, 0, :]
+    floor = 8 * np.finfo(np.float64).eps * np.abs(exp["f"]).max() * np.sqrt(run["steps"])
+    assert np.abs(got["vel"] - eu).max() <= max(1e-12 * np.abs(eu).max(), floor)
 
 
 @pytest.mark.parametrize("prec,tol_f,tol_u", [("f32", 1e-6, 1e-4), ("f16", 5e-4, 2e-2), ("bf16", 5e-3, 1.5e-1)])
