@@ -5,6 +5,7 @@ Translation units are compiled in parallel:
                          compiled with -fmad=false (no FMA contraction)
   csrc/bclbm_kernels.cu  FP64 (FMA) and FP32-compute kernels, reductions
   csrc/bclbm_api.cu      the C ABI of include/bclbm.h (host code)
+  csrc/bclbm_static.cu   bclbm_moments_static, the entry point that allocates nothing
 Host code is compiled with -ffp-contract=off so that host-side arithmetic is
 the same on x86-64 and aarch64.
 """
@@ -28,6 +29,7 @@ UNITS = {
     "bclbm_exact.cu": ["-fmad=false"],
     "bclbm_kernels.cu": [],
     "bclbm_api.cu": [],
+    "bclbm_static.cu": [],
 }
 
 

@@ -65,7 +65,7 @@ class Timing(ctypes.Structure):
 
 EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_step_timed", "bclbm_download_f", "bclbm_download_macros", "bclbm_reduce",
            "bclbm_set_force", "bclbm_node_perm", "bclbm_footprint", "bclbm_sync", "bclbm_destroy", "bclbm_error",
-           "bclbm_last_error", "bclbm_launch_count"]
+           "bclbm_last_error", "bclbm_launch_count", "bclbm_moments_static"]
 
 
 def lib_path() -> Path:
@@ -110,6 +110,9 @@ def lib():
     L.bclbm_last_error.restype = ctypes.c_char_p
     L.bclbm_launch_count.argtypes = []
     L.bclbm_launch_count.restype = ctypes.c_int64
+    L.bclbm_moments_static.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.c_int32, vp, ctypes.c_double, ctypes.c_double, vp, vp]
+    L.bclbm_moments_static.restype = ctypes.c_int
     _lib = L
     return L
 

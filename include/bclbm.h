@@ -145,6 +145,37 @@ const char* bclbm_last_error(const bclbm_handle* h);
 /* kernel launches issued by this process since load (for launch accounting) */
 int64_t bclbm_launch_count(void);
 
+/* No counterpart in the reference.  The one entry point of this library that
+ * allocates nothing.  It is for callers that cannot call cudaMalloc: a host
+ * application whose device memory belongs to its own allocator or pool (an
+ * allocation behind its back breaks its accounting or its HBM budget), or a
+ * latency-critical loop that cannot afford cudaMalloc/cudaFree, which may
+ * synchronise the whole device.  Such a caller cannot create a handle, because
+ * bclbm_create allocates.
+ *
+ * It computes the FP64 sums that bclbm_reduce computes - per field
+ * sum_q f, sum_q f c_q, and max |f| (+Inf if any value is NaN or Inf) - over a
+ * population array the caller holds on the device, in the library's device
+ * layout [nfields][Q][slot_stride] and storage format (F64: f itself; the
+ * shifted formats as described at BCLBM_F32..BCLBM_BF16, with rho_ref and
+ * store_scale as given to bclbm_create, 0 meaning the default).
+ * d_out: caller-allocated device buffer of 6 doubles,
+ *   [mass0, mass1, flux_x, flux_y, flux_z, max|f|].
+ * stream: a cudaStream_t, or NULL for the default stream; the call is
+ * asynchronous on that stream.
+ *
+ * The only scratch (per-block partial sums) is a fixed device array inside
+ * the library, 1.5 MiB, held by every GPU that loads the library until the
+ * process exits.  n_slots above BCLBM_STATIC_MAX_SLOTS is rejected with
+ * BCLBM_ERR_INVALID and a message on stderr.  All calls share that array:
+ * calls whose kernels overlap on the GPU race and give wrong sums, so order
+ * them on one stream.  The first call on a device looks up the array's device
+ * address with that device current; make it before any stream capture. */
+#define BCLBM_STATIC_MAX_SLOTS 8388608
+int bclbm_moments_static(int32_t lattice_q, int32_t precision, int32_t nfields, int32_t n_slots,
+                         int32_t slot_stride, const void* d_pops, double rho_ref, double store_scale,
+                         double* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
