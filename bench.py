@@ -249,9 +249,12 @@ def run_mine(args, world, rank):
     gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0) \
         if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else 0
 
-    # ---- headline: plain FP64 BGK, resident in HBM -------------------------------
+    # ---- headline: plain FP64 BGK (by default), resident in HBM -------------------
     launches0 = bclbm.native.launch_count()
-    with L.Solver(lat, f0, collision=L.BGK, precision="f64", tau=(args.tau, args.tau), force=F) as s:
+    hp = args.precision
+    hcoll = L.TRT if args.collision == "trt" else L.BGK
+    htau = (args.tau, tau_anti if hcoll == L.TRT else args.tau)
+    with L.Solver(lat, f0, collision=hcoll, precision=hp, tau=htau, force=F, exact=args.exact) as s:
         s.step(args.warmup)
         s.sync()
         torch.cuda.synchronize()
@@ -266,9 +269,10 @@ def run_mine(args, world, rank):
     total_ms = allreduce_max(world, tm["total_ms"])
     kernel_ms = tm["step_kernel_ms"] / args.steps
     mlups = world * lat.n_bulk * args.steps / (total_ms * 1e-3) / 1e6
-    bpu = BYTES_PER_UPDATE["f64"]
+    bpu = BYTES_PER_UPDATE[hp]
     achieved = lat.n_bulk * bpu / (kernel_ms * 1e-3) / 1e9
-    traffic = committed_traffic("k_single_d3q19_f64_bgk")
+    kernel_tag = f"k_single_d3q19_{hp}{'_exact' if args.exact else ''}_{args.collision}"
+    traffic = committed_traffic(kernel_tag)
 
     # ---- variants ----------------------------------------------------------------
     variants = {}
@@ -330,13 +334,13 @@ def run_mine(args, world, rank):
         line = {
             "metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": hp,
             "data": "synthetic: seeded periodic sphere pack (numpy default_rng), no dataset",
-            "config": workload_config(args, lat, phi, "bgk"),
+            "config": workload_config(args, lat, phi, args.collision),
             "hbm_gbs": achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "k_single<19,double,FMA,BGK> (pull stream + fused bounce-back)",
+                         "kernel": kernel_tag + " (pull stream + fused bounce-back)",
                          "bytes_per_update": bpu, "units_per_launch": lat.n_bulk,
                          "kernel_ms": kernel_ms},
             "cpu_baseline": cpu,
@@ -366,6 +370,10 @@ def main():
     ap.add_argument("--tau", type=float, default=0.8)
     ap.add_argument("--gx", type=float, default=1e-5)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "f16", "bf16"],
+                    help="storage of the headline run (f64 = plain FP64, the reference's precision)")
+    ap.add_argument("--collision", default="bgk", choices=["bgk", "trt"])
+    ap.add_argument("--exact", action="store_true", help="headline with the reference-order FP64 kernel")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
