@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -20,7 +22,7 @@ using namespace bclbm;
 struct bclbm_handle {
     int q = 0, nd = 0, nfields = 1, collision = 0, precision = 0;
     uint32_t flags = 0;
-    bool exact = false, trt = false, flux = false;
+    bool exact = false, trt = false, flux = false, fma64 = false;
     int n_nodes = 0, nf = 0, nf_pad = 0, ns = 0;
     double tau[2] = {1.0, 1.0};
     double sigma = 0.0, beta = 0.0, mom_x = 0.0, rho_ref = 1.0, scale = 1.0;
@@ -42,6 +44,7 @@ struct bclbm_handle {
     double* d_rho = nullptr;
     double* d_vel = nullptr;
     double* d_cg = nullptr;
+    float* d_cgf = nullptr;
     DevParams* d_params = nullptr;
     double* d_partials = nullptr;
     double* d_red = nullptr;
@@ -207,10 +210,42 @@ size_t footprint_bytes(const bclbm_desc* d, const Plan& p) {
     b += static_cast<size_t>(Q - 1) * pad * 4;                                             // neighbour table
     b += (static_cast<size_t>(p.nfields) + D) * pad * 8;                                   // macros
     b += pad * 4;                                                                          // slot -> bulk
-    if (d->collision == BCLBM_RK) b += (static_cast<size_t>(p.nf) + p.ns + 1) * 8;         // colour field
+    if (d->collision == BCLBM_RK)                                                           // colour field
+        b += (static_cast<size_t>(p.nf) + p.ns + 1) * (d->precision == BCLBM_F64 ? 8 : 12);
     b += (static_cast<size_t>(grid_for(p.nf)) * 6 + 64) * 8;                               // reduction partials
     return b;
 }
+
+template <int Q>
+fx::Consts fixed_consts_q(const bclbm_handle* h) {
+    using L = Lat<Q>;
+    fx::Consts K;
+    std::memset(&K, 0, sizeof(K));
+    const double oms = 1.0 / h->tau[0], oma = 1.0 / h->tau[1];
+    const double tsf = 1 - 0.5 / h->tau[0], taf = 1 - 0.5 / h->tau[1];
+    K.alpha = fx::param(1.0 - 0.5 * (oms + oma));
+    K.beta = fx::param(0.5 * (oma - oms));
+    K.alpha_rest = fx::param(1.0 - oms);
+    const double wc[3] = {L::w(L::REST), L::w(0), L::w(L::NP - 1)};
+    for (int c = 0; c < 3; ++c) {
+        K.oms_w[c] = fx::param(oms * wc[c]);
+        K.oma3_w[c] = fx::param(3.0 * oma * wc[c]);
+        K.ktsf_w[c] = fx::param(-3.0 * wc[c] * tsf);
+    }
+    const double* F = h->force;
+    for (int q = 0; q < Q; ++q) {
+        const double cF = L::cx(q) * F[0] + L::cy(q) * F[1] + L::cz(q) * F[2];
+        K.kf9[q] = fx::param(9.0 * L::w(q) * tsf * cF);
+        K.ka3[q] = fx::param(3.0 * L::w(q) * taf * cF);
+    }
+    for (int d = 0; d < 3; ++d) {
+        K.force[d] = fx::param(F[d]);
+        K.half_force[d] = fx::param(0.5 * F[d]);
+    }
+    return K;
+}
+
+fx::Consts fixed_consts(const bclbm_handle* h) { return h->q == 9 ? fixed_consts_q<9>(h) : fixed_consts_q<19>(h); }
 
 StepArgs make_args(const bclbm_handle* h) {
     StepArgs a;
@@ -218,9 +253,11 @@ StepArgs make_args(const bclbm_handle* h) {
     a.L.nf = h->nf;
     a.L.nf_pad = h->nf_pad;
     a.L.ns = h->ns;
-    a.L.nbr = h->d_nbr;
+    a.L.nbr = h->collision == BCLBM_RK ? h->d_nbr : nullptr;
+    a.L.pull = h->collision == BCLBM_RK ? nullptr : h->d_nbr;
     for (int q = 0; q < 19; ++q) a.L.ghost_src[q] = h->ghost_src[q];
     a.cg = h->d_cg;
+    a.cgf = h->d_cgf;
     a.params = h->d_params;
     a.tau = h->tau[0];
     a.tau_anti = h->tau[1];
@@ -239,6 +276,19 @@ StepArgs make_args(const bclbm_handle* h) {
     a.inv_scale = 1.0 / h->scale;
     a.partials = h->d_partials;
     a.n_bulk = h->nf;
+    a.f_tau_inv = static_cast<float>(a.tau_inv);
+    a.f_tauA_inv = static_cast<float>(a.tauA_inv);
+    a.f_tf = static_cast<float>(a.tf);
+    a.f_taf = static_cast<float>(a.taf);
+    a.f_rho_ref = static_cast<float>(a.rho_ref);
+    a.f_scale = static_cast<float>(a.scale);
+    a.f_inv_scale = static_cast<float>(a.inv_scale);
+    a.f_nu0inv = static_cast<float>(a.nu0inv);
+    a.f_nu1inv = static_cast<float>(a.nu1inv);
+    a.f_sigma = static_cast<float>(a.sigma);
+    a.f_beta = static_cast<float>(a.beta);
+    a.fx_flag = h->d_params ? &h->d_params->fx_overflow : nullptr;
+    a.fxk = fixed_consts(h);
     return a;
 }
 
@@ -284,6 +334,7 @@ void free_all(bclbm_handle* h) {
     cudaFree(h->d_rho);
     cudaFree(h->d_vel);
     cudaFree(h->d_cg);
+    cudaFree(h->d_cgf);
     cudaFree(h->d_params);
     cudaFree(h->d_partials);
     cudaFree(h->d_red);
@@ -358,6 +409,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     h->flags = d->flags;
     h->exact = (d->flags & BCLBM_FLAG_EXACT) != 0 || (d->collision == BCLBM_RK && d->precision == BCLBM_F64);
     h->trt = d->collision == BCLBM_TRT;
+    h->fma64 = (d->flags & BCLBM_FLAG_FP64_FMA) != 0;
     h->flux = d->collision == BCLBM_RK && d->flux_control != 0;
     h->n_nodes = d->n_nodes;
     h->nf = p.nf;
@@ -394,12 +446,6 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         }                                                                               \
     } while (0)
 
-    // extended neighbour table in device numbering
-    std::vector<int32_t> tab(static_cast<size_t>(R) * pad, static_cast<int32_t>(h->nf + h->ns));
-    for (int s = 0; s < h->nf; ++s) {
-        const size_t n = static_cast<size_t>(h->slot_node[s]);
-        for (int q = 0; q < R; ++q) tab[static_cast<size_t>(q) * pad + s] = p.ext_of_node[d->neigh[n * Q + q]];
-    }
     // ghost sources: last bulk node (bulk order) whose neighbour along c_p is node 0
     std::vector<int32_t> slot_of_bulk(h->nf);
     for (int s = 0; s < h->nf; ++s) slot_of_bulk[h->slot_bulk[s]] = s;
@@ -410,6 +456,37 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
                 h->ghost_src[pdir] = slot_of_bulk[b];
                 break;
             }
+    std::vector<int32_t> tab;
+    if (h->collision == BCLBM_RK) {
+        // extended neighbour table in device numbering (pull + colour gradient)
+        tab.assign(static_cast<size_t>(R) * pad, static_cast<int32_t>(h->nf + h->ns));
+        for (int s = 0; s < h->nf; ++s) {
+            const size_t n = static_cast<size_t>(h->slot_node[s]);
+            for (int q = 0; q < R; ++q) tab[static_cast<size_t>(q) * pad + s] = p.ext_of_node[d->neigh[n * Q + q]];
+        }
+    } else {
+        // resolved pull table: element index (row * pad + slot) of the post-collision
+        // value that streams into slot s along c_q (fluid upstream, wall, or ghost)
+        if (static_cast<size_t>(Q) * pad > static_cast<size_t>(INT32_MAX)) {
+            std::fprintf(stderr, "bclbm_create: %d fluid nodes exceed the int32 pull table\n", h->nf);
+            free_all(h);
+            delete h;
+            return BCLBM_ERR_UNSUPPORTED;
+        }
+        tab.assign(static_cast<size_t>(R) * pad, 0);
+        for (int s = 0; s < h->nf; ++s) {
+            const size_t n = static_cast<size_t>(h->slot_node[s]);
+            for (int q = 0; q < R; ++q) {
+                const int rq = rev_dir(Q, q);
+                const int y = d->neigh[n * Q + rq];
+                int64_t e;
+                if (y != 0 && d->types[y] > 1) e = static_cast<int64_t>(q) * pad + p.ext_of_node[y];
+                else if (y == 0) e = static_cast<int64_t>(rq) * pad + h->ghost_src[rq];
+                else e = static_cast<int64_t>(rq) * pad + s;
+                tab[static_cast<size_t>(q) * pad + s] = static_cast<int32_t>(e);
+            }
+        }
+    }
     CREATE_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     const size_t sb = store_bytes(h->precision);
     const size_t pop_bytes = static_cast<size_t>(h->nfields) * Q * pad * sb;
@@ -426,7 +503,11 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     CREATE_TRY(cudaMemcpyAsync(h->d_slot_bulk, h->slot_bulk.data(), h->nf * sizeof(int32_t), cudaMemcpyHostToDevice,
                                h->stream));
     DevParams prm;
-    for (int k = 0; k < 3; ++k) prm.force[k] = h->force[k];
+    std::memset(&prm, 0, sizeof(prm));
+    for (int k = 0; k < 3; ++k) {
+        prm.force[k] = h->force[k];
+        prm.forcef[k] = static_cast<float>(h->force[k]);
+    }
     CREATE_TRY(cudaMemcpyAsync(h->d_params, &prm, sizeof(prm), cudaMemcpyHostToDevice, h->stream));
 
     // colour field: fluid slots (written every step), stored solids (fixed), ghost (0)
@@ -444,6 +525,11 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             cg[static_cast<size_t>(h->nf) + k] = h->solid_cg[k];
         }
         CREATE_TRY(cudaMemcpyAsync(h->d_cg, cg.data(), ncg * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        if (h->precision != BCLBM_F64) {
+            std::vector<float> cgf(cg.begin(), cg.end());
+            CREATE_TRY(cudaMalloc(&h->d_cgf, ncg * sizeof(float)));
+            CREATE_TRY(cudaMemcpyAsync(h->d_cgf, cgf.data(), ncg * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+        }
         CREATE_TRY(cudaStreamSynchronize(h->stream));
     }
 
@@ -504,6 +590,8 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
         if (h->collision != BCLBM_RK) {
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
             if (h->exact) CUDA_TRY(h, launch_single_exact(h->q, h->trt, local, a, h->stream));
+            else if (h->precision == BCLBM_F64 && !h->fma64)
+                CUDA_TRY(h, launch_single_fixed(h->q, h->trt, local, a, h->stream));
             else CUDA_TRY(h, launch_single_fast(h->q, h->precision, h->trt, local, a, h->stream));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
         } else {
@@ -603,11 +691,20 @@ int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg)
     std::vector<double> r(static_cast<size_t>(h->nfields) * pad), v(static_cast<size_t>(h->nd) * pad), c;
     CUDA_TRY(h, cudaMemcpyAsync(r.data(), h->d_rho, r.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(v.data(), h->d_vel, v.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    std::vector<float> cf;
     if (cg && h->collision == BCLBM_RK) {
         c.resize(h->nf);
-        CUDA_TRY(h, cudaMemcpyAsync(c.data(), h->d_cg, c.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        if (h->d_cgf) {
+            cf.resize(h->nf);
+            CUDA_TRY(h, cudaMemcpyAsync(cf.data(), h->d_cgf, cf.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                                        h->stream));
+        } else {
+            CUDA_TRY(h, cudaMemcpyAsync(c.data(), h->d_cg, c.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                        h->stream));
+        }
     }
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    for (size_t k = 0; k < cf.size(); ++k) c[k] = cf[k];
     for (int s = 0; s < h->nf; ++s) {
         const size_t n = static_cast<size_t>(h->slot_node[s]);
         if (rho)
@@ -645,6 +742,10 @@ int bclbm_reduce(bclbm_handle* h, bclbm_stats* out) {
     out->n_bulk = h->nf;
     out->steps_done = h->steps_done;
     out->nonfinite = std::isfinite(red[5]) && std::isfinite(red[0]) && std::isfinite(red[1]) ? 0 : 1;
+    if (prm.fx_overflow) {
+        out->nonfinite = 1;
+        return fail(h, BCLBM_ERR_NONFINITE, "a node left the fixed-point range (sum |f| < 8, rho > 0.15)");
+    }
     return out->nonfinite ? fail(h, BCLBM_ERR_NONFINITE, "NaN or Inf in the populations") : BCLBM_OK;
 }
 
@@ -652,8 +753,12 @@ int bclbm_set_force(bclbm_handle* h, const double force[3]) {
     if (!h || !force) return BCLBM_ERR_INVALID;
     CUDA_TRY(h, cudaSetDevice(h->device));
     DevParams prm;
-    for (int k = 0; k < 3; ++k) prm.force[k] = h->force[k] = force[k];
-    CUDA_TRY(h, cudaMemcpyAsync(h->d_params, &prm, sizeof(prm), cudaMemcpyHostToDevice, h->stream));
+    for (int k = 0; k < 3; ++k) {
+        prm.force[k] = h->force[k] = force[k];
+        prm.forcef[k] = static_cast<float>(force[k]);
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_params, &prm, offsetof(DevParams, fx_overflow), cudaMemcpyHostToDevice,
+                                h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return BCLBM_OK;
 }

@@ -129,7 +129,10 @@ struct LatticeView {
     int nf;          // fluid (bulk) slots
     int nf_pad;      // row stride of pops / nbr
     int ns;          // stored solid nodes; nbr value nf+ns is the ghost node
-    const int32_t* nbr;
+    const int32_t* nbr;   // extended neighbour table (two-phase instances)
+    const int32_t* pull;  // single-phase instances: [Q-1][nf_pad] element index (row * nf_pad + slot)
+                          // of the post-collision value that streams into slot i along c_q, with
+                          // the bounce-back and ghost cases of pull_raw resolved at set-up
     int32_t ghost_src[19];
 };
 

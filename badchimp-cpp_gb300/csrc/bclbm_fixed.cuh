@@ -1,0 +1,360 @@
+// 64-bit fixed-point arithmetic for the FP64-storage collision.
+//
+// GB300 executes FP64 at about 1/64 of its FP32 rate, so an FP64 BGK/TRT
+// collision (~200 FP64 instructions per node update) saturates the FP64 pipe
+// at ~15 % of HBM bandwidth.  The integer pipes have the throughput.  Values
+// are held as int64 with FB = 60 fractional bits (range |x| < 8, resolution
+// 2^-60 = 8.7e-19).  LB populations of a fluid with rho ~ 1 are O(w_q) > 0.02,
+// so the resolution is finer than an FP64 ulp of any population (>= 3.5e-18),
+// sums of populations are exact, and each product is rounded to nearest once.
+// Results are rounded back to FP64.  Values of magnitude >= 8 cannot be held:
+// they saturate and raise a flag the host reads (bclbm_reduce).
+//
+// Everything here is __host__ __device__ so that the arithmetic can be tested
+// on the CPU against 128-bit integer references.
+#pragma once
+
+#include <cstdint>
+
+#include "bclbm_device.cuh"
+
+#ifndef __CUDACC__
+#define __host__
+#define __device__
+#define __forceinline__ inline
+#endif
+
+namespace bclbm {
+namespace fx {
+
+constexpr int FB = 60;
+constexpr int64_t ONE = int64_t(1) << FB;
+
+__host__ __device__ __forceinline__ uint64_t bits_of(double d) {
+#ifdef __CUDA_ARCH__
+    return static_cast<uint64_t>(__double_as_longlong(d));
+#else
+    uint64_t b;
+    __builtin_memcpy(&b, &d, 8);
+    return b;
+#endif
+}
+
+__host__ __device__ __forceinline__ double double_of(uint64_t b) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double(static_cast<long long>(b));
+#else
+    double d;
+    __builtin_memcpy(&d, &b, 8);
+    return d;
+#endif
+}
+
+__host__ __device__ __forceinline__ int clz64(uint64_t a) {
+#ifdef __CUDA_ARCH__
+    return __clzll(static_cast<long long>(a));
+#else
+    return a ? __builtin_clzll(a) : 64;
+#endif
+}
+
+// high 64 bits of the signed 128-bit product
+__host__ __device__ __forceinline__ int64_t mulhi(int64_t a, int64_t b) {
+#ifdef __CUDA_ARCH__
+    return __mul64hi(static_cast<long long>(a), static_cast<long long>(b));
+#else
+    return static_cast<int64_t>((static_cast<__int128>(a) * static_cast<__int128>(b)) >> 64);
+#endif
+}
+
+// a * b / 2^FB, rounded to nearest (ties toward +inf), through __mul64hi
+__host__ __device__ __forceinline__ int64_t mul(int64_t a, int64_t b) {
+    const uint64_t lo = static_cast<uint64_t>(a) * static_cast<uint64_t>(b);
+    int64_t hi = mulhi(a, b);
+    const uint64_t lo2 = lo + (uint64_t(1) << (FB - 1));
+    hi += (lo2 < lo) ? 1 : 0;
+    return static_cast<int64_t>((static_cast<uint64_t>(hi) << (64 - FB)) | (lo2 >> FB));
+}
+
+// The kernel's products, by operand signs (uu: both >= 0, su: b >= 0, ss).
+// All equal mul() bit for bit.
+// hi:lo of the unsigned 128-bit product a b + 2^59 (the rounding constant),
+// from four 32 x 32 -> 64 partial products that share their carries.
+__host__ __device__ __forceinline__ void umul128_round(uint64_t a, uint64_t b, uint64_t& hi, uint32_t& lo_hi) {
+#ifdef __CUDA_ARCH__
+    const uint32_t a0 = static_cast<uint32_t>(a), a1 = static_cast<uint32_t>(a >> 32);
+    const uint32_t b0 = static_cast<uint32_t>(b), b1 = static_cast<uint32_t>(b >> 32);
+    const uint64_t p00 = static_cast<uint64_t>(a0) * b0;
+    // + 2^27 at weight 2^32 is the rounding constant 2^59; the sum stays below 2^64
+    const uint64_t p01 = static_cast<uint64_t>(a0) * b1 + ((p00 >> 32) + (uint64_t(1) << 27));
+    const uint64_t p10 = static_cast<uint64_t>(a1) * b0 + static_cast<uint32_t>(p01);
+    hi = static_cast<uint64_t>(a1) * b1 + (p01 >> 32) + (p10 >> 32);
+    lo_hi = static_cast<uint32_t>(p10);  // bits [32, 64) of the low word
+#else
+    const unsigned __int128 p = static_cast<unsigned __int128>(a) * b + (static_cast<unsigned __int128>(1) << (FB - 1));
+    hi = static_cast<uint64_t>(p >> 64);
+    lo_hi = static_cast<uint32_t>(static_cast<uint64_t>(p) >> 32);
+#endif
+}
+
+// bits [60, 124) of the 128-bit product
+__host__ __device__ __forceinline__ int64_t combine(uint64_t hi, uint32_t lo_hi) {
+    return static_cast<int64_t>((hi << (64 - FB)) | (lo_hi >> (FB - 32)));
+}
+
+// a b / 2^FB rounded to nearest, for a, b >= 0
+__host__ __device__ __forceinline__ int64_t mul_uu(int64_t a, int64_t b) {
+    uint64_t hi;
+    uint32_t lh;
+    umul128_round(static_cast<uint64_t>(a), static_cast<uint64_t>(b), hi, lh);
+    return combine(hi, lh);
+}
+
+// a signed, b >= 0: the two's-complement pattern of a is a + 2^64 when a < 0, so
+// the signed product's high word is the unsigned one minus b
+__host__ __device__ __forceinline__ int64_t mul_su(int64_t a, int64_t b) {
+    uint64_t hi;
+    uint32_t lh;
+    umul128_round(static_cast<uint64_t>(a), static_cast<uint64_t>(b), hi, lh);
+    hi -= static_cast<uint64_t>(a >> 63) & static_cast<uint64_t>(b);
+    return combine(hi, lh);
+}
+
+// both signed
+__host__ __device__ __forceinline__ int64_t mul_ss(int64_t a, int64_t b) {
+    uint64_t hi;
+    uint32_t lh;
+    umul128_round(static_cast<uint64_t>(a), static_cast<uint64_t>(b), hi, lh);
+    hi -= (static_cast<uint64_t>(a >> 63) & static_cast<uint64_t>(b)) + (static_cast<uint64_t>(b >> 63) & static_cast<uint64_t>(a));
+    return combine(hi, lh);
+}
+
+// FP64 -> fixed, rounded to nearest; |d| >= 8 saturates and sets ovf.
+__host__ __device__ __forceinline__ int64_t from_f64(double d, int& ovf) {
+    const uint64_t b = bits_of(d);
+    const int e = static_cast<int>((b >> 52) & 0x7FF);
+    const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (uint64_t(1) << 52);
+    const int sh = e - 1075 + FB;  // d = m 2^(e - 1075)
+    uint64_t mag;
+    if (e == 0) {
+        mag = 0;  // zero or subnormal
+    } else if (sh >= 0) {
+        if (sh > 10 || e == 0x7FF) {
+            ovf = 1;
+            mag = uint64_t(7) << FB;
+        } else {
+            mag = m << sh;
+        }
+    } else if (sh > -64) {
+        mag = (m + (uint64_t(1) << (-sh - 1))) >> (-sh);
+    } else {
+        mag = 0;
+    }
+    return (b >> 63) ? -static_cast<int64_t>(mag) : static_cast<int64_t>(mag);
+}
+
+// fixed -> FP64, rounded to nearest (ties away from zero)
+__host__ __device__ __forceinline__ double to_f64(int64_t x) {
+    if (x == 0) return 0.0;
+    const uint64_t s = static_cast<uint64_t>(x) >> 63;
+    const uint64_t a = s ? static_cast<uint64_t>(-x) : static_cast<uint64_t>(x);
+    const int lz = clz64(a);
+    const uint64_t n = a << lz;
+    uint64_t m = (n >> 11) + ((n >> 10) & 1);
+    int e = 63 - lz - FB + 1023;
+    if (m >> 53) {
+        m >>= 1;
+        e += 1;
+    }
+    return double_of((s << 63) | (static_cast<uint64_t>(e) << 52) | (m & 0xFFFFFFFFFFFFFull));
+}
+
+// Conversions used by the kernel (BCLBM_FX_CONV):
+//   0  from_f64 / to_f64 above (generic integer code)
+//   1  integer code specialised for the common exponent ranges, funnel shifts
+//   2  hardware F2I.S64.F64 / I2F.F64.S64, the 2^60 scaling done as an
+//      integer add to the exponent field
+#ifndef BCLBM_FX_CONV
+#define BCLBM_FX_CONV 2
+#endif
+// the store side can use its own choice (default: the same)
+#ifndef BCLBM_FX_CONV_STORE
+#define BCLBM_FX_CONV_STORE BCLBM_FX_CONV
+#endif
+
+__host__ __device__ __forceinline__ int64_t load_f64(double d, int& ovf) {
+#if BCLBM_FX_CONV == 2 && defined(__CUDA_ARCH__)
+    const long long b = __double_as_longlong(d);
+    // 2^60 d: exponent + 60 (d = 0 stays 0; |d| >= 8 saturates in the conversion and
+    // is caught by the range guard of collide())
+    const long long bs = ((b & 0x7FF0000000000000ll) == 0) ? 0ll : b + (60ll << 52);
+    const long long r = __double2ll_rn(__longlong_as_double(bs));
+    if (((b >> 52) & 0x7FF) >= 1026) ovf = 1;
+    return r;
+#elif BCLBM_FX_CONV == 1 && defined(__CUDA_ARCH__)
+    const unsigned hi = static_cast<unsigned>(__double2hiint(d));
+    const unsigned lo = static_cast<unsigned>(__double2loint(d));
+    const int e = static_cast<int>((hi >> 20) & 0x7FF);
+    const int sh = e - 1075 + FB;
+    if (sh >= 0 && sh <= 10) {  // |d| in [2^-10, 8)
+        const unsigned mhi = (hi & 0xFFFFFu) | 0x100000u;
+        const unsigned rhi = __funnelshift_l(lo, mhi, sh);
+        const unsigned rlo = lo << sh;
+        int64_t r = static_cast<int64_t>((static_cast<uint64_t>(rhi) << 32) | rlo);
+        const int64_t sm = static_cast<int64_t>(static_cast<int>(hi) >> 31);  // 0 or -1
+        return (r ^ sm) - sm;
+    }
+    return from_f64(d, ovf);
+#else
+    return from_f64(d, ovf);
+#endif
+}
+
+__host__ __device__ __forceinline__ double store_f64(int64_t x) {
+#if BCLBM_FX_CONV_STORE == 2 && defined(__CUDA_ARCH__)
+    const long long b = __double_as_longlong(__ll2double_rn(x));
+    return __longlong_as_double(b == 0 ? 0ll : b - (60ll << 52));
+#elif BCLBM_FX_CONV_STORE == 1 && defined(__CUDA_ARCH__)
+    const int64_t sm = x >> 63;
+    const uint64_t a = static_cast<uint64_t>((x ^ sm) - sm);
+    const unsigned ahi = static_cast<unsigned>(a >> 32), alo = static_cast<unsigned>(a);
+    if (ahi != 0) {  // |x| >= 2^32
+        const int lz = __clz(static_cast<int>(ahi));
+        const unsigned nhi = __funnelshift_l(alo, ahi, lz);
+        const unsigned nlo = alo << lz;
+        uint64_t m = ((static_cast<uint64_t>(nhi) << 32 | nlo) >> 11) + ((nlo >> 10) & 1u);
+        const unsigned e = static_cast<unsigned>(63 - lz - FB + 1023) + static_cast<unsigned>(m >> 53);
+        const uint64_t bits = (static_cast<uint64_t>(sm) & 0x8000000000000000ull) |
+                              (static_cast<uint64_t>(e) << 52) | (m & 0xFFFFFFFFFFFFFull);
+        return __longlong_as_double(static_cast<long long>(bits));
+    }
+    return to_f64(x);
+#else
+    return to_f64(x);
+#endif
+}
+
+// Host-side conversion of a parameter (no overflow expected).
+inline int64_t param(double d) {
+    int ovf = 0;
+    return from_f64(d, ovf);
+}
+
+// Per-handle constants of the fixed-point BGK/TRT collision (see collide_fx).
+struct Consts {
+    int64_t alpha, beta, alpha_rest;  // 1 - (oms + oma)/2, (oma - oms)/2, 1 - oms
+    int64_t oms_w[3];                 // oms w_c            (c: 0 rest, 1 axis, 2 diagonal)
+    int64_t oma3_w[3];                // 3 oma w_c
+    int64_t ktsf_w[3];                // -3 w_c tsf
+    int64_t kf9[19];                  // 9 w_q tsf (c_q . F)
+    int64_t ka3[19];                  // 3 w_q taf (c_q . F)
+    int64_t force[3];                 // F
+    int64_t half_force[3];            // F / 2
+};
+
+// One BGK (TRT = false) or TRT collision in fixed point.  F holds the Q
+// populations on entry and the post-collision populations on exit; rho and u
+// receive the moments (u = (sum_q f c_q + F/2) / rho, Guo).  The algebra is the
+// regrouping by direction pairs of calcOmegaBGK(TRT) + calcDeltaOmegaF(TRT)
+// (src/lbsolver/LBcollision.h:27-75, 194-236):
+//   post_q  = alpha f_q + beta f_rq + X + Y,  post_rq = alpha f_rq + beta f_q + X - Y
+//   X = oms w rho (1 + 4.5 (c.u)^2 - 1.5 u^2) + w tsf (9 (c.F)(c.u) - 3 u.F)
+//   Y = 3 oma w rho (c.u) + 3 w taf (c.F)
+//   post_rest = (1 - oms) f_rest + oms w0 rho (1 - 1.5 u^2) - 3 w0 tsf u.F
+// ovf is set when the node's values do not fit the fixed-point range: the sum
+// of |f_q| must stay below 8 (it bounds rho and every momentum component) and
+// rho above 0.15 (1 / rho below 8).
+//
+// Weight classes: w_rest : w_axis : w_diag = 12 : 2 : 1 (D3Q19) and 16 : 4 : 1
+// (D2Q9), so the per-class products rho oms w_c, rho 3 oma w_c and
+// -3 w_c tsf u.F are exact integer multiples of the diagonal one.
+// Populations of a pair enter through P = f_q + f_rq and M = f_q - f_rq:
+//   alpha f_q + beta f_rq = (alpha + beta)/2 P + (alpha - beta)/2 M.
+template <int Q, bool TRT>
+__host__ __device__ __forceinline__ void collide(int64_t* F, const Consts& K, int64_t& rho_o, int64_t* u_o,
+                                                 int& ovf) {
+    constexpr int D = Lat<Q>::D, NP = Lat<Q>::NP, R = Lat<Q>::REST;
+    constexpr int SH1 = Q == 19 ? 1 : 2;  // w_axis / w_diag = 2 or 4
+    {
+        // sum_q |f_q| / 2^56 <= t + Q; t <= 108 keeps sum |f_q| below 127 * 2^56 < 8 * 2^60
+        int t = 0;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int h = static_cast<int>(F[q] >> 56);
+            t += h < 0 ? -h : h;
+        }
+        if (t > 108) ovf = 1;
+    }
+    int64_t rho = F[R];
+    int64_t J[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const int64_t Pk = F[k] + F[k + NP], Mk = F[k] - F[k + NP];
+        rho += Pk;
+        if (Lat<Q>::cx(k) > 0) J[0] += Mk;
+        if (Lat<Q>::cx(k) < 0) J[0] -= Mk;
+        if (Lat<Q>::cy(k) > 0) J[1] += Mk;
+        if (Lat<Q>::cy(k) < 0) J[1] -= Mk;
+        if (D == 3 && Lat<Q>::cz(k) > 0) J[2] += Mk;
+        if (D == 3 && Lat<Q>::cz(k) < 0) J[2] -= Mk;
+    }
+    // 1 / rho: FP32 estimate (24 bits), one Newton step in fixed point (48 bits):
+    // u = (J + F/2) / rho is O(1e-2) or less, so its absolute error stays below 2^-60
+    const float rf = static_cast<float>(rho) * 8.67361737988403547e-19f;  // 2^-60
+    if (!(rf > 0.15f)) ovf = 1;
+#ifdef __CUDA_ARCH__
+    const float ri = __frcp_rn(rf);
+#else
+    const float ri = 1.0f / rf;
+#endif
+    int64_t inv = static_cast<int64_t>(ri * 1.152921504606846976e18f);  // 2^60
+    inv = mul_uu(inv, 2 * ONE - mul_uu(rho, inv));
+    int64_t u[3], ua[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        u[d] = (d < D) ? mul_su(J[d] + K.half_force[d], inv) : 0;
+        ua[d] = u[d] < 0 ? -u[d] : u[d];
+    }
+    rho_o = rho;
+#pragma unroll
+    for (int d = 0; d < D; ++d) u_o[d] = u[d];
+    int64_t uu = mul_uu(ua[0], ua[0]) + mul_uu(ua[1], ua[1]);
+    if (D == 3) uu += mul_uu(ua[2], ua[2]);
+    int64_t uF = mul_ss(u[0], K.force[0]) + mul_ss(u[1], K.force[1]);
+    if (D == 3) uF += mul_ss(u[2], K.force[2]);
+    const int64_t base = ONE - (uu + (uu >> 1));  // 1 - 1.5 u^2
+    // diagonal-class products, the others by the exact weight ratios
+    const int64_t A2 = mul_uu(rho, K.oms_w[2]);
+    const int64_t B2 = mul_uu(rho, K.oma3_w[2]);
+    const int64_t K2 = mul_ss(uF, K.ktsf_w[2]);
+    const int64_t Aw[3] = {Q == 19 ? (A2 << 3) + (A2 << 2) : (A2 << 4), A2 << SH1, A2};
+    const int64_t Bw[3] = {0, B2 << SH1, B2};
+    const int64_t Kw[3] = {Q == 19 ? (K2 << 3) + (K2 << 2) : (K2 << 4), K2 << SH1, K2};
+    const int64_t AB2 = mul_uu(A2, base);
+    const int64_t ABw[3] = {Q == 19 ? (AB2 << 3) + (AB2 << 2) : (AB2 << 4), AB2 << SH1, AB2};
+    const int64_t hs = TRT ? (K.alpha + K.beta) >> 1 : K.alpha >> 1;  // (alpha + beta) / 2
+    const int64_t ha = TRT ? (K.alpha - K.beta) >> 1 : K.alpha >> 1;  // (alpha - beta) / 2
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const int c = Lat<Q>::wclass(k);
+        const int64_t cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];
+        const int64_t cua = cu < 0 ? -cu : cu;
+        const int64_t cu2 = mul_uu(cua, cua);
+        // X = Aw (4.5 cu^2 + base) + kf9 cu + Kw;  Y = Bw cu + ka3
+        int64_t X = ABw[c] + mul_uu(Aw[c], (cu2 << 2) + (cu2 >> 1)) + Kw[c];
+        // the force product vanishes for directions normal to the force; the
+        // (warp-uniform) branch also bounds how far the compiler interleaves the
+        // pairs, which keeps the kernel at ~114 registers and 2 blocks per SM
+        if (K.kf9[k] != 0) X += mul_ss(K.kf9[k], cu);
+        const int64_t Y = mul_su(cu, Bw[c]) + K.ka3[k];
+        // alpha f_q + beta f_rq = hs P + ha M
+        const int64_t sp = mul_ss(hs, F[k] + F[k + NP]);
+        const int64_t sm = mul_ss(ha, F[k] - F[k + NP]);
+        F[k] = sp + sm + X + Y;
+        F[k + NP] = sp - sm + X - Y;
+    }
+    F[R] = mul_ss(K.alpha_rest, F[R]) + ABw[0] + Kw[0];
+}
+
+}  // namespace fx
+}  // namespace bclbm

@@ -12,7 +12,10 @@ std::atomic<int64_t>& launch_counter() {
 __global__ void k_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params) {
     // meanfcXGlobal /= numNodesGlobal; bodyForce.x = 2 * (setMomX - meanfcXGlobal)
     // (src/twophase/main_TWOPHASE.cpp:301-308)
-    if (threadIdx.x == 0 && blockIdx.x == 0) params->force[0] = 2 * (mom_x - sum[0] * inv_n);
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        params->force[0] = 2 * (mom_x - sum[0] * inv_n);
+        params->forcef[0] = static_cast<float>(params->force[0]);
+    }
 }
 
 namespace {
@@ -26,6 +29,20 @@ cudaError_t single_fast_qs(bool trt, bool local, const StepArgs& a, cudaStream_t
     } else {
         if (local) k_single<Q, S, 1, false, true><<<g, kBlock, 0, s>>>(a);
         else k_single<Q, S, 1, false, false><<<g, kBlock, 0, s>>>(a);
+    }
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+template <int Q>
+cudaError_t single_fixed_q(bool trt, bool local, const StepArgs& a, cudaStream_t s) {
+    const int g = grid_for(a.L.nf);
+    if (trt) {
+        if (local) k_single_fixed<Q, true, true><<<g, kBlock, 0, s>>>(a);
+        else k_single_fixed<Q, true, false><<<g, kBlock, 0, s>>>(a);
+    } else {
+        if (local) k_single_fixed<Q, false, true><<<g, kBlock, 0, s>>>(a);
+        else k_single_fixed<Q, false, false><<<g, kBlock, 0, s>>>(a);
     }
     launch_counter()++;
     return cudaGetLastError();
@@ -123,6 +140,10 @@ cudaError_t moments_q(int precision, int nfields, bool local, const StepArgs& a,
 
 cudaError_t launch_single_fast(int Q, int precision, bool trt, bool local, const StepArgs& a, cudaStream_t s) {
     return Q == 9 ? single_fast_q<9>(precision, trt, local, a, s) : single_fast_q<19>(precision, trt, local, a, s);
+}
+
+cudaError_t launch_single_fixed(int Q, bool trt, bool local, const StepArgs& a, cudaStream_t s) {
+    return Q == 9 ? single_fixed_q<9>(trt, local, a, s) : single_fixed_q<19>(trt, local, a, s);
 }
 
 cudaError_t launch_rk_shift(int Q, int precision, bool local, bool flux, const StepArgs& a, cudaStream_t s,

@@ -17,6 +17,7 @@
 #include <type_traits>
 
 #include "bclbm_device.cuh"
+#include "bclbm_fixed.cuh"
 
 namespace bclbm {
 
@@ -25,6 +26,8 @@ constexpr double C2 = 1.0 / 3.0;  // DXQY::c2 = 1.0 / c2Inv
 
 struct DevParams {
     double force[3];
+    float forcef[3];  // the same force rounded to FP32, for the FP32-arithmetic kernels
+    int fx_overflow;  // set by the fixed-point kernel when a value left its range
 };
 
 struct StepArgs {
@@ -33,7 +36,8 @@ struct StepArgs {
     void* dst;              // post-collision output
     double* rho_out;        // [nfields][nf_pad] when MACROS
     double* vel_out;        // [D][nf_pad] when MACROS
-    double* cg;             // RK: colour of [nf fluid | ns solids | ghost]
+    double* cg;             // RK, F64: colour of [nf fluid | ns solids | ghost]
+    float* cgf;             // RK, shifted formats: the same colour field in FP32
     const DevParams* params;
     double tau, tau_anti;   // single phase: relaxation times; RK: unused
     double tau_inv, tf;     // exact single phase: 1/tau, 1 - 0.5/tau (host-computed like the reference)
@@ -44,6 +48,11 @@ struct StepArgs {
     double scale, inv_scale;// shifted storage scale
     double* partials;       // per-block partial sums (flux controller)
     int n_bulk;             // RK flux controller divisor
+    // FP32 copies of the parameters above, rounded on the host, for the FP32-arithmetic
+    // kernels (a double -> float conversion in every thread runs on the FP64 pipe)
+    float f_tau_inv, f_tauA_inv, f_tf, f_taf, f_rho_ref, f_scale, f_inv_scale, f_nu0inv, f_nu1inv, f_sigma, f_beta;
+    int* fx_flag;           // &params->fx_overflow
+    fx::Consts fxk;         // constants of the fixed-point collision
 };
 
 // ---------------------------------------------------------------------------
@@ -123,7 +132,9 @@ __device__ __forceinline__ double cnorm_ref(int wclass) {  // DXQY::cNorm (SQRT2
 // ---------------------------------------------------------------------------
 // Population access
 // ---------------------------------------------------------------------------
-template <int Q, class S, bool LOCAL>
+// PULL: single-phase instances read the resolved pull table, two-phase
+// instances the extended neighbour table (which the colour gradient needs too).
+template <int Q, class S, bool LOCAL, bool PULL = false>
 __device__ __forceinline__ void load_field(const S* __restrict__ g, const LatticeView& L, int i,
                                            typename Store<S>::T* v) {
     constexpr int R = Lat<Q>::REST;
@@ -131,6 +142,8 @@ __device__ __forceinline__ void load_field(const S* __restrict__ g, const Lattic
     for (int q = 0; q < Q; ++q) {
         if (q == R || LOCAL) {
             v[q] = g[static_cast<size_t>(q) * L.nf_pad + i];
+        } else if (PULL) {
+            v[q] = g[__ldg(L.pull + static_cast<size_t>(q) * L.nf_pad + i)];
         } else {
             const int y = __ldg(L.nbr + static_cast<size_t>(Lat<Q>::rev(q)) * L.nf_pad + i);
             v[q] = pull_raw<Q, S>(g, L, q, y, i);
@@ -293,7 +306,7 @@ __global__ void __launch_bounds__(kBlock) k_single(StepArgs a) {
     if (i >= a.L.nf) return;
     using T = typename Store<S>::T;
     T v[Q];
-    load_field<Q, S, LOCAL>(static_cast<const S*>(a.src), a.L, i, v);
+    load_field<Q, S, LOCAL, true>(static_cast<const S*>(a.src), a.L, i, v);
     S* out = static_cast<S*>(a.dst);
     if constexpr (MODE == 0) {
         double f[Q], F[3], rho, vel[3];
@@ -311,22 +324,75 @@ __global__ void __launch_bounds__(kBlock) k_single(StepArgs a) {
 #pragma unroll
         for (int q = 0; q < Q; ++q) out[static_cast<size_t>(q) * a.L.nf_pad + i] = f[q];
     } else {
-        using C = typename std::conditional<std::is_same<S, double>::value, double, float>::type;
+        constexpr bool F64 = std::is_same<S, double>::value;
+        using C = typename std::conditional<F64, double, float>::type;
         C f[Q], F[3], rho, vel[3];
-        decode<Q, S, C>(v, f, static_cast<C>(a.inv_scale));
-        F[0] = static_cast<C>(a.params->force[0]);
-        F[1] = static_cast<C>(a.params->force[1]);
-        F[2] = static_cast<C>(a.params->force[2]);
-        const C oms = static_cast<C>(a.tau_inv), oma = static_cast<C>(TRT ? a.tauA_inv : a.tau_inv);
-        const C tsf = static_cast<C>(a.tf), taf = static_cast<C>(TRT ? a.taf : a.tf);
-        collide_fast<Q, C, TRT, Store<S>::shifted>(f, F, oms, oma, tsf, taf, static_cast<C>(a.rho_ref), rho, vel);
+        C oms, oma, tsf, taf, rho_ref, scale, inv_scale;
+        if constexpr (F64) {
+            F[0] = a.params->force[0];
+            F[1] = a.params->force[1];
+            F[2] = a.params->force[2];
+            oms = a.tau_inv;
+            oma = TRT ? a.tauA_inv : a.tau_inv;
+            tsf = a.tf;
+            taf = TRT ? a.taf : a.tf;
+            rho_ref = a.rho_ref;
+            scale = a.scale;
+            inv_scale = a.inv_scale;
+        } else {
+            F[0] = a.params->forcef[0];
+            F[1] = a.params->forcef[1];
+            F[2] = a.params->forcef[2];
+            oms = a.f_tau_inv;
+            oma = TRT ? a.f_tauA_inv : a.f_tau_inv;
+            tsf = a.f_tf;
+            taf = TRT ? a.f_taf : a.f_tf;
+            rho_ref = a.f_rho_ref;
+            scale = a.f_scale;
+            inv_scale = a.f_inv_scale;
+        }
+        decode<Q, S, C>(v, f, inv_scale);
+        collide_fast<Q, C, TRT, Store<S>::shifted>(f, F, oms, oma, tsf, taf, rho_ref, rho, vel);
         if (MACROS) {
             a.rho_out[i] = static_cast<double>(rho);
 #pragma unroll
             for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * a.L.nf_pad + i] = static_cast<double>(vel[d]);
         }
-        encode_store<Q, S, C>(out, a.L.nf_pad, i, f, static_cast<C>(a.scale));
+        encode_store<Q, S, C>(out, a.L.nf_pad, i, f, scale);
     }
+}
+
+// ---------------------------------------------------------------------------
+// k_single_fixed: one single-phase step on F64 storage with 64-bit fixed-point
+// arithmetic (bclbm_fixed.cuh).  BCLBM_FX_MINB is the minimum number of
+// resident blocks per SM requested from the register allocator.
+// ---------------------------------------------------------------------------
+#ifndef BCLBM_FX_MINB
+#define BCLBM_FX_MINB 1
+#endif
+
+template <int Q, bool TRT, bool LOCAL>
+__global__ void __launch_bounds__(kBlock, BCLBM_FX_MINB) k_single_fixed(StepArgs a) {
+    constexpr int D = Lat<Q>::D;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.L.nf) return;
+    double v[Q];
+    load_field<Q, double, LOCAL, true>(static_cast<const double*>(a.src), a.L, i, v);
+    int ovf = 0;
+    int64_t X[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) X[q] = fx::load_f64(v[q], ovf);
+    int64_t rho, u[3];
+    fx::collide<Q, TRT>(X, a.fxk, rho, u, ovf);
+    if (a.rho_out != nullptr) {
+        a.rho_out[i] = fx::store_f64(rho);
+#pragma unroll
+        for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * a.L.nf_pad + i] = fx::store_f64(u[d]);
+    }
+    double* out = static_cast<double*>(a.dst);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) out[static_cast<size_t>(q) * a.L.nf_pad + i] = fx::store_f64(X[q]);
+    if (ovf) atomicOr(a.fx_flag, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -450,7 +516,7 @@ __global__ void __launch_bounds__(kBlock) k_rk_density(StepArgs a) {
             load_field<Q, S, LOCAL>(g, a.L, i, v0);
             load_field<Q, S, LOCAL>(g + fs, a.L, i, v1);
             float rs = 0.f, dr = 0.f, jx = 0.f;
-            const float isc = static_cast<float>(a.inv_scale);
+            const float isc = a.f_inv_scale;
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
                 const float w = static_cast<float>(Lat<Q>::w(q));
@@ -459,8 +525,8 @@ __global__ void __launch_bounds__(kBlock) k_rk_density(StepArgs a) {
                 dr += Store<S>::val(v1[q]) * (w * isc);
                 jx += Lat<Q>::cx(q) * t;
             }
-            const float rho = static_cast<float>(a.rho_ref) + rs;
-            a.cg[i] = static_cast<double>(dr / rho);
+            const float rho = a.f_rho_ref + rs;
+            a.cgf[i] = dr / rho;
             fx = jx;
         }
     }
@@ -567,9 +633,9 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_shift(StepArgs a) {
     load_field<Q, S, LOCAL>(g + fs, a.L, i, v1);
     float sc[Q];
 #pragma unroll
-    for (int q = 0; q < Q - 1; ++q) sc[q] = static_cast<float>(a.cg[__ldg(a.L.nbr + static_cast<size_t>(q) * a.L.nf_pad + i)]);
+    for (int q = 0; q < Q - 1; ++q) sc[q] = a.cgf[__ldg(a.L.nbr + static_cast<size_t>(q) * a.L.nf_pad + i)];
     sc[R] = 0.f;
-    const float isc = static_cast<float>(a.inv_scale);
+    const float isc = a.f_inv_scale;
     float ft[Q], dc[Q];
     float rs = 0.f, dr = 0.f, j[3] = {0.f, 0.f, 0.f};
 #pragma unroll
@@ -583,16 +649,15 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_shift(StepArgs a) {
         j[1] += Lat<Q>::cy(q) * ft[q];
         j[2] += Lat<Q>::cz(q) * ft[q];
     }
-    const float F[3] = {static_cast<float>(a.params->force[0]), static_cast<float>(a.params->force[1]),
-                        static_cast<float>(a.params->force[2])};
-    const float rho_ref = static_cast<float>(a.rho_ref);
+    const float F[3] = {a.params->forcef[0], a.params->forcef[1], a.params->forcef[2]};
+    const float rho_ref = a.f_rho_ref;
     const float rho = rho_ref + rs;
     const float inv = 1.f / rho;
     const float rho0 = 0.5f * (rho + dr), rho1 = 0.5f * (rho - dr);
     float u[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) u[d] = (d < D) ? (j[d] + 0.5f * F[d]) * inv : 0.f;
-    const float om = 1.f / (3.f * rho / (rho0 * static_cast<float>(a.nu0inv) + rho1 * static_cast<float>(a.nu1inv)) + 0.5f);
+    const float om = 1.f / (3.f * rho / (rho0 * a.f_nu0inv + rho1 * a.f_nu1inv) + 0.5f);
     const float tf = 1.f - 0.5f * om;
     const float uu = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
     const float uF = u[0] * F[0] + u[1] * F[1] + u[2] * F[2];
@@ -609,10 +674,10 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_shift(StepArgs a) {
     }
     const float cgn = sqrtf(G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
     const float gs = 1.f / (cgn + (cgn < 1.1920929e-07f ? 1.f : 0.f));
-    const float af = 1.125f * cgn * static_cast<float>(a.sigma) * om;
-    const float rfb = static_cast<float>(a.beta) * rho0 * rho1 * inv;
+    const float af = 1.125f * cgn * a.f_sigma * om;
+    const float rfb = a.f_beta * rho0 * rho1 * inv;
     const float dcf = dr * inv;  // c0 - c1
-    const float sc_out = static_cast<float>(a.scale);
+    const float sc_out = a.f_scale;
     S* out = static_cast<S*>(a.dst);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -653,7 +718,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(StepArgs a, const int32_t* __
     if constexpr (NF == 1) {
         using T = typename Store<S>::T;
         T v[Q];
-        load_field<Q, S, LOCAL>(g, a.L, i, v);
+        load_field<Q, S, LOCAL, true>(g, a.L, i, v);
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             double f;
@@ -688,7 +753,7 @@ __global__ void __launch_bounds__(kBlock) k_moments(StepArgs a) {
         if constexpr (NF == 1) {
             using T = typename Store<S>::T;
             T v[Q];
-            load_field<Q, S, LOCAL>(g, a.L, i, v);
+            load_field<Q, S, LOCAL, true>(g, a.L, i, v);
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
                 if constexpr (Store<S>::shifted)

@@ -25,6 +25,7 @@ cudaError_t launch_rk_f64(int Q, bool local, bool flux, const StepArgs& a, cudaS
 
 // bclbm_kernels.cu
 cudaError_t launch_single_fast(int Q, int precision, bool trt, bool local, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_single_fixed(int Q, bool trt, bool local, const StepArgs& a, cudaStream_t s);
 cudaError_t launch_rk_shift(int Q, int precision, bool local, bool flux, const StepArgs& a, cudaStream_t s,
                             bool density);
 cudaError_t launch_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params, cudaStream_t s);

@@ -254,7 +254,8 @@ def run_mine(args, world, rank):
     hp = args.precision
     hcoll = L.TRT if args.collision == "trt" else L.BGK
     htau = (args.tau, tau_anti if hcoll == L.TRT else args.tau)
-    with L.Solver(lat, f0, collision=hcoll, precision=hp, tau=htau, force=F, exact=args.exact) as s:
+    with L.Solver(lat, f0, collision=hcoll, precision=hp, tau=htau, force=F, exact=args.exact,
+                  fma64=args.fma64) as s:
         s.step(args.warmup)
         s.sync()
         torch.cuda.synchronize()
@@ -271,16 +272,18 @@ def run_mine(args, world, rank):
     mlups = world * lat.n_bulk * args.steps / (total_ms * 1e-3) / 1e6
     bpu = BYTES_PER_UPDATE[hp]
     achieved = lat.n_bulk * bpu / (kernel_ms * 1e-3) / 1e9
-    kernel_tag = f"k_single_d3q19_{hp}{'_exact' if args.exact else ''}_{args.collision}"
+    arith = "exact" if args.exact else ("fma" if args.fma64 else ("fixed" if hp == "f64" else "fp32"))
+    kernel_tag = f"k_single_d3q19_{hp}_{arith}_{args.collision}"
     traffic = committed_traffic(kernel_tag)
 
     # ---- variants ----------------------------------------------------------------
     variants = {}
     if not args.no_variants:
         for tag, coll, prec in (("trt_f64", L.TRT, "f64"), ("bgk_f32", L.BGK, "f32"), ("bgk_f16", L.BGK, "f16"),
-                                ("bgk_bf16", L.BGK, "bf16"), ("bgk_f64_exact", L.BGK, "f64x")):
-            kw = dict(exact=True) if prec == "f64x" else {}
-            p = "f64" if prec == "f64x" else prec
+                                ("bgk_bf16", L.BGK, "bf16"), ("bgk_f64_exact", L.BGK, "f64x"),
+                                ("bgk_f64_fma", L.BGK, "f64fma")):
+            kw = dict(exact=True) if prec == "f64x" else (dict(fma64=True) if prec == "f64fma" else {})
+            p = "f64" if prec.startswith("f64") else prec
             with L.Solver(lat, f0, collision=coll, precision=p, tau=(args.tau, tau_anti if coll == L.TRT else args.tau),
                           force=F, **kw) as s:
                 vsteps = max(5, args.steps // 2)
@@ -374,6 +377,7 @@ def main():
                     help="storage of the headline run (f64 = plain FP64, the reference's precision)")
     ap.add_argument("--collision", default="bgk", choices=["bgk", "trt"])
     ap.add_argument("--exact", action="store_true", help="headline with the reference-order FP64 kernel")
+    ap.add_argument("--fma64", action="store_true", help="headline with the native-FP64 FMA kernel")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

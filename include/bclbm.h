@@ -59,7 +59,13 @@ extern "C" {
 #define BCLBM_RK 2  /* Rothman-Keller two-phase step of src/twophase/main_TWOPHASE.cpp:238-392 */
 
 /* population storage on the device */
-#define BCLBM_F64 0  /* plain FP64 populations, FP64 arithmetic */
+#define BCLBM_F64 0  /* plain FP64 populations; arithmetic: 64-bit fixed point with 2^-60
+                        resolution (finer than an FP64 ulp of any population of a fluid
+                        with rho ~ 1; needs sum_q |f_q| < 8 and rho > 0.15 per node,
+                        else bclbm_reduce reports BCLBM_ERR_NONFINITE), results rounded
+                        to FP64.  With
+                        BCLBM_FLAG_EXACT: FP64 in the reference's expression order;
+                        with BCLBM_FLAG_FP64_FMA: FP64 with FMA. */
 #define BCLBM_F32 1  /* FP32 shifted deviations (f - w*rho_ref)/w, FP32 arithmetic */
 #define BCLBM_F16 2  /* FP16 shifted, scaled deviations, FP32 arithmetic */
 #define BCLBM_BF16 3 /* BF16 shifted, scaled deviations, FP32 arithmetic */
@@ -69,6 +75,7 @@ extern "C" {
                                    contraction: results bit-identical to the reference */
 #define BCLBM_FLAG_SFC_ORDER 2u /* reorder fluid nodes along a Morton curve of their
                                    positions (needs pos); downloads keep reference order */
+#define BCLBM_FLAG_FP64_FMA 4u  /* BCLBM_F64 single phase: native FP64 arithmetic with FMA */
 
 typedef struct {
     int32_t lattice_q;        /* 9 or 19 */

@@ -1,0 +1,154 @@
+// Test harness: runs the fixed-point collision of csrc/bclbm_fixed.cuh on the
+// CPU (host branch of its __host__ __device__ functions, 128-bit integer
+// multiplies) so that its arithmetic can be checked against the reference
+// fixtures without a GPU.  Built by tests/test_fixed_point.py with nvcc as
+// host-only code; never part of the library.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "bclbm_fixed.cuh"
+
+using namespace bclbm;
+
+namespace {
+
+template <int Q>
+fx::Consts make_consts(bool trt, double tau, double tau_anti, const double* F) {
+    using L = Lat<Q>;
+    fx::Consts K;
+    std::memset(&K, 0, sizeof(K));
+    const double oms = 1.0 / tau, oma = trt ? 1.0 / tau_anti : oms;
+    const double tsf = 1 - 0.5 / tau, taf = trt ? 1 - 0.5 / tau_anti : tsf;
+    K.alpha = fx::param(1.0 - 0.5 * (oms + oma));
+    K.beta = fx::param(0.5 * (oma - oms));
+    K.alpha_rest = fx::param(1.0 - oms);
+    const double wc[3] = {L::w(L::REST), L::w(0), L::w(L::NP - 1)};
+    for (int c = 0; c < 3; ++c) {
+        K.oms_w[c] = fx::param(oms * wc[c]);
+        K.oma3_w[c] = fx::param(3.0 * oma * wc[c]);
+        K.ktsf_w[c] = fx::param(-3.0 * wc[c] * tsf);
+    }
+    for (int q = 0; q < Q; ++q) {
+        const double cF = L::cx(q) * F[0] + L::cy(q) * F[1] + L::cz(q) * F[2];
+        K.kf9[q] = fx::param(9.0 * L::w(q) * tsf * cF);
+        K.ka3[q] = fx::param(3.0 * L::w(q) * taf * cF);
+    }
+    for (int d = 0; d < 3; ++d) {
+        K.force[d] = fx::param(F[d]);
+        K.half_force[d] = fx::param(0.5 * F[d]);
+    }
+    return K;
+}
+
+template <int Q, bool TRT>
+int run(int n_nodes, const int32_t* neigh, const int16_t* types, int n_bulk, const int32_t* bulk, int steps,
+        double tau, double tau_anti, const double* F, double* f, double* rho_out, double* vel_out) {
+    using L = Lat<Q>;
+    const fx::Consts K = make_consts<Q>(TRT, tau, tau_anti, F);
+    // ghost sources: last bulk node whose neighbour along c_p is node 0
+    int gsrc[19] = {0};
+    for (int p = 0; p < Q - 1; ++p)
+        for (int b = n_bulk - 1; b >= 0; --b)
+            if (neigh[static_cast<size_t>(bulk[b]) * Q + p] == 0) {
+                gsrc[p] = bulk[b];
+                break;
+            }
+    std::vector<double> G(static_cast<size_t>(n_nodes) * Q, 0.0), G2(G.size(), 0.0);
+    int ovf = 0;
+    for (int s = 0; s < steps; ++s) {
+        for (int b = 0; b < n_bulk; ++b) {
+            const size_t x = static_cast<size_t>(bulk[b]);
+            int64_t Fx[Q];
+            for (int q = 0; q < Q; ++q) {
+                double v;
+                if (s == 0 || q == L::REST) {
+                    v = s == 0 ? f[x * Q + q] : G[x * Q + q];
+                } else {
+                    const int rq = L::rev(q);
+                    const int y = neigh[x * Q + rq];
+                    if (y != 0 && types[y] > 1) v = G[static_cast<size_t>(y) * Q + q];
+                    else if (y == 0) v = G[static_cast<size_t>(gsrc[rq]) * Q + rq];
+                    else v = G[x * Q + rq];
+                }
+                Fx[q] = fx::from_f64(v, ovf);
+            }
+            int64_t rho, u[3];
+            fx::collide<Q, TRT>(Fx, K, rho, u, ovf);
+            rho_out[x] = fx::to_f64(rho);
+            for (int d = 0; d < L::D; ++d) vel_out[x * L::D + d] = fx::to_f64(u[d]);
+            for (int q = 0; q < Q; ++q) G2[x * Q + q] = fx::to_f64(Fx[q]);
+        }
+        G.swap(G2);
+    }
+    // the reference's f after the last step: one pull of G
+    for (int b = 0; b < n_bulk; ++b) {
+        const size_t x = static_cast<size_t>(bulk[b]);
+        for (int q = 0; q < Q; ++q) {
+            double v;
+            if (q == L::REST) {
+                v = G[x * Q + q];
+            } else {
+                const int rq = L::rev(q);
+                const int y = neigh[x * Q + rq];
+                if (y != 0 && types[y] > 1) v = G[static_cast<size_t>(y) * Q + q];
+                else if (y == 0) v = G[static_cast<size_t>(gsrc[rq]) * Q + rq];
+                else v = G[x * Q + rq];
+            }
+            f[x * Q + q] = v;
+        }
+    }
+    return ovf;
+}
+
+}  // namespace
+
+extern "C" int fx_collide_ovf(double scale) {
+    // one D3Q19 rest-state node at rho = scale: does the collision flag it?
+    fx::Consts K;
+    std::memset(&K, 0, sizeof(K));
+    K.alpha = K.alpha_rest = fx::param(-0.25);
+    int ovf = 0;
+    int64_t F[19];
+    for (int q = 0; q < 19; ++q) F[q] = fx::from_f64(Lat<19>::w(q) * scale, ovf);
+    int64_t rho, u[3];
+    fx::collide<19, false>(F, K, rho, u, ovf);
+    return ovf;
+}
+
+extern "C" {
+
+int fx_run(int nq, int trt, int n_nodes, const int32_t* neigh, const int16_t* types, int n_bulk, const int32_t* bulk,
+           int steps, double tau, double tau_anti, const double* F, double* f, double* rho, double* vel) {
+    if (nq == 9) return trt ? run<9, true>(n_nodes, neigh, types, n_bulk, bulk, steps, tau, tau_anti, F, f, rho, vel)
+                            : run<9, false>(n_nodes, neigh, types, n_bulk, bulk, steps, tau, tau_anti, F, f, rho, vel);
+    return trt ? run<19, true>(n_nodes, neigh, types, n_bulk, bulk, steps, tau, tau_anti, F, f, rho, vel)
+               : run<19, false>(n_nodes, neigh, types, n_bulk, bulk, steps, tau, tau_anti, F, f, rho, vel);
+}
+
+// elementwise checks of the primitives; returns the number of failures
+int fx_primitives(const double* a, const double* b, int n) {
+    int bad = 0;
+    for (int i = 0; i < n; ++i) {
+        int ovf = 0;
+        const int64_t xa = fx::from_f64(a[i], ovf), xb = fx::from_f64(b[i], ovf);
+        // conversion: exact integer reference by long double (64-bit mantissa)
+        const long double ra = std::nearbyintl(static_cast<long double>(a[i]) * 1152921504606846976.0L);
+        if (std::fabs(static_cast<long double>(xa) - ra) > 1.0L) ++bad;
+        // round trip back to FP64: within half an ulp of FP64 and of the fixed resolution
+        const double back = fx::to_f64(xa);
+        const double tol = std::fabs(a[i]) * 1.2e-16 + 8.7e-19;
+        if (std::fabs(back - a[i]) > tol) ++bad;
+        // product: 128-bit reference, rounded to nearest
+        const __int128 p = static_cast<__int128>(xa) * static_cast<__int128>(xb);
+        const int64_t ref = static_cast<int64_t>((p + (static_cast<__int128>(1) << 59)) >> 60);
+        if (fx::mul(xa, xb) != ref) ++bad;
+        if (fx::mul_ss(xa, xb) != ref) ++bad;
+        if (xb >= 0 && fx::mul_su(xa, xb) != ref) ++bad;
+        if (xa >= 0 && xb >= 0 && fx::mul_uu(xa, xb) != ref) ++bad;
+    }
+    return bad;
+}
+
+}  // extern "C"

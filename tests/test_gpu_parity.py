@@ -4,7 +4,8 @@
   reference for every golden run, in reference order and in Morton order;
   runs with the flux controller differ only through the order of the global
   sum and stay within 1e-12;
-* restructured FP64 step (FMA): relative L2 error <= 1e-12 in f and rho; u
+* FP64-storage steps with 64-bit fixed-point arithmetic (the default) and with
+  native FP64 FMA arithmetic: relative L2 error <= 1e-12 in f and rho; u
   within 1e-12 of max |u| or the reference's own rounding floor of sum_q f c_q
   (see test_fast_f64_within_1e12);
 * FP32 / FP16 / BF16 shifted storage with FP32 arithmetic: errors against the
@@ -81,12 +82,15 @@ def test_exact_f64_matches_reference(bclbm, gpu, name, tag, sfc):
 SINGLE = [(n, t) for n, t in RUNS if not t.startswith("rk")]
 
 
+@pytest.mark.parametrize("arith", ["fixed", "fma"])
 @pytest.mark.parametrize("name,tag", SINGLE, ids=[f"{n}-{t}" for n, t in SINGLE])
-def test_fast_f64_within_1e12(bclbm, gpu, name, tag):
+def test_fast_f64_within_1e12(bclbm, gpu, name, tag, arith):
+    """BCLBM_F64 without BCLBM_FLAG_EXACT: 64-bit fixed-point arithmetic (default)
+    or native FP64 with FMA (BCLBM_FLAG_FP64_FMA)."""
     case = lbcases.Case(name, bclbm)
     run = case.runs[tag]
     exp = case.expected(tag)
-    with make_solver(case, run) as s:
+    with make_solver(case, run, fma64=(arith == "fma")) as s:
         s.step(run["steps"])
         got = outputs(case, run, s)
     assert relerr(got["f"], exp["f"]) <= 1e-12
@@ -130,6 +134,19 @@ def test_shifted_storage_two_phase(bclbm, gpu, prec, tol_sat, tol_u):
     sat_ref = exp["rho"][:, 0].sum() / exp["rho"].sum()
     assert abs(st["saturation"] - sat_ref) <= tol_sat
     assert relerr(got["vel"], exp["vel"][:, 0, :]) <= tol_u
+
+
+def test_fixed_point_overflow_is_reported(bclbm, gpu):
+    """Populations outside the fixed-point range |f| < 8 raise the overflow flag,
+    which bclbm_reduce reports as BCLBM_ERR_NONFINITE (no GPU fault)."""
+    case = lbcases.Case("box_12x10x8", bclbm)
+    run = case.runs["bgk_400"]
+    f0, _ = case.init(run)
+    for scale in (20.0, 0.05):  # rho = 20 and rho = 0.05 leave the range
+        with case.L.Solver(case.lat, f0 * scale, tau=(0.9, 0.9), force=case.force(run)) as s:
+            s.step(1)
+            with pytest.raises(bclbm.native.BclbmError, match="fixed-point range"):
+                s.reduce()
 
 
 def test_download_before_any_step_returns_initial_state(bclbm, gpu):
