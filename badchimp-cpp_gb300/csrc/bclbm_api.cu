@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
 #include <cstddef>
 #include <cmath>
@@ -12,6 +13,7 @@
 #include <new>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "bclbm.h"
@@ -83,6 +85,34 @@ int rev_dir(int Q, int q) {
     return q == 18 ? 18 : (q + 9) % 18;
 }
 
+// fn(begin, end) over [0, n) on the host cores, in contiguous chunks
+template <class F>
+void parallel_for(size_t n, F&& fn) {
+    const unsigned hw = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    const size_t nt = std::min<size_t>(hw, (n + 32767) / 32768);
+    if (nt <= 1) {
+        fn(size_t(0), n);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve(nt - 1);
+    for (size_t t = 1; t < nt; ++t) th.emplace_back([&fn, n, t, nt] { fn(n * t / nt, n * (t + 1) / nt); });
+    fn(size_t(0), n / nt);
+    for (auto& x : th) x.join();
+}
+
+// smallest index at which a parallel check failed (INT64_MAX: none)
+struct FirstBad {
+    std::atomic<int64_t> v{INT64_MAX};
+    void set(int64_t i) {
+        int64_t cur = v.load();
+        while (i < cur && !v.compare_exchange_weak(cur, i)) {
+        }
+    }
+    bool any() const { return v.load() != INT64_MAX; }
+    int64_t get() const { return v.load(); }
+};
+
 uint64_t spread_bits(uint64_t v, int dims) {
     uint64_t out = 0;
     for (int b = 0; b < 21; ++b)
@@ -117,22 +147,57 @@ int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full)
     p.nfields = d->collision == BCLBM_RK ? 2 : 1;
     const int32_t* nbr = d->neigh;
     const int16_t* ty = d->types;
-    for (size_t k = 0; k < static_cast<size_t>(N) * Q; ++k)
-        if (nbr[k] < 0 || nbr[k] >= N) {
-            err = "neighbour id out of range at entry " + std::to_string(k);
+    {
+        FirstBad bad;
+        parallel_for(static_cast<size_t>(N) * Q, [&](size_t b0, size_t b1) {
+            for (size_t k = b0; k < b1; ++k)
+                if (nbr[k] < 0 || nbr[k] >= N) {
+                    bad.set(static_cast<int64_t>(k));
+                    return;
+                }
+        });
+        if (bad.any()) {
+            err = "neighbour id out of range at entry " + std::to_string(bad.get());
             return BCLBM_ERR_TABLE;
         }
-    std::vector<int32_t> slot_of(N, -1);
-    for (int b = 0; b < nb; ++b) {
-        const int n = d->bulk[b];
-        if (n < 1 || n >= N) { err = "bulk node out of range"; return BCLBM_ERR_INVALID; }
-        if (b > 0 && n <= d->bulk[b - 1]) { err = "bulk list must be increasing"; return BCLBM_ERR_INVALID; }
-        if (ty[n] != 2 && ty[n] != 3) { err = "bulk node " + std::to_string(n) + " is not own-rank fluid"; return BCLBM_ERR_TABLE; }
-        slot_of[n] = b;  // provisional: bulk index
     }
-    for (int n = 1; n < N; ++n) {
-        if (ty[n] > 1 && slot_of[n] < 0) {
-            err = "fluid node " + std::to_string(n) + " missing from the bulk list";
+    std::vector<int32_t> slot_of(N, -1);
+    {
+        FirstBad bad;
+        parallel_for(static_cast<size_t>(nb), [&](size_t b0, size_t b1) {
+            for (size_t b = b0; b < b1; ++b) {
+                const int n = d->bulk[b];
+                int c = 0;
+                if (n < 1 || n >= N) c = 1;
+                else if (b > 0 && n <= d->bulk[b - 1]) c = 2;
+                else if (ty[n] != 2 && ty[n] != 3) c = 3;
+                if (c) {
+                    bad.set(static_cast<int64_t>(b));
+                    return;
+                }
+                slot_of[n] = static_cast<int32_t>(b);  // provisional: bulk index
+            }
+        });
+        if (bad.any()) {
+            const int64_t b = bad.get();
+            const int n = d->bulk[b];
+            if (n < 1 || n >= N) { err = "bulk node out of range"; return BCLBM_ERR_INVALID; }
+            if (b > 0 && n <= d->bulk[b - 1]) { err = "bulk list must be increasing"; return BCLBM_ERR_INVALID; }
+            err = "bulk node " + std::to_string(n) + " is not own-rank fluid";
+            return BCLBM_ERR_TABLE;
+        }
+    }
+    {
+        FirstBad bad;
+        parallel_for(static_cast<size_t>(N), [&](size_t n0, size_t n1) {
+            for (size_t n = std::max<size_t>(n0, 1); n < n1; ++n)
+                if (ty[n] > 1 && slot_of[n] < 0) {
+                    bad.set(static_cast<int64_t>(n));
+                    return;
+                }
+        });
+        if (bad.any()) {
+            err = "fluid node " + std::to_string(bad.get()) + " missing from the bulk list";
             return BCLBM_ERR_TABLE;
         }
     }
@@ -142,63 +207,85 @@ int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full)
     if (d->flags & BCLBM_FLAG_SFC_ORDER) {
         const int nd = Q == 9 ? 2 : 3;
         std::vector<uint64_t> code(nb);
-        for (int b = 0; b < nb; ++b) {
-            const int n = d->bulk[b];
-            uint64_t c = 0;
-            for (int k = 0; k < nd; ++k) {
-                const int64_t v = static_cast<int64_t>(d->pos[static_cast<size_t>(n) * nd + k]) + 1;
-                c |= spread_bits(static_cast<uint64_t>(std::max<int64_t>(v, 0)), nd) << (nd - 1 - k);
+        parallel_for(static_cast<size_t>(nb), [&](size_t b0, size_t b1) {
+            for (size_t b = b0; b < b1; ++b) {
+                const int n = d->bulk[b];
+                uint64_t c = 0;
+                for (int k = 0; k < nd; ++k) {
+                    const int64_t v = static_cast<int64_t>(d->pos[static_cast<size_t>(n) * nd + k]) + 1;
+                    c |= spread_bits(static_cast<uint64_t>(std::max<int64_t>(v, 0)), nd) << (nd - 1 - k);
+                }
+                code[b] = c;
             }
-            code[b] = c;
-        }
+        });
         std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return code[a] < code[b]; });
     }
     p.nf = nb;
     p.nf_pad = (nb + 63) / 64 * 64;
     p.slot_node.resize(nb);
     p.slot_bulk.resize(nb);
-    for (int s = 0; s < nb; ++s) {
-        p.slot_bulk[s] = order[s];
-        p.slot_node[s] = d->bulk[order[s]];
-        slot_of[d->bulk[order[s]]] = s;
-    }
-    // extended numbering: fluid slots, then referenced solids in node order, then the ghost
-    p.ext_of_node.assign(N, -1);
-    for (int n = 1; n < N; ++n)
-        if (slot_of[n] >= 0) p.ext_of_node[n] = slot_of[n];
-    std::vector<char> used(N, 0);
-    for (int b = 0; b < nb; ++b) {
-        const size_t n = static_cast<size_t>(d->bulk[b]);
-        for (int q = 0; q < Q; ++q) used[nbr[n * Q + q]] = 1;
-    }
-    p.solid_node.clear();
-    for (int n = 1; n < N; ++n)
-        if (used[n] && ty[n] < 2) {
-            p.ext_of_node[n] = nb + static_cast<int>(p.solid_node.size());
-            p.solid_node.push_back(n);
+    parallel_for(static_cast<size_t>(nb), [&](size_t s0, size_t s1) {
+        for (size_t s = s0; s < s1; ++s) {
+            p.slot_bulk[s] = order[s];
+            p.slot_node[s] = d->bulk[order[s]];
+            slot_of[d->bulk[order[s]]] = static_cast<int32_t>(s);
         }
+    });
+    // extended numbering: fluid slots, then (two-phase only) the referenced solids in
+    // node order, then the ghost; single-phase instances only need the fluid slots
+    p.ext_of_node.assign(N, -1);
+    parallel_for(static_cast<size_t>(N), [&](size_t n0, size_t n1) {
+        for (size_t n = std::max<size_t>(n0, 1); n < n1; ++n)
+            if (slot_of[n] >= 0) p.ext_of_node[n] = slot_of[n];
+    });
+    p.solid_node.clear();
+    if (d->collision == BCLBM_RK) {
+        std::vector<char> used(N, 0);
+        for (int b = 0; b < nb; ++b) {
+            const size_t n = static_cast<size_t>(d->bulk[b]);
+            for (int q = 0; q < Q; ++q) used[nbr[n * Q + q]] = 1;
+        }
+        for (int n = 1; n < N; ++n)
+            if (used[n] && ty[n] < 2) {
+                p.ext_of_node[n] = nb + static_cast<int>(p.solid_node.size());
+                p.solid_node.push_back(n);
+            }
+    }
     p.ns = static_cast<int>(p.solid_node.size());
     p.ext_of_node[0] = nb + p.ns;
     if (!full) return BCLBM_OK;
-    // the reference streams rest populations to neighbor(rest, n); it must be n itself
+    // the reference streams rest populations to neighbor(rest, n); it must be n itself.
+    // Pull equivalence: the fluid upstream neighbour pushes into this node, and this
+    // node's fluid downstream neighbour pulls from it (a one-to-one stream map).
     const int R = Q - 1;
-    for (int b = 0; b < nb; ++b) {
-        const size_t n = static_cast<size_t>(d->bulk[b]);
-        if (nbr[n * Q + R] != static_cast<int32_t>(n)) {
-            err = "rest-direction neighbour of node " + std::to_string(n) + " is not the node itself";
-            return BCLBM_ERR_TABLE;
-        }
-        // pull equivalence: the fluid upstream neighbour pushes into this node, and
-        // this node's fluid downstream neighbour pulls from it (a one-to-one stream map)
-        for (int q = 0; q < R; ++q) {
-            const int y = nbr[n * Q + rev_dir(Q, q)];
-            const int t = nbr[n * Q + q];
-            if ((y != 0 && ty[y] > 1 && nbr[static_cast<size_t>(y) * Q + q] != static_cast<int32_t>(n)) ||
-                (t != 0 && ty[t] > 1 && nbr[static_cast<size_t>(t) * Q + rev_dir(Q, q)] != static_cast<int32_t>(n))) {
-                err = "neighbour table not symmetric at node " + std::to_string(n) + " direction " + std::to_string(q);
-                return BCLBM_ERR_TABLE;
+    FirstBad bad_rest, bad_sym;
+    parallel_for(static_cast<size_t>(nb), [&](size_t b0, size_t b1) {
+        for (size_t b = b0; b < b1; ++b) {
+            const size_t n = static_cast<size_t>(d->bulk[b]);
+            if (nbr[n * Q + R] != static_cast<int32_t>(n)) {
+                bad_rest.set(static_cast<int64_t>(b));
+                return;
+            }
+            for (int q = 0; q < R; ++q) {
+                const int y = nbr[n * Q + rev_dir(Q, q)];
+                const int t = nbr[n * Q + q];
+                if ((y != 0 && ty[y] > 1 && nbr[static_cast<size_t>(y) * Q + q] != static_cast<int32_t>(n)) ||
+                    (t != 0 && ty[t] > 1 && nbr[static_cast<size_t>(t) * Q + rev_dir(Q, q)] != static_cast<int32_t>(n))) {
+                    bad_sym.set(static_cast<int64_t>(b) * 32 + q);
+                    return;
+                }
             }
         }
+    });
+    if (bad_rest.any()) {
+        err = "rest-direction neighbour of node " + std::to_string(d->bulk[bad_rest.get()]) + " is not the node itself";
+        return BCLBM_ERR_TABLE;
+    }
+    if (bad_sym.any()) {
+        const int64_t v = bad_sym.get();
+        err = "neighbour table not symmetric at node " + std::to_string(d->bulk[v / 32]) + " direction " +
+              std::to_string(v % 32);
+        return BCLBM_ERR_TABLE;
     }
     return BCLBM_OK;
 }
@@ -448,22 +535,40 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
 
     // ghost sources: last bulk node (bulk order) whose neighbour along c_p is node 0
     std::vector<int32_t> slot_of_bulk(h->nf);
-    for (int s = 0; s < h->nf; ++s) slot_of_bulk[h->slot_bulk[s]] = s;
+    parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
+        for (size_t s = s0; s < s1; ++s) slot_of_bulk[h->slot_bulk[s]] = static_cast<int32_t>(s);
+    });
     for (int pdir = 0; pdir < 19; ++pdir) h->ghost_src[pdir] = 0;
-    for (int pdir = 0; pdir < R; ++pdir)
-        for (int b = h->nf - 1; b >= 0; --b)
-            if (d->neigh[static_cast<size_t>(d->bulk[b]) * Q + pdir] == 0) {
-                h->ghost_src[pdir] = slot_of_bulk[b];
-                break;
+    {
+        std::atomic<int> last[19];
+        for (auto& x : last) x.store(-1);
+        parallel_for(static_cast<size_t>(h->nf), [&](size_t b0, size_t b1) {
+            int loc[19];
+            for (int k = 0; k < 19; ++k) loc[k] = -1;
+            for (size_t b = b0; b < b1; ++b) {
+                const int32_t* row = d->neigh + static_cast<size_t>(d->bulk[b]) * Q;
+                for (int pdir = 0; pdir < R; ++pdir)
+                    if (row[pdir] == 0) loc[pdir] = static_cast<int>(b);
             }
+            for (int pdir = 0; pdir < R; ++pdir) {
+                int cur = last[pdir].load();
+                while (loc[pdir] > cur && !last[pdir].compare_exchange_weak(cur, loc[pdir])) {
+                }
+            }
+        });
+        for (int pdir = 0; pdir < R; ++pdir)
+            if (last[pdir].load() >= 0) h->ghost_src[pdir] = slot_of_bulk[last[pdir].load()];
+    }
     std::vector<int32_t> tab;
     if (h->collision == BCLBM_RK) {
         // extended neighbour table in device numbering (pull + colour gradient)
         tab.assign(static_cast<size_t>(R) * pad, static_cast<int32_t>(h->nf + h->ns));
-        for (int s = 0; s < h->nf; ++s) {
-            const size_t n = static_cast<size_t>(h->slot_node[s]);
-            for (int q = 0; q < R; ++q) tab[static_cast<size_t>(q) * pad + s] = p.ext_of_node[d->neigh[n * Q + q]];
-        }
+        parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
+            for (size_t s = s0; s < s1; ++s) {
+                const size_t n = static_cast<size_t>(h->slot_node[s]);
+                for (int q = 0; q < R; ++q) tab[static_cast<size_t>(q) * pad + s] = p.ext_of_node[d->neigh[n * Q + q]];
+            }
+        });
     } else {
         // resolved pull table: element index (row * pad + slot) of the post-collision
         // value that streams into slot s along c_q (fluid upstream, wall, or ghost)
@@ -474,18 +579,20 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             return BCLBM_ERR_UNSUPPORTED;
         }
         tab.assign(static_cast<size_t>(R) * pad, 0);
-        for (int s = 0; s < h->nf; ++s) {
-            const size_t n = static_cast<size_t>(h->slot_node[s]);
-            for (int q = 0; q < R; ++q) {
-                const int rq = rev_dir(Q, q);
-                const int y = d->neigh[n * Q + rq];
-                int64_t e;
-                if (y != 0 && d->types[y] > 1) e = static_cast<int64_t>(q) * pad + p.ext_of_node[y];
-                else if (y == 0) e = static_cast<int64_t>(rq) * pad + h->ghost_src[rq];
-                else e = static_cast<int64_t>(rq) * pad + s;
-                tab[static_cast<size_t>(q) * pad + s] = static_cast<int32_t>(e);
+        parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
+            for (size_t s = s0; s < s1; ++s) {
+                const size_t n = static_cast<size_t>(h->slot_node[s]);
+                for (int q = 0; q < R; ++q) {
+                    const int rq = rev_dir(Q, q);
+                    const int y = d->neigh[n * Q + rq];
+                    int64_t e;
+                    if (y != 0 && d->types[y] > 1) e = static_cast<int64_t>(q) * pad + p.ext_of_node[y];
+                    else if (y == 0) e = static_cast<int64_t>(rq) * pad + h->ghost_src[rq];
+                    else e = static_cast<int64_t>(rq) * pad + static_cast<int64_t>(s);
+                    tab[static_cast<size_t>(q) * pad + s] = static_cast<int32_t>(e);
+                }
             }
-        }
+        });
     }
     CREATE_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     const size_t sb = store_bytes(h->precision);
@@ -538,12 +645,14 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         const size_t nsoa = static_cast<size_t>(h->nfields) * Q * pad;
         std::vector<double> soa(nsoa, 0.0);
         const int es = h->nfields * Q;
-        for (int s = 0; s < h->nf; ++s) {
-            const size_t n = static_cast<size_t>(h->slot_node[s]);
-            for (int k = 0; k < h->nfields; ++k)
-                for (int q = 0; q < Q; ++q)
-                    soa[(static_cast<size_t>(k) * Q + q) * pad + s] = d->f_init[n * es + static_cast<size_t>(k) * Q + q];
-        }
+        parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
+            for (size_t s = s0; s < s1; ++s) {
+                const size_t n = static_cast<size_t>(h->slot_node[s]);
+                for (int k = 0; k < h->nfields; ++k)
+                    for (int q = 0; q < Q; ++q)
+                        soa[(static_cast<size_t>(k) * Q + q) * pad + s] = d->f_init[n * es + static_cast<size_t>(k) * Q + q];
+            }
+        });
         if (h->precision == BCLBM_F64) {
             CREATE_TRY(cudaMemcpyAsync(h->pops[0], soa.data(), nsoa * sizeof(double), cudaMemcpyHostToDevice, h->stream));
             CREATE_TRY(cudaStreamSynchronize(h->stream));
@@ -676,9 +785,10 @@ int bclbm_download_f(bclbm_handle* h, double* f) {
         std::vector<double> tmp(n);
         CUDA_TRY(h, cudaMemcpyAsync(tmp.data(), h->d_gather, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-        for (int b = 0; b < h->nf; ++b)
-            std::memcpy(f + static_cast<size_t>(h->bulk[b]) * es, tmp.data() + static_cast<size_t>(b) * es,
-                        es * sizeof(double));
+        parallel_for(static_cast<size_t>(h->nf), [&](size_t b0, size_t b1) {
+            for (size_t b = b0; b < b1; ++b)
+                std::memcpy(f + static_cast<size_t>(h->bulk[b]) * es, tmp.data() + b * es, es * sizeof(double));
+        });
     }
     return BCLBM_OK;
 }
@@ -705,14 +815,16 @@ int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg)
     }
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     for (size_t k = 0; k < cf.size(); ++k) c[k] = cf[k];
-    for (int s = 0; s < h->nf; ++s) {
-        const size_t n = static_cast<size_t>(h->slot_node[s]);
-        if (rho)
-            for (int k = 0; k < h->nfields; ++k) rho[n * h->nfields + k] = r[k * pad + s];
-        if (vel)
-            for (int dd = 0; dd < h->nd; ++dd) vel[n * h->nd + dd] = v[dd * pad + s];
-        if (cg && h->collision == BCLBM_RK) cg[n] = c[s];
-    }
+    parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
+        for (size_t s = s0; s < s1; ++s) {
+            const size_t n = static_cast<size_t>(h->slot_node[s]);
+            if (rho)
+                for (int k = 0; k < h->nfields; ++k) rho[n * h->nfields + k] = r[k * pad + s];
+            if (vel)
+                for (int dd = 0; dd < h->nd; ++dd) vel[n * h->nd + dd] = v[dd * pad + s];
+            if (cg && h->collision == BCLBM_RK) cg[n] = c[s];
+        }
+    });
     if (cg && h->collision == BCLBM_RK)
         for (int k = 0; k < h->ns; ++k) cg[h->solid_node[k]] = h->solid_cg[k];
     return BCLBM_OK;

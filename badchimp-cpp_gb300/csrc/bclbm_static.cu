@@ -116,6 +116,9 @@ extern "C" int bclbm_moments_static(int32_t lattice_q, int32_t precision, int32_
     const double scale = store_scale > 0 ? store_scale : (precision == BCLBM_F16 ? 4096.0 : 1.0);
     a.scale = scale;
     a.inv_scale = 1.0 / scale;
+    a.f_rho_ref = static_cast<float>(a.rho_ref);  // FP32 copies read by the shifted-format path
+    a.f_scale = static_cast<float>(a.scale);
+    a.f_inv_scale = static_cast<float>(a.inv_scale);
     a.partials = scratch;
     const int nblocks = bclbm::grid_for(n_slots);
     const cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -298,6 +298,20 @@ def run_mine(args, world, rank):
         if "bgk_f16" in variants:
             variants["f16_speedup_vs_f64"] = variants["bgk_f16"]["mlups"] / mlups * world
 
+    # ---- accuracy: permeability of the shifted formats against FP64 -------------
+    accuracy = None
+    if rank == 0 and args.accuracy_steps > 0:
+        nu = (args.tau - 0.5) / 3.0
+        vol = float(args.size) ** 3
+        ks = {}
+        for prec in ("f64", "f32", "f16", "bf16"):
+            with L.Solver(lat, f0, collision=L.BGK, precision=prec, tau=(args.tau, args.tau), force=F) as s:
+                s.step(args.accuracy_steps)
+                ks[prec] = nu * s.reduce()["momentum"][0] / (vol * args.gx)
+        accuracy = {"steps": args.accuracy_steps, "permeability_f64": ks["f64"],
+                    "definition": "k = nu * sum_fluid(rho u_x) / (V F_x), FP64 reductions on the GPU",
+                    "rel_err_vs_f64": {p: abs(ks[p] - ks["f64"]) / abs(ks["f64"]) for p in ("f32", "f16", "bf16")}}
+
     # ---- end to end through the C ABI with host buffers -------------------------
     torch.cuda.synchronize()
     barrier(world)
@@ -355,6 +369,7 @@ def run_mine(args, world, rank):
             "gpu_launches": launches,
             "launches_total": bclbm.native.launch_count() - launches0,
             "variants": variants,
+            "accuracy": accuracy,
             "check": {"mass": st["mass"][0], "flux_x": st["momentum"][0], "nonfinite": st["nonfinite"]},
         }
         print(json.dumps(line), flush=True)
@@ -379,6 +394,8 @@ def main():
     ap.add_argument("--exact", action="store_true", help="headline with the reference-order FP64 kernel")
     ap.add_argument("--fma64", action="store_true", help="headline with the native-FP64 FMA kernel")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=10000,
+                    help="steps of the FP64 / FP32 / FP16 / BF16 permeability comparison (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
