@@ -14,8 +14,9 @@ Submodules
 from . import geometry  # noqa: F401
 from . import native  # noqa: F401
 from . import lbsolver  # noqa: F401
+from . import serving  # noqa: F401
 
-__all__ = ["geometry", "native", "lbsolver", "build_native"]
+__all__ = ["geometry", "native", "lbsolver", "serving", "build_native"]
 
 
 def build_native(force: bool = False):

@@ -6,6 +6,8 @@ Translation units are compiled in parallel:
   csrc/bclbm_kernels.cu  FP64 (FMA) and FP32-compute kernels, reductions
   csrc/bclbm_api.cu      the C ABI of include/bclbm.h (host code)
   csrc/bclbm_static.cu   bclbm_moments_static, the entry point that allocates nothing
+  csrc/bclbm_batch.cu    the multi-instance batch (persistent kernel, CUDA graph)
+  csrc/bclbm_geometry.cu the host-side lattice builder (voxel mask to node tables)
 Host code is compiled with -ffp-contract=off so that host-side arithmetic is
 the same on x86-64 and aarch64.
 """
@@ -30,6 +32,8 @@ UNITS = {
     "bclbm_kernels.cu": [],
     "bclbm_api.cu": [],
     "bclbm_static.cu": [],
+    "bclbm_batch.cu": [],
+    "bclbm_geometry.cu": [],
 }
 
 

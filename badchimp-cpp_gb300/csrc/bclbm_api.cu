@@ -17,44 +17,14 @@
 #include <vector>
 
 #include "bclbm.h"
+#include "bclbm_internal.h"
+#include "bclbm_host.h"
 #include "bclbm_launch.h"
 
 using namespace bclbm;
+using bclbm::host::FirstBad;
+using bclbm::host::parallel_for;
 
-struct bclbm_handle {
-    int q = 0, nd = 0, nfields = 1, collision = 0, precision = 0;
-    uint32_t flags = 0;
-    bool exact = false, trt = false, flux = false, fma64 = false;
-    int n_nodes = 0, nf = 0, nf_pad = 0, ns = 0;
-    double tau[2] = {1.0, 1.0};
-    double sigma = 0.0, beta = 0.0, mom_x = 0.0, rho_ref = 1.0, scale = 1.0;
-    double force[3] = {0.0, 0.0, 0.0};
-    std::vector<int32_t> slot_node;   // device slot -> reference node number
-    std::vector<int32_t> slot_bulk;   // device slot -> index in the bulk list
-    std::vector<int32_t> bulk;        // the bulk list
-    std::vector<int32_t> solid_node;  // extended solid index -> reference node number
-    std::vector<double> solid_cg;     // RK colour of the stored solids
-    bool bulk_contiguous = false;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    void* pops[2] = {nullptr, nullptr};
-    int cur = 0;
-    bool state_post = false;          // pops[cur] holds post-collision populations
-    bool macros_valid = false;
-    int32_t* d_nbr = nullptr;
-    int32_t* d_slot_bulk = nullptr;
-    double* d_rho = nullptr;
-    double* d_vel = nullptr;
-    double* d_cg = nullptr;
-    float* d_cgf = nullptr;
-    DevParams* d_params = nullptr;
-    double* d_partials = nullptr;
-    double* d_red = nullptr;
-    double* d_gather = nullptr;
-    int32_t ghost_src[19] = {0};
-    int64_t steps_done = 0;
-    std::string last_error;
-};
 
 namespace {
 
@@ -84,34 +54,6 @@ int rev_dir(int Q, int q) {
     if (Q == 9) return q == 8 ? 8 : (q + 4) % 8;
     return q == 18 ? 18 : (q + 9) % 18;
 }
-
-// fn(begin, end) over [0, n) on the host cores, in contiguous chunks
-template <class F>
-void parallel_for(size_t n, F&& fn) {
-    const unsigned hw = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
-    const size_t nt = std::min<size_t>(hw, (n + 32767) / 32768);
-    if (nt <= 1) {
-        fn(size_t(0), n);
-        return;
-    }
-    std::vector<std::thread> th;
-    th.reserve(nt - 1);
-    for (size_t t = 1; t < nt; ++t) th.emplace_back([&fn, n, t, nt] { fn(n * t / nt, n * (t + 1) / nt); });
-    fn(size_t(0), n / nt);
-    for (auto& x : th) x.join();
-}
-
-// smallest index at which a parallel check failed (INT64_MAX: none)
-struct FirstBad {
-    std::atomic<int64_t> v{INT64_MAX};
-    void set(int64_t i) {
-        int64_t cur = v.load();
-        while (i < cur && !v.compare_exchange_weak(cur, i)) {
-        }
-    }
-    bool any() const { return v.load() != INT64_MAX; }
-    int64_t get() const { return v.load(); }
-};
 
 uint64_t spread_bits(uint64_t v, int dims) {
     uint64_t out = 0;
@@ -334,7 +276,9 @@ fx::Consts fixed_consts_q(const bclbm_handle* h) {
 
 fx::Consts fixed_consts(const bclbm_handle* h) { return h->q == 9 ? fixed_consts_q<9>(h) : fixed_consts_q<19>(h); }
 
-StepArgs make_args(const bclbm_handle* h) {
+}  // namespace
+
+StepArgs bclbm::handle_args(const bclbm_handle* h) {
     StepArgs a;
     std::memset(&a, 0, sizeof(a));
     a.L.nf = h->nf;
@@ -378,6 +322,10 @@ StepArgs make_args(const bclbm_handle* h) {
     a.fxk = fixed_consts(h);
     return a;
 }
+
+namespace {
+
+StepArgs make_args(const bclbm_handle* h) { return handle_args(h); }
 
 __global__ void k_encode(const double* __restrict__ f, void* out, int nf, int nf_pad, int Q, int nfields,
                          int precision, double rho_ref, double scale) {

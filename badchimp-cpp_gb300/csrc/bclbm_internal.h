@@ -1,0 +1,52 @@
+// Internal to the library: the handle's state, shared by the C ABI
+// (bclbm_api.cu) and the multi-instance batch (bclbm_batch.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "bclbm.h"
+#include "bclbm_kernels.cuh"
+
+struct bclbm_handle {
+    int q = 0, nd = 0, nfields = 1, collision = 0, precision = 0;
+    uint32_t flags = 0;
+    bool exact = false, trt = false, flux = false, fma64 = false;
+    int n_nodes = 0, nf = 0, nf_pad = 0, ns = 0;
+    double tau[2] = {1.0, 1.0};
+    double sigma = 0.0, beta = 0.0, mom_x = 0.0, rho_ref = 1.0, scale = 1.0;
+    double force[3] = {0.0, 0.0, 0.0};
+    std::vector<int32_t> slot_node;   // device slot -> reference node number
+    std::vector<int32_t> slot_bulk;   // device slot -> index in the bulk list
+    std::vector<int32_t> bulk;        // the bulk list
+    std::vector<int32_t> solid_node;  // extended solid index -> reference node number
+    std::vector<double> solid_cg;     // RK colour of the stored solids
+    bool bulk_contiguous = false;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void* pops[2] = {nullptr, nullptr};
+    int cur = 0;
+    bool state_post = false;          // pops[cur] holds post-collision populations
+    bool macros_valid = false;
+    int32_t* d_nbr = nullptr;
+    int32_t* d_slot_bulk = nullptr;
+    double* d_rho = nullptr;
+    double* d_vel = nullptr;
+    double* d_cg = nullptr;
+    float* d_cgf = nullptr;
+    bclbm::DevParams* d_params = nullptr;
+    double* d_partials = nullptr;
+    double* d_red = nullptr;
+    double* d_gather = nullptr;
+    int32_t ghost_src[19] = {0};
+    int64_t steps_done = 0;
+    std::string last_error;
+};
+
+namespace bclbm {
+// kernel arguments of a handle's current configuration (src/dst left for the caller)
+StepArgs handle_args(const bclbm_handle* h);
+}  // namespace bclbm

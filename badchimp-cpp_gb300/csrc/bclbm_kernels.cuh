@@ -299,11 +299,9 @@ __device__ __forceinline__ void collide_fast(C* f, const C* F, C oms, C oma, C t
 // MODE 1: restructured, compute in double (F64) or float (shifted formats)
 // ---------------------------------------------------------------------------
 template <int Q, class S, int MODE, bool TRT, bool LOCAL>
-__global__ void __launch_bounds__(kBlock) k_single(StepArgs a) {
+__device__ __forceinline__ void single_node(const StepArgs& a, int i) {
     const bool MACROS = a.rho_out != nullptr;
     constexpr int D = Lat<Q>::D;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.L.nf) return;
     using T = typename Store<S>::T;
     T v[Q];
     load_field<Q, S, LOCAL, true>(static_cast<const S*>(a.src), a.L, i, v);
@@ -362,6 +360,12 @@ __global__ void __launch_bounds__(kBlock) k_single(StepArgs a) {
     }
 }
 
+template <int Q, class S, int MODE, bool TRT, bool LOCAL>
+__global__ void __launch_bounds__(kBlock) k_single(StepArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.L.nf) single_node<Q, S, MODE, TRT, LOCAL>(a, i);
+}
+
 // ---------------------------------------------------------------------------
 // k_single_fixed: one single-phase step on F64 storage with 64-bit fixed-point
 // arithmetic (bclbm_fixed.cuh).  BCLBM_FX_MINB is the minimum number of
@@ -372,10 +376,8 @@ __global__ void __launch_bounds__(kBlock) k_single(StepArgs a) {
 #endif
 
 template <int Q, bool TRT, bool LOCAL>
-__global__ void __launch_bounds__(kBlock, BCLBM_FX_MINB) k_single_fixed(StepArgs a) {
+__device__ __forceinline__ void fixed_node(const StepArgs& a, int i) {
     constexpr int D = Lat<Q>::D;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.L.nf) return;
     double v[Q];
     load_field<Q, double, LOCAL, true>(static_cast<const double*>(a.src), a.L, i, v);
     int ovf = 0;
@@ -395,12 +397,18 @@ __global__ void __launch_bounds__(kBlock, BCLBM_FX_MINB) k_single_fixed(StepArgs
     if (ovf) atomicOr(a.fx_flag, 1);
 }
 
+template <int Q, bool TRT, bool LOCAL>
+__global__ void __launch_bounds__(kBlock, BCLBM_FX_MINB) k_single_fixed(StepArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.L.nf) fixed_node<Q, TRT, LOCAL>(a, i);
+}
+
 // ---------------------------------------------------------------------------
 // Deterministic block reduction of NV doubles (fixed shuffle tree + fixed
 // warp order); thread 0 writes partials[blockIdx.x * NV + k].
 // ---------------------------------------------------------------------------
 template <int NV>
-__device__ __forceinline__ void block_reduce_store(double* vals, double* partials, bool max_last) {
+__device__ __forceinline__ void block_reduce_store(double* vals, double* partials, bool max_last, int slot = -1) {
     __shared__ double sh[kBlock / 32][NV];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -419,7 +427,7 @@ __device__ __forceinline__ void block_reduce_store(double* vals, double* partial
         for (int k = 0; k < NV; ++k) {
             double s = sh[0][k];
             for (int w = 1; w < kBlock / 32; ++w) s = (max_last && k == NV - 1) ? fmax(s, sh[w][k]) : s + sh[w][k];
-            partials[static_cast<size_t>(blockIdx.x) * NV + k] = s;
+            partials[static_cast<size_t>(slot < 0 ? static_cast<int>(blockIdx.x) : slot) * NV + k] = s;
         }
     }
 }
@@ -747,12 +755,9 @@ __global__ void __launch_bounds__(kBlock) k_gather(StepArgs a, const int32_t* __
 // the stored deviations (exact in FP64) and scaled by w_q / scale afterwards, per
 // weight class; max |f| and the finite check are done on the integer / FP32 side.
 template <int Q, class S, int NF, bool LOCAL>
-__global__ void __launch_bounds__(kBlock) k_moments(StepArgs a) {
-    constexpr int NV = 6;
+__device__ __forceinline__ void moments_node(const StepArgs& a, int i, double* vals) {
     constexpr int D = Lat<Q>::D, NP = Lat<Q>::NP, R = Lat<Q>::REST;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double vals[NV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    if (i < a.L.nf) {
+    {
         const S* g = static_cast<const S*>(a.src);
         if constexpr (NF == 1) {
             using T = typename Store<S>::T;
@@ -827,6 +832,14 @@ __global__ void __launch_bounds__(kBlock) k_moments(StepArgs a) {
             vals[5] = mx;
         }
     }
+}
+
+template <int Q, class S, int NF, bool LOCAL>
+__global__ void __launch_bounds__(kBlock) k_moments(StepArgs a) {
+    constexpr int NV = 6;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double vals[NV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (i < a.L.nf) moments_node<Q, S, NF, LOCAL>(a, i, vals);
     block_reduce_store<NV>(vals, a.partials, true);
 }
 

@@ -108,8 +108,26 @@ def build_lattice(geo: np.ndarray, lattice: str, periodic: str = "") -> dict:
     ``geo`` holds 1 for fluid and 0 for solid.  Returns a dict with
     ``neigh`` (int32 [N*Q], row 0 all zero), ``types`` (int16 [N]),
     ``pos`` (int32 [N*nD], -1 for node 0), ``nf`` (fluid count) and ``ns``
-    (stored boundary-solid count); N = 1 + nf + ns.
+    (stored boundary-solid count); N = 1 + nf + ns.  Built on the host cores by
+    the library's bclbm_lattice_build; ``build_lattice_numpy`` is the same
+    numbering in numpy.
     """
+    from . import native
+
+    c = LATTICE_C[lattice]
+    nq, nd = c.shape
+    geo = np.asarray(geo)
+    if geo.ndim != nd:
+        raise ValueError(f"{lattice} needs a {nd}-D geometry, got {geo.ndim}-D")
+    if not np.all((geo == 0) | (geo == 1)):
+        raise ValueError("geometry must hold 0 (solid) and 1 (fluid) only")
+    bits = sum(1 << d for d, ax in enumerate("xyz"[:nd]) if ax in periodic.lower())
+    neigh, types, pos, nf, ns = native.lattice_tables(geo, nq, bits)
+    return {"neigh": neigh, "types": types, "pos": pos, "nf": nf, "ns": ns, "nq": nq, "nd": nd, "lattice": lattice}
+
+
+def build_lattice_numpy(geo: np.ndarray, lattice: str, periodic: str = "") -> dict:
+    """``build_lattice`` in plain numpy (the same arrays, bit for bit)."""
     c = LATTICE_C[lattice]
     nq, nd = c.shape
     geo = np.asarray(geo)
@@ -125,8 +143,8 @@ def build_lattice(geo: np.ndarray, lattice: str, periodic: str = "") -> dict:
     fluid_int = np.zeros(pshape, dtype=bool)
     fluid_int[interior] = geo == 1
     nf = int(np.count_nonzero(fluid_int))
-    label = np.zeros(pshape, dtype=np.int64)
-    label[fluid_int] = np.arange(1, nf + 1)
+    label = np.zeros(pshape, dtype=np.int32)
+    label[fluid_int] = np.arange(1, nf + 1, dtype=np.int32)
     for d, ax in enumerate("xyz"[:nd]):
         if ax in periodic:
             lo = [slice(None)] * nd
@@ -140,35 +158,47 @@ def build_lattice(geo: np.ndarray, lattice: str, periodic: str = "") -> dict:
             label[tuple(lo)] = label[tuple(src_lo)]
             label[tuple(hi)] = label[tuple(src_hi)]
 
-    fpos = np.nonzero(fluid_int)  # C order == label order
-    added = np.zeros(pshape, dtype=bool)
-    for v in c:
-        p = tuple(fpos[d] + v[d] for d in range(nd))
-        added[p] |= P[p] == 0
-    spos = np.nonzero(added)
-    ns = int(spos[0].size)
-    local = np.zeros(pshape, dtype=np.int64)
-    local[fpos] = np.arange(1, nf + 1)
-    local[spos] = np.arange(nf + 1, nf + ns + 1)
+    # flat indices into the padded array; a lattice step is a constant offset
+    strides = np.cumprod((1,) + pshape[::-1][:-1])[::-1].astype(np.int64)
+    offs = c @ strides
+    Pf = P.reshape(-1)
+    labelf = label.reshape(-1)
+    fpos = np.flatnonzero(fluid_int)  # C order == label order; all interior
+    added = np.zeros(Pf.size, dtype=bool)
+    for off in offs:
+        p = fpos + off
+        added[p[Pf[p] == 0]] = True
+    spos = np.flatnonzero(added)
+    ns = int(spos.size)
+    local = np.zeros(Pf.size, dtype=np.int32)
+    local[fpos] = np.arange(1, nf + 1, dtype=np.int32)
+    local[spos] = np.arange(nf + 1, nf + ns + 1, dtype=np.int32)
 
     n_nodes = 1 + nf + ns
-    allpos = [np.concatenate([fpos[d], spos[d]]) for d in range(nd)]
+    scoord = np.unravel_index(spos, pshape)
     neigh = np.zeros((n_nodes, nq), dtype=np.int32)
     for q in range(nq):
-        p = [allpos[d] + c[q, d] for d in range(nd)]
-        ok = np.ones(allpos[0].shape, dtype=bool)
+        # fluid nodes are interior: every neighbour is inside the padded array
+        p = fpos + offs[q]
+        nb = local[p]
+        img = (nb == 0) & (Pf[p] == 1)
+        neigh[1:nf + 1, q] = np.where(img, labelf[p], nb)
+        # stored solids may sit on the rim: neighbours outside the array are node 0
+        ok = np.ones(ns, dtype=bool)
         for d in range(nd):
-            ok &= (p[d] >= 0) & (p[d] < pshape[d])
-        pp = tuple(p[d][ok] for d in range(nd))
-        nb = local[pp]
-        img = (nb == 0) & (P[pp] == 1)
-        nb = np.where(img, label[pp], nb)
-        col = np.zeros(allpos[0].shape, dtype=np.int64)
-        col[ok] = nb
-        neigh[1:, q] = col
+            x = scoord[d] + c[q, d]
+            ok &= (x >= 0) & (x < pshape[d])
+        ps = spos[ok] + offs[q]
+        nbs = local[ps]
+        imgs = (nbs == 0) & (Pf[ps] == 1)
+        col = np.zeros(ns, dtype=np.int32)
+        col[ok] = np.where(imgs, labelf[ps], nbs)
+        neigh[nf + 1:, q] = col
     pos = np.full((n_nodes, nd), -1, dtype=np.int32)
+    fcoord = np.unravel_index(fpos, pshape)
     for d in range(nd):
-        pos[1:, d] = allpos[d] - 1
+        pos[1:nf + 1, d] = fcoord[d] - 1
+        pos[nf + 1:, d] = scoord[d] - 1
 
     types = node_types(neigh, nf)
     return {"neigh": neigh.reshape(-1), "types": types, "pos": pos.reshape(-1),

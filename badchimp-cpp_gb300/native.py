@@ -65,7 +65,10 @@ class Timing(ctypes.Structure):
 
 EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_step_timed", "bclbm_download_f", "bclbm_download_macros", "bclbm_reduce",
            "bclbm_set_force", "bclbm_node_perm", "bclbm_footprint", "bclbm_sync", "bclbm_destroy", "bclbm_error",
-           "bclbm_last_error", "bclbm_launch_count", "bclbm_moments_static"]
+           "bclbm_last_error", "bclbm_launch_count", "bclbm_moments_static", "bclbm_batch_create", "bclbm_batch_admit",
+           "bclbm_batch_retire", "bclbm_batch_step", "bclbm_batch_stats", "bclbm_batch_download_f", "bclbm_batch_info",
+           "bclbm_batch_sync", "bclbm_batch_last_error", "bclbm_batch_destroy", "bclbm_lattice_build",
+           "bclbm_lattice_info", "bclbm_lattice_export", "bclbm_lattice_free"]
 
 
 def lib_path() -> Path:
@@ -113,6 +116,32 @@ def lib():
     L.bclbm_moments_static.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                        ctypes.c_int32, vp, ctypes.c_double, ctypes.c_double, vp, vp]
     L.bclbm_moments_static.restype = ctypes.c_int
+    i32 = ctypes.c_int32
+    L.bclbm_batch_create.argtypes = [i32, i32, i32, ctypes.c_uint32, i32, ctypes.c_size_t, i32, ctypes.POINTER(vp)]
+    L.bclbm_batch_admit.argtypes = [vp, ctypes.POINTER(Desc), ctypes.POINTER(i32)]
+    L.bclbm_batch_retire.argtypes = [vp, i32]
+    L.bclbm_batch_step.argtypes = [vp, i32]
+    L.bclbm_batch_stats.argtypes = [vp, i32, vp, ctypes.POINTER(Stats)]
+    L.bclbm_batch_download_f.argtypes = [vp, i32, vp]
+    L.bclbm_batch_info.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(i32),
+                                   ctypes.POINTER(ctypes.c_int64)]
+    L.bclbm_batch_sync.argtypes = [vp]
+    for name in ("bclbm_batch_create", "bclbm_batch_admit", "bclbm_batch_retire", "bclbm_batch_step",
+                 "bclbm_batch_stats", "bclbm_batch_download_f", "bclbm_batch_info", "bclbm_batch_sync"):
+        getattr(L, name).restype = ctypes.c_int
+    L.bclbm_batch_last_error.argtypes = [vp]
+    L.bclbm_batch_last_error.restype = ctypes.c_char_p
+    L.bclbm_batch_destroy.argtypes = [vp]
+    L.bclbm_batch_destroy.restype = None
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    L.bclbm_lattice_build.argtypes = [i32, i32, vp, vp, ctypes.c_uint32, ctypes.POINTER(vp)]
+    L.bclbm_lattice_build.restype = ctypes.c_int
+    L.bclbm_lattice_info.argtypes = [vp, i64p, i64p, i64p]
+    L.bclbm_lattice_info.restype = ctypes.c_int
+    L.bclbm_lattice_export.argtypes = [vp, vp, vp, vp]
+    L.bclbm_lattice_export.restype = ctypes.c_int
+    L.bclbm_lattice_free.argtypes = [vp]
+    L.bclbm_lattice_free.restype = None
     _lib = L
     return L
 
@@ -124,14 +153,16 @@ def dp(a):
 ip = dp
 
 
-def check(rc: int, handle=None):
+def check(rc: int, handle=None, batch=None):
     if rc != 0:
         msg = lib().bclbm_error(rc).decode()
-        if handle:
-            detail = lib().bclbm_last_error(handle)
+        if handle or batch:
+            detail = lib().bclbm_last_error(handle) if handle else lib().bclbm_batch_last_error(batch)
             if detail:
                 msg += ": " + detail.decode()
-        raise BclbmError(f"bclbm status {rc}: {msg}")
+        err = BclbmError(f"bclbm status {rc}: {msg}")
+        err.status = rc
+        raise err
 
 
 def make_desc(lat, f_init, collision, precision, flags, tau, force, sigma, beta, flux_control, mom_x, rho_ref,
@@ -179,12 +210,16 @@ def footprint(lat, collision, precision, flags=0):
     return int(n.value)
 
 
-def reduce(h) -> dict:
-    s = Stats()
-    check(lib().bclbm_reduce(h, ctypes.byref(s)), h)
+def stats_dict(s: Stats) -> dict:
     return {"mass": list(s.mass), "momentum": list(s.momentum), "flux_fc": list(s.flux_fc),
             "saturation": s.saturation, "max_abs_f": s.max_abs_f, "n_bulk": s.n_bulk,
             "steps_done": s.steps_done, "nonfinite": bool(s.nonfinite)}
+
+
+def reduce(h) -> dict:
+    s = Stats()
+    check(lib().bclbm_reduce(h, ctypes.byref(s)), h)
+    return stats_dict(s)
 
 
 def step_timed(h, nsteps: int) -> dict:
@@ -196,3 +231,21 @@ def step_timed(h, nsteps: int) -> dict:
 
 def launch_count() -> int:
     return int(lib().bclbm_launch_count())
+
+
+def lattice_tables(mask, nq: int, periodic_bits: int):
+    """bclbm_lattice_build: (neigh int32 [N*Q], types int16 [N], pos int32 [N*nD], nf, ns)."""
+    m = np.ascontiguousarray(mask, dtype=np.int8)
+    shape = np.asarray(m.shape, dtype=np.int32)
+    h = ctypes.c_void_p()
+    check(lib().bclbm_lattice_build(nq, m.ndim, dp(shape), dp(m), periodic_bits, ctypes.byref(h)))
+    try:
+        n, nf, ns = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        check(lib().bclbm_lattice_info(h, ctypes.byref(n), ctypes.byref(nf), ctypes.byref(ns)))
+        neigh = np.empty(n.value * nq, dtype=np.int32)
+        types = np.empty(n.value, dtype=np.int16)
+        pos = np.empty(n.value * m.ndim, dtype=np.int32)
+        check(lib().bclbm_lattice_export(h, dp(neigh), dp(types), dp(pos)))
+    finally:
+        lib().bclbm_lattice_free(h)
+    return neigh, types, pos, int(nf.value), int(ns.value)

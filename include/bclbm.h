@@ -183,6 +183,68 @@ int bclbm_moments_static(int32_t lattice_q, int32_t precision, int32_t nfields, 
                          int32_t slot_stride, const void* d_pops, double rho_ref, double store_scale,
                          double* d_out, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Lattice builder: a voxel mask to the arrays bclbm_desc takes.  The
+ * reference builds them in Python (PythonScripts/vtklb.py writes a .vtklb
+ * file, src/lbsolver/LBgrid.h and LBnodes.h read it); this restates the
+ * single-rank numbering of vtklb.py:6-45, 84-114, 182-218 and
+ * Nodes::setupNodeType (LBnodes.h:141-209) on the host cores.
+ * mask: [shape[0]*...*shape[nd-1]] in C order (x slowest), 1 fluid, 0 solid.
+ * periodic: bit d set for a periodic axis d (x = 1, y = 2, z = 4).
+ * The result holds neigh [N*Q], types [N] and pos [N*nD] (-1 for node 0) with
+ * N = 1 + n_fluid + n_solid; the bulk list is nodes 1..n_fluid.
+ * ------------------------------------------------------------------------- */
+typedef struct bclbm_lattice bclbm_lattice;
+
+int bclbm_lattice_build(int32_t lattice_q, int32_t nd, const int32_t* shape, const int8_t* mask,
+                        uint32_t periodic, bclbm_lattice** out);
+int bclbm_lattice_info(const bclbm_lattice* lat, int64_t* n_nodes, int64_t* n_fluid, int64_t* n_solid);
+/* copies the arrays out (any pointer may be NULL) */
+int bclbm_lattice_export(const bclbm_lattice* lat, int32_t* neigh, int16_t* types, int32_t* pos);
+void bclbm_lattice_free(bclbm_lattice* lat);
+
+/* ---------------------------------------------------------------------------
+ * Multi-instance batch (continuous batching of many solves on one GPU).  No
+ * counterpart in the reference, whose executables run one geometry per
+ * process; it serves many independent geometries, each one the reference's
+ * std_case time loop (src/std_case/main.cpp:110-145) over its own lattice.
+ *
+ * A batch holds up to max_instances single-phase instances of one lattice,
+ * collision and precision (BGK or TRT; F64 fixed-point or FMA, or a shifted
+ * storage format; BCLBM_FLAG_EXACT is BCLBM_ERR_UNSUPPORTED).  Each instance is
+ * built from an ordinary bclbm_desc, as bclbm_create builds a handle.  All
+ * instances advance together: one persistent kernel per step walks the
+ * concatenated list of every instance's 256-node blocks, and a block of
+ * steps_per_graph steps is captured once as a CUDA graph and replayed (0: no
+ * graph).  Instances are admitted and retired between steps without
+ * re-capturing.  Each instance's populations, moments and sums are
+ * bit-identical to a handle created from the same descriptor and stepped the
+ * same number of times, whatever else is in the batch.
+ * ------------------------------------------------------------------------- */
+typedef struct bclbm_batch bclbm_batch;
+
+int bclbm_batch_create(int32_t lattice_q, int32_t collision, int32_t precision, uint32_t flags,
+                       int32_t max_instances, size_t hbm_budget, int32_t steps_per_graph, bclbm_batch** out);
+/* Admission by HBM footprint: BCLBM_ERR_BUDGET (nothing allocated) if the
+ * instance's bclbm_footprint would take the batch above hbm_budget or no slot
+ * is free.  *id receives the instance id (its slot).  Admission takes the
+ * instance's first time step (the one that reads the initial populations), so
+ * its steps_done is 1 on return. */
+int bclbm_batch_admit(bclbm_batch* b, const bclbm_desc* desc, int32_t* id);
+/* Frees the instance and its HBM; its id may be reused by a later admission. */
+int bclbm_batch_retire(bclbm_batch* b, int32_t id);
+/* Advances every admitted instance by nsteps steps (asynchronous). */
+int bclbm_batch_step(bclbm_batch* b, int32_t nsteps);
+/* bclbm_reduce's sums for n instances (synchronises); steps_done is per instance. */
+int bclbm_batch_stats(bclbm_batch* b, int32_t n, const int32_t* ids, bclbm_stats* out);
+/* bclbm_download_f of one instance (synchronises). */
+int bclbm_batch_download_f(bclbm_batch* b, int32_t id, double* f);
+/* device bytes held by the admitted instances, their number, steps taken by the batch */
+int bclbm_batch_info(bclbm_batch* b, size_t* used_bytes, int32_t* n_active, int64_t* steps);
+int bclbm_batch_sync(bclbm_batch* b);
+const char* bclbm_batch_last_error(const bclbm_batch* b);
+void bclbm_batch_destroy(bclbm_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,7 +16,9 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def bclbm():
+    """The package, with libbclbm.so built (the lattice builder is native too)."""
     import __graft_entry__ as ge
+    ge._load_build_module().build()
     return ge.load()
 
 

@@ -92,3 +92,26 @@ def test_missing_library_fails_loudly(bclbm, tmp_path, monkeypatch):
     monkeypatch.setattr(N, "HERE", tmp_path)
     with pytest.raises(N.BclbmError):
         N.lib()
+
+
+def test_batch_create_validates_on_host(bclbm, native_lib):
+    b = ctypes.c_void_p()
+    L = bclbm.native.lib()
+    assert L.bclbm_batch_create(19, 0, 0, 0, 4, 1 << 30, 50, None) == -1
+    assert L.bclbm_batch_create(7, 0, 0, 0, 4, 1 << 30, 50, ctypes.byref(b)) == -1
+    assert L.bclbm_batch_create(19, 2, 0, 0, 4, 1 << 30, 50, ctypes.byref(b)) == -1  # RK is not batched
+    assert L.bclbm_batch_create(19, 0, 5, 0, 4, 1 << 30, 50, ctypes.byref(b)) == -1
+    assert L.bclbm_batch_create(19, 0, 0, 0, 0, 1 << 30, 50, ctypes.byref(b)) == -1
+    assert L.bclbm_batch_create(19, 0, 0, 1, 4, 1 << 30, 50, ctypes.byref(b)) == -5  # reference order not batched
+    assert not b.value
+    assert L.bclbm_batch_admit(None, None, None) == -1
+    assert L.bclbm_batch_step(None, 1) == -1
+    L.bclbm_batch_destroy(None)
+
+
+def test_batch_create_without_gpu_says_so(bclbm, native_lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    b = ctypes.c_void_p()
+    assert bclbm.native.lib().bclbm_batch_create(19, 0, 2, 0, 4, 1 << 30, 50, ctypes.byref(b)) == -8

@@ -58,3 +58,25 @@ def test_periodic_tables_are_symmetric(bclbm):
             if types[y] > 1:
                 assert nb[y, q] == x
         assert nb[x, 18] == x
+
+
+@pytest.mark.parametrize("lattice,shape", [("D2Q9", (23, 17)), ("D3Q19", (13, 11, 9)), ("D3Q19", (1, 6, 5)),
+                                           ("D2Q9", (2, 40))])
+@pytest.mark.parametrize("periodic", ["", "x", "y", "xz", "xyz"])
+def test_native_lattice_builder_matches_numpy(bclbm, lattice, shape, periodic):
+    rng = np.random.default_rng(len(shape) * 100 + sum(shape) + len(periodic))
+    geo = (rng.random(shape) < 0.6).astype(np.int8)
+    a = bclbm.geometry.build_lattice(geo, lattice, periodic)
+    b = bclbm.geometry.build_lattice_numpy(geo, lattice, periodic)
+    for k in ("neigh", "types", "pos"):
+        assert np.array_equal(a[k], b[k]), k
+    assert (a["nf"], a["ns"]) == (b["nf"], b["ns"])
+
+
+def test_native_lattice_builder_rejects_bad_masks(bclbm):
+    with pytest.raises(ValueError):
+        bclbm.geometry.build_lattice(np.full((4, 4, 4), 2, dtype=np.int8), "D3Q19", "")
+    with pytest.raises(bclbm.native.BclbmError):
+        bclbm.native.lattice_tables(np.full((4, 4, 4), 2, dtype=np.int8), 19, 0)
+    with pytest.raises(bclbm.native.BclbmError):
+        bclbm.native.lattice_tables(np.ones((4, 4), dtype=np.int8), 19, 0)
