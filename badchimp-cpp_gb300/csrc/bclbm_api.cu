@@ -447,6 +447,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     h->fma64 = (d->flags & BCLBM_FLAG_FP64_FMA) != 0;
     h->flux = d->collision == BCLBM_RK && d->flux_control != 0;
     h->n_nodes = d->n_nodes;
+    h->footprint = footprint_bytes(d, p);
     h->nf = p.nf;
     h->nf_pad = p.nf_pad;
     h->ns = p.ns;

@@ -8,8 +8,11 @@
 //               step at which it was admitted;
 //   work[w]     (slot, first fluid slot) of every 256-node block of every
 //               admitted instance, instances contiguous;
-//   n_work, step  the work-list length and the global step counter.
-// The persistent kernel reads all four at run time, so its launch parameters
+//   n_work, step  the work-list length and the global step counter;
+//   next        the item counter: the persistent kernel's blocks (a fixed
+//               grid, one wave) take items from it in list order; the tick
+//               after each step advances step and rewinds next.
+// The persistent kernel reads all of them at run time, so its launch parameters
 // never change and the graph captured once stays valid while instances are
 // admitted and retired between replays.  An instance's ping-pong parity follows
 // from (step - admitted_step), so instances that joined at different times
@@ -29,6 +32,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "bclbm.h"
@@ -71,16 +75,34 @@ __device__ __forceinline__ void load_inst(const BatchInst* __restrict__ inst, in
     __syncthreads();
 }
 
+// resident blocks per SM asked of the register allocator: the kernel arguments
+// live in shared memory, and without a bound the allocator keeps them all in
+// registers across the item loop (FP16/FP32: 85 instead of the ~62 of the
+// single-instance kernel, one block per SM fewer)
+template <class S, int MODE>
+constexpr int batch_min_blocks() {
+    return std::is_same<S, double>::value ? 2 : 4;
+}
+
 template <int Q, class S, int MODE, bool TRT>
-__global__ void __launch_bounds__(kBlock, MODE == 2 ? 2 : 1) k_batch_step(const BatchInst* __restrict__ inst,
+__global__ void __launch_bounds__(kBlock, batch_min_blocks<S, MODE>()) k_batch_step(const BatchInst* __restrict__ inst,
                                                        const int2* __restrict__ work, const int* n_work,
-                                                       const long long* step) {
+                                                       const long long* step, int* next_item) {
     __shared__ __align__(16) unsigned char smem[sizeof(StepArgs)];
+    __shared__ int s_item;
     StepArgs& a = *reinterpret_cast<StepArgs*>(smem);
     const long long st = *step;
     const int nw = *n_work;
+    // Items are taken from a counter in list order, as the hardware hands out the
+    // blocks of an ordinary launch: the items in flight stay a compact window of
+    // the node list, whose upstream neighbours are still in L2 (a static
+    // grid-stride split lets the blocks drift apart: 20% slower on 256^3).
     int cur = -1;
-    for (int w = blockIdx.x; w < nw; w += gridDim.x) {
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(next_item, 1);
+        __syncthreads();
+        const int w = s_item;
+        if (w >= nw) break;
         const int2 wk = work[w];
         if (wk.x != cur) {
             load_inst(inst, wk.x, st, a);
@@ -88,11 +110,16 @@ __global__ void __launch_bounds__(kBlock, MODE == 2 ? 2 : 1) k_batch_step(const 
         }
         const int i = wk.y + threadIdx.x;
         if (i < a.L.nf) batch_node<Q, S, MODE, TRT>(a, i);
+        __syncthreads();  // s_item is rewritten at the next item
     }
 }
 
-__global__ void k_batch_tick(long long* step) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) *step += 1;
+// after each step: advance the step counter, rewind the item counter
+__global__ void k_batch_tick(long long* step, int* next_item) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        *step += 1;
+        *next_item = 0;
+    }
 }
 
 template <int Q, class S>
@@ -142,7 +169,7 @@ __global__ void __launch_bounds__(kBlock) k_batch_final(const double* __restrict
         }
 }
 
-using StepKernel = void (*)(const BatchInst*, const int2*, const int*, const long long*);
+using StepKernel = void (*)(const BatchInst*, const int2*, const int*, const long long*, int*);
 using MomKernel = void (*)(const BatchInst*, const int2*, const int*, const long long*, double*);
 
 template <int Q>
@@ -189,6 +216,7 @@ struct bclbm_batch {
     int2* d_work = nullptr;
     int* d_nwork = nullptr;
     long long* d_step = nullptr;
+    int* d_next = nullptr;  // item counter of the step kernel
     double* d_partials = nullptr;
     int* d_first = nullptr;
     int* d_count = nullptr;
@@ -220,6 +248,7 @@ void batch_free(bclbm_batch* b) {
     cudaFree(b->d_work);
     cudaFree(b->d_nwork);
     cudaFree(b->d_step);
+    cudaFree(b->d_next);
     cudaFree(b->d_partials);
     cudaFree(b->d_first);
     cudaFree(b->d_count);
@@ -271,8 +300,8 @@ int upload_work(bclbm_batch* b) {
 
 int launch_steps_direct(bclbm_batch* b, int n) {
     for (int k = 0; k < n; ++k) {
-        b->step_kernel<<<b->grid, kBlock, 0, b->stream>>>(b->d_inst, b->d_work, b->d_nwork, b->d_step);
-        k_batch_tick<<<1, 32, 0, b->stream>>>(b->d_step);
+        b->step_kernel<<<b->grid, kBlock, 0, b->stream>>>(b->d_inst, b->d_work, b->d_nwork, b->d_step, b->d_next);
+        k_batch_tick<<<1, 32, 0, b->stream>>>(b->d_step, b->d_next);
         launch_counter() += 2;
     }
     BTRY(b, cudaGetLastError());
@@ -284,8 +313,8 @@ int ensure_graph(bclbm_batch* b) {
     cudaGraph_t g = nullptr;
     BTRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < b->graph_steps; ++k) {
-        b->step_kernel<<<b->grid, kBlock, 0, b->stream>>>(b->d_inst, b->d_work, b->d_nwork, b->d_step);
-        k_batch_tick<<<1, 32, 0, b->stream>>>(b->d_step);
+        b->step_kernel<<<b->grid, kBlock, 0, b->stream>>>(b->d_inst, b->d_work, b->d_nwork, b->d_step, b->d_next);
+        k_batch_tick<<<1, 32, 0, b->stream>>>(b->d_step, b->d_next);
     }
     const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
     if (ec != cudaSuccess) return bfail(b, BCLBM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
@@ -348,6 +377,7 @@ int bclbm_batch_create(int32_t lattice_q, int32_t collision, int32_t precision, 
     if (cudaMalloc(&b->d_inst, sizeof(BatchInst) * max_instances) != cudaSuccess ||
         cudaMalloc(&b->d_work, sizeof(int2) * b->max_work) != cudaSuccess ||
         cudaMalloc(&b->d_nwork, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_step, sizeof(long long)) != cudaSuccess ||
+        cudaMalloc(&b->d_next, sizeof(int)) != cudaSuccess ||
         cudaMalloc(&b->d_partials, sizeof(double) * 6 * static_cast<size_t>(b->max_work)) != cudaSuccess ||
         cudaMalloc(&b->d_first, sizeof(int) * max_instances) != cudaSuccess ||
         cudaMalloc(&b->d_count, sizeof(int) * max_instances) != cudaSuccess ||
@@ -356,6 +386,7 @@ int bclbm_batch_create(int32_t lattice_q, int32_t collision, int32_t precision, 
     const int zero = 0;
     const long long zstep = 0;
     if (cudaMemcpyAsync(b->d_nwork, &zero, sizeof(int), cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
+        cudaMemcpyAsync(b->d_next, &zero, sizeof(int), cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
         cudaMemcpyAsync(b->d_step, &zstep, sizeof(long long), cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
         cudaStreamSynchronize(b->stream) != cudaSuccess)
         return cleanup(BCLBM_ERR_CUDA);
@@ -364,14 +395,20 @@ int bclbm_batch_create(int32_t lattice_q, int32_t collision, int32_t precision, 
 }
 
 int bclbm_batch_admit(bclbm_batch* b, const bclbm_desc* desc, int32_t* id) {
-    if (!b || !desc || !id) return BCLBM_ERR_INVALID;
+    return bclbm_batch_admit_steps(b, desc, 1, id);
+}
+
+int bclbm_batch_attach(bclbm_batch* b, bclbm_handle* h, int32_t* id) {
+    if (!b || !h || !id) return BCLBM_ERR_INVALID;
     *id = -1;
-    if (desc->lattice_q != b->q || desc->collision != b->collision || desc->precision != b->precision ||
-        (desc->flags & (BCLBM_FLAG_EXACT | BCLBM_FLAG_FP64_FMA)) != (b->flags & (BCLBM_FLAG_EXACT | BCLBM_FLAG_FP64_FMA)))
-        return bfail(b, BCLBM_ERR_INVALID, "descriptor does not match the batch's lattice, collision or precision");
-    size_t need = 0;
-    int rc = bclbm_footprint(desc, &need);
-    if (rc) return rc;
+    if (h->q != b->q || h->collision != b->collision || h->precision != b->precision || h->exact ||
+        h->fma64 != ((b->flags & BCLBM_FLAG_FP64_FMA) != 0))
+        return bfail(b, BCLBM_ERR_INVALID, "handle does not match the batch's lattice, collision or precision");
+    if (h->steps_done < 1 || !h->state_post)
+        return bfail(b, BCLBM_ERR_INVALID, "attach needs a handle that has taken at least one step");
+    for (int s = 0; s < b->max_inst; ++s)
+        if (b->handle[s] == h) return bfail(b, BCLBM_ERR_INVALID, "handle already attached");
+    const size_t need = h->footprint;
     int slot = -1;
     for (int s = 0; s < b->max_inst; ++s)
         if (!b->handle[s]) {
@@ -380,37 +417,52 @@ int bclbm_batch_admit(bclbm_batch* b, const bclbm_desc* desc, int32_t* id) {
         }
     if (slot < 0 || b->used + need > b->budget) return bfail(b, BCLBM_ERR_BUDGET, "no free slot or HBM budget");
     BTRY(b, cudaSetDevice(b->device));
+    BTRY(b, cudaStreamSynchronize(h->stream));
     BTRY(b, cudaStreamSynchronize(b->stream));
-    bclbm_handle* h = nullptr;
-    rc = bclbm_create(desc, &h);
-    if (rc) return bfail(b, rc, std::string("instance creation: ") + bclbm_error(rc));
-    rc = bclbm_step(h, 1);
-    if (rc == BCLBM_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = BCLBM_ERR_CUDA;
-    if (rc) {
-        b->last_error = std::string("first step: ") + bclbm_last_error(h);
-        bclbm_destroy(h);
-        return rc;
-    }
     BatchInst bi;
     std::memset(&bi, 0, sizeof(bi));
     bi.args = handle_args(h);
     bi.pops[0] = h->pops[0];
     bi.pops[1] = h->pops[1];
-    bi.start_step = b->host_step - 1;  // one step taken: the state is in pops[1]
+    // the state is in pops[steps_done & 1] (== h->cur); start_step keeps that parity
+    bi.start_step = b->host_step - h->steps_done;
     for (int k = 0; k < 3; ++k) bi.force[k] = h->force[k];
-    cudaError_t e = cudaMemcpyAsync(b->d_inst + slot, &bi, sizeof(bi), cudaMemcpyHostToDevice, b->stream);
-    if (e != cudaSuccess) {
-        bclbm_destroy(h);
-        return bfail(b, BCLBM_ERR_CUDA, cudaGetErrorString(e));
-    }
+    BTRY(b, cudaMemcpyAsync(b->d_inst + slot, &bi, sizeof(bi), cudaMemcpyHostToDevice, b->stream));
     b->handle[slot] = h;
     b->bytes[slot] = need;
-    b->start[slot] = b->host_step - 1;
+    b->start[slot] = bi.start_step;
     b->used += need;
-    rc = upload_work(b);
+    const int rc = upload_work(b);
     if (rc) return rc;
     *id = slot;
     return BCLBM_OK;
+}
+
+int bclbm_batch_admit_steps(bclbm_batch* b, const bclbm_desc* desc, int32_t first_steps, int32_t* id) {
+    if (!b || !desc || !id || first_steps < 1) return BCLBM_ERR_INVALID;
+    *id = -1;
+    if (desc->lattice_q != b->q || desc->collision != b->collision || desc->precision != b->precision ||
+        (desc->flags & (BCLBM_FLAG_EXACT | BCLBM_FLAG_FP64_FMA)) != (b->flags & (BCLBM_FLAG_EXACT | BCLBM_FLAG_FP64_FMA)))
+        return bfail(b, BCLBM_ERR_INVALID, "descriptor does not match the batch's lattice, collision or precision");
+    size_t need = 0;
+    int rc = bclbm_footprint(desc, &need);
+    if (rc) return rc;
+    int free_slots = 0;
+    for (auto* x : b->handle) free_slots += x == nullptr;
+    if (free_slots == 0 || b->used + need > b->budget) return bfail(b, BCLBM_ERR_BUDGET, "no free slot or HBM budget");
+    BTRY(b, cudaSetDevice(b->device));
+    bclbm_handle* h = nullptr;
+    rc = bclbm_create(desc, &h);
+    if (rc) return bfail(b, rc, std::string("instance creation: ") + bclbm_error(rc));
+    rc = bclbm_step(h, first_steps);
+    if (rc) {
+        b->last_error = std::string("first steps: ") + bclbm_last_error(h);
+        bclbm_destroy(h);
+        return rc;
+    }
+    rc = bclbm_batch_attach(b, h, id);
+    if (rc) bclbm_destroy(h);
+    return rc;
 }
 
 int bclbm_batch_retire(bclbm_batch* b, int32_t id) {

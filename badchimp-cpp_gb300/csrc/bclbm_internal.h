@@ -43,6 +43,7 @@ struct bclbm_handle {
     double* d_gather = nullptr;
     int32_t ghost_src[19] = {0};
     int64_t steps_done = 0;
+    size_t footprint = 0;             // device bytes (bclbm_footprint of the descriptor)
     std::string last_error;
 };
 

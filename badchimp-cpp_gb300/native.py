@@ -63,12 +63,13 @@ class Timing(ctypes.Structure):
                 ("density_ms", ctypes.c_double), ("launches", ctypes.c_int64), ("nsteps", ctypes.c_int32)]
 
 
-EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_step_timed", "bclbm_download_f", "bclbm_download_macros", "bclbm_reduce",
-           "bclbm_set_force", "bclbm_node_perm", "bclbm_footprint", "bclbm_sync", "bclbm_destroy", "bclbm_error",
-           "bclbm_last_error", "bclbm_launch_count", "bclbm_moments_static", "bclbm_batch_create", "bclbm_batch_admit",
-           "bclbm_batch_retire", "bclbm_batch_step", "bclbm_batch_stats", "bclbm_batch_download_f", "bclbm_batch_info",
-           "bclbm_batch_sync", "bclbm_batch_last_error", "bclbm_batch_destroy", "bclbm_lattice_build",
-           "bclbm_lattice_info", "bclbm_lattice_export", "bclbm_lattice_free"]
+EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_step_timed", "bclbm_download_f", "bclbm_download_macros",
+           "bclbm_reduce", "bclbm_set_force", "bclbm_node_perm", "bclbm_footprint", "bclbm_sync", "bclbm_destroy",
+           "bclbm_error", "bclbm_last_error", "bclbm_launch_count", "bclbm_moments_static", "bclbm_batch_create",
+           "bclbm_batch_admit", "bclbm_batch_admit_steps", "bclbm_batch_attach", "bclbm_batch_retire",
+           "bclbm_batch_step", "bclbm_batch_stats", "bclbm_batch_download_f", "bclbm_batch_info", "bclbm_batch_sync",
+           "bclbm_batch_last_error", "bclbm_batch_destroy", "bclbm_lattice_build", "bclbm_lattice_info",
+           "bclbm_lattice_export", "bclbm_lattice_free"]
 
 
 def lib_path() -> Path:
@@ -119,6 +120,8 @@ def lib():
     i32 = ctypes.c_int32
     L.bclbm_batch_create.argtypes = [i32, i32, i32, ctypes.c_uint32, i32, ctypes.c_size_t, i32, ctypes.POINTER(vp)]
     L.bclbm_batch_admit.argtypes = [vp, ctypes.POINTER(Desc), ctypes.POINTER(i32)]
+    L.bclbm_batch_admit_steps.argtypes = [vp, ctypes.POINTER(Desc), i32, ctypes.POINTER(i32)]
+    L.bclbm_batch_attach.argtypes = [vp, vp, ctypes.POINTER(i32)]
     L.bclbm_batch_retire.argtypes = [vp, i32]
     L.bclbm_batch_step.argtypes = [vp, i32]
     L.bclbm_batch_stats.argtypes = [vp, i32, vp, ctypes.POINTER(Stats)]
@@ -126,8 +129,9 @@ def lib():
     L.bclbm_batch_info.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(i32),
                                    ctypes.POINTER(ctypes.c_int64)]
     L.bclbm_batch_sync.argtypes = [vp]
-    for name in ("bclbm_batch_create", "bclbm_batch_admit", "bclbm_batch_retire", "bclbm_batch_step",
-                 "bclbm_batch_stats", "bclbm_batch_download_f", "bclbm_batch_info", "bclbm_batch_sync"):
+    for name in ("bclbm_batch_create", "bclbm_batch_admit", "bclbm_batch_admit_steps", "bclbm_batch_attach",
+                 "bclbm_batch_retire", "bclbm_batch_step", "bclbm_batch_stats", "bclbm_batch_download_f",
+                 "bclbm_batch_info", "bclbm_batch_sync"):
         getattr(L, name).restype = ctypes.c_int
     L.bclbm_batch_last_error.argtypes = [vp]
     L.bclbm_batch_last_error.restype = ctypes.c_char_p

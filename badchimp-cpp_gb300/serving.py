@@ -18,10 +18,11 @@ from the FP64 flux reduction, run until k changes by less than ``tol``
   from a captured CUDA graph;
 * after each block the FP64 sums of every instance give its permeability;
   converged instances are retired and their HBM is free for the next request;
-* with a precision ladder ("f16>f32", the default) a request runs in FP16
-  storage while its flow develops and moves to FP32 storage once k has
-  settled to within ``promote_tol`` per block: FP16 rounding leaves k a noise
-  floor of 1e-6..1e-5 per block, above the convergence tolerance.
+* the storage format is FP32-shifted by default.  FP16 rounding leaves k a
+  noise floor of 1e-6..1e-5 per 500-step block, above the 1e-6 stopping
+  tolerance, so an FP16 solve stops late or not at all; a precision ladder
+  ("f16>f32") runs a request in FP16 while its flow develops and moves it to
+  FP32 once k has settled to within ``promote_tol`` per block.
 
 ``Server.run_sequential`` serves the same requests one at a time through the
 single-instance ``Solver`` (the baseline).  Both report per-request latency
@@ -133,19 +134,32 @@ class Batch:
     def footprint(self, lat) -> int:
         return _native.footprint(lat, self.collision, self.precision, self.flags)
 
-    def admit(self, lat, f_init, tau, force):
-        """Admits one instance; returns its id, or None when the budget or slots are full."""
+    def admit(self, lat, f_init, tau, force, first_steps: int = 1):
+        """Admits one instance (taking its first ``first_steps`` steps); returns its id,
+        or None when the budget or slots are full."""
         F = np.zeros(3)
         F[:len(force)] = force
         f_init = np.ascontiguousarray(f_init, dtype=np.float64)
         d = _native.make_desc(lat, f_init, self.collision, self.precision, self.flags,
                               (float(tau[0]), float(tau[-1])), F, 0.0, 0.0, 0, 0.0, 1.0, 0.0, None)
         i = ctypes.c_int32(-1)
-        rc = _native.lib().bclbm_batch_admit(self._b, ctypes.byref(d), ctypes.byref(i))
+        rc = _native.lib().bclbm_batch_admit_steps(self._b, ctypes.byref(d), int(first_steps), ctypes.byref(i))
         if rc == BUDGET:
             return None
         self._check(rc)
         self._lat[i.value] = lat
+        return i.value
+
+    def attach(self, solver):
+        """Admits a Solver created elsewhere (it must have taken >= 1 step); the batch
+        takes its handle over.  Returns the id, or None when the budget or slots are full."""
+        i = ctypes.c_int32(-1)
+        rc = _native.lib().bclbm_batch_attach(self._b, solver._h, ctypes.byref(i))
+        if rc == BUDGET:
+            return None
+        self._check(rc)
+        solver._h = None  # owned by the batch from here on
+        self._lat[i.value] = solver.lat
         return i.value
 
     def retire(self, iid: int):
@@ -209,7 +223,7 @@ def summarize(results, t_start: float, t_end: float) -> dict:
 class Server:
     """Continuous-batching server for permeability requests on one GPU."""
 
-    def __init__(self, precision="f16>f32", max_instances: int = 256, hbm_budget: int | None = None,
+    def __init__(self, precision="f32", max_instances: int = 256, hbm_budget: int | None = None,
                  check_every: int = 500, tol: float = 1e-6, max_steps: int = 50000, steps_per_graph: int = 50,
                  prep_workers: int = 4, fma64: bool = False, promote_tol: float = 1e-4):
         self.precision = precision
@@ -230,37 +244,55 @@ class Server:
             return True, True
         return steps >= self.max_steps, False
 
+    def _create(self, stage: int, lat, f_init, r: Request, first_steps: int):
+        """Host thread: a single-instance handle in the stage's format, stepped
+        first_steps times on its own stream (overlaps the running batch)."""
+        s = _lb.Solver(lat, f_init, tau=(r.tau, r.tau), force=(r.gx, 0.0, 0.0), precision=self.stages[stage],
+                       fma64=self.fma64)
+        s.step(first_steps)
+        s.sync()
+        return s
+
     def run(self, requests, prepared=None) -> dict:
         """Serves ``requests`` with continuous batching; returns the report.
         ``prepared`` optionally maps rid -> (lattice, f0) built beforehand.
 
-        With a precision ladder such as "f16>f32", an instance starts in the
-        first storage format; once its permeability changes by less than
-        ``promote_tol`` over a block, its populations (the reference f after the
-        last step) move into the next format's batch, where the convergence
-        test runs afresh."""
+        Instances are created (upload and first step) on host threads while the
+        batch runs, and attached between blocks.  With a precision ladder such
+        as "f16>f32", an instance starts in the first storage format; once its
+        permeability changes by less than ``promote_tol`` over a block, its
+        populations (the reference f after the last step) move into the next
+        format, where the convergence test runs afresh."""
         reqs = sorted(requests, key=lambda r: (r.arrival, r.rid))
         by_id = {r.rid: r for r in reqs}
         results = []
         cnt = {"admitted": 0, "retired": 0, "promoted": 0, "refused_budget": 0, "rejected_too_large": 0,
                "blocks": 0, "peak_active": 0, "peak_bytes": 0}
-        pool = cf.ThreadPoolExecutor(max_workers=self.prep_workers)
+        prep_pool = cf.ThreadPoolExecutor(max_workers=self.prep_workers)
+        make_pool = cf.ThreadPoolExecutor(max_workers=2)
         budget = self.hbm_budget
         if budget is None:
             import torch
             budget = int(torch.cuda.mem_get_info()[0] * 0.8)
         batches = [Batch(precision=p, max_instances=self.max_instances, hbm_budget=budget,
                          steps_per_graph=self.steps_per_graph, fma64=self.fma64) for p in self.stages]
+        creating = []  # [stage, future, need, record]
         try:
             pending = deque(reqs)
             preps = deque()  # (rid, future) in arrival order
             ready = deque()  # (rid, lattice, f0)
-            active = {}  # (stage, iid) -> dict
+            active = {}  # (stage, iid) -> record
             t0 = time.perf_counter()
             clock = lambda: time.perf_counter() - t0  # noqa: E731
 
             def used():
                 return sum(b.info()["used_bytes"] for b in batches)
+
+            def committed():
+                return used() + sum(c[2] for c in creating)
+
+            def in_stage(st):
+                return sum(1 for k in active if k[0] == st) + sum(1 for c in creating if c[0] == st)
 
             while len(results) < len(reqs):
                 now = clock()
@@ -269,32 +301,43 @@ class Server:
                     if prepared is not None and r.rid in prepared:
                         preps.append((r.rid, None))
                     else:
-                        preps.append((r.rid, pool.submit(prepare, r)))
+                        preps.append((r.rid, prep_pool.submit(prepare, r)))
                 while preps and (preps[0][1] is None or preps[0][1].done()):
                     rid, fut = preps.popleft()
                     lat, f0 = prepared[rid] if fut is None else fut.result()
                     ready.append((rid, lat, f0))
+                # admission by HBM footprint, in arrival order
                 while ready:
                     rid, lat, f0 = ready[0]
                     r = by_id[rid]
-                    need = max(b.footprint(lat) for b in batches)
-                    if need > budget:
+                    if max(b.footprint(lat) for b in batches) > budget:
                         ready.popleft()
                         cnt["rejected_too_large"] += 1
                         results.append(Result(rid, float("nan"), 0, False, r.arrival, clock(), clock(), lat.n_bulk))
                         continue
-                    iid = None
-                    if used() + batches[0].footprint(lat) <= budget:
-                        iid = batches[0].admit(lat, f0, (r.tau, r.tau), (r.gx, 0.0, 0.0))
-                    if iid is None:
+                    need = batches[0].footprint(lat)
+                    if committed() + need > budget or in_stage(0) >= self.max_instances:
                         cnt["refused_budget"] += 1
                         break
                     ready.popleft()
-                    cnt["admitted"] += 1
-                    active[(0, iid)] = {"rid": rid, "k": None, "admitted": clock(), "n": lat.n_bulk, "hist": [],
-                                        "lat": lat, "offset": 0}
+                    rec = {"rid": rid, "k": None, "admitted": clock(), "n": lat.n_bulk, "hist": [], "lat": lat,
+                           "offset": 0}
+                    creating.append([0, make_pool.submit(self._create, 0, lat, f0, r, 1), need, rec])
+                # attach the instances whose set-up has finished
+                for c in [c for c in creating if c[1].done()]:
+                    st, fut, need, rec = c
+                    iid = batches[st].attach(fut.result())
+                    if iid is None:
+                        raise RuntimeError("attach refused an instance whose footprint was reserved")
+                    creating.remove(c)
+                    active[(st, iid)] = rec
+                    if st == 0:
+                        cnt["admitted"] += 1
                 if not active:
-                    time.sleep(0.0005)
+                    if creating:
+                        cf.wait([c[1] for c in creating], timeout=0.05, return_when=cf.FIRST_COMPLETED)
+                    else:
+                        time.sleep(0.0005)
                     continue
                 cnt["peak_active"] = max(cnt["peak_active"], len(active))
                 cnt["peak_bytes"] = max(cnt["peak_bytes"], used())
@@ -319,14 +362,17 @@ class Server:
                             if not done and a["k"] is not None and k != 0.0 \
                                     and abs(k - a["k"]) / abs(k) < self.promote_tol:
                                 lat = a["lat"]
-                                if used() - batches[st].footprint(lat) + batches[st + 1].footprint(lat) <= budget:
+                                need = batches[st + 1].footprint(lat)
+                                if committed() - batches[st].footprint(lat) + need <= budget:
                                     f = batches[st].download_f(key[1])
                                     batches[st].retire(key[1])
-                                    nid = batches[st + 1].admit(lat, f, (r.tau, r.tau), (r.gx, 0.0, 0.0))
                                     del active[key]
-                                    # steps_done restarts at 1 there: the admission step
+                                    # two first steps keep the parity of the step count at the
+                                    # checks: the flux of a pack can differ between odd and even
+                                    # steps (a period-2 mode of the step), by 1e-3 of k in small packs
                                     a.update(k=None, offset=steps)
-                                    active[(st + 1, nid)] = a
+                                    creating.append([st + 1, make_pool.submit(self._create, st + 1, lat, f, r, 2),
+                                                     need, a])
                                     cnt["promoted"] += 1
                                     continue
                         else:
@@ -340,9 +386,15 @@ class Server:
                             del active[key]
             t_end = clock()
         finally:
+            for c in creating:
+                try:
+                    c[1].result().close()
+                except Exception:
+                    pass
             for b in batches:
                 b.close()
-        pool.shutdown(wait=True)
+            prep_pool.shutdown(wait=True)
+            make_pool.shutdown(wait=True)
         results.sort(key=lambda x: x.rid)
         rep = summarize(results, 0.0, t_end)
         rep["counters"] = cnt

@@ -394,7 +394,7 @@ def run_serving(args, world, rank):
             prepared[r.rid] = res
     log(f"prepared {len(reqs)} requests in {time.time() - t:.1f}s; sides {sorted(r.size for r in reqs)}")
     srv = S.Server(precision=args.serving_precision, check_every=args.check_every, tol=args.tol,
-                   max_steps=args.max_steps, steps_per_graph=args.steps_per_graph)
+                   max_steps=args.max_steps, steps_per_graph=args.steps_per_graph, promote_tol=args.promote_tol)
     peak, peak_kind = peaks()
     gpu_index = 0
     # warm-up: one small request through both paths (graph capture, module load)
@@ -434,6 +434,11 @@ def run_serving(args, world, rank):
                    "host_preparation": "geometry and node tables built before the timed region for both arms",
                    "l2": "instances of up to several GB against 129 MB L2"},
         "serving": {str(r): brief(out[r]) | {"counters": out[r]["counters"]} for r in rates},
+        "requests": [{"rid": q.rid, "side": q.size, "tau": round(q.tau, 4), "radius": round(q.radius, 3),
+                      "porosity": round(q.porosity, 4), "fluid": a.n_fluid, "steps": a.steps,
+                      "steps_baseline": c.steps, "latency_s": round(a.latency, 4),
+                      "latency_baseline_s": round(c.latency, 4), "k": a.permeability, "k_baseline": c.permeability}
+                     for q, a, c in zip(reqs, head["results"], base["results"])],
         "sequential_baseline": brief(base) | {"precision": args.baseline_precision},
         "speedup_solves_per_s": head["solves_per_s"] / base["solves_per_s"],
         "accuracy": {"max_rel_perm_err_vs_baseline": max(errs) if errs else None,
@@ -441,13 +446,13 @@ def run_serving(args, world, rank):
         "clocks": clk.summary(), "gpu_launches": launches,
         "e2e": {"value": head["solves_per_s"], "unit": "solves/s",
                 "h2d_bytes_per_step": float(np.mean([prepared[r.rid][1].nbytes + prepared[r.rid][0].neigh.nbytes
-                                                     for r in reqs])),
+                                                     + prepared[r.rid][0].types.nbytes for r in reqs])),
                 "d2h_bytes_per_step": 96.0 * args.max_steps / args.check_every,
                 "path": "per request: bclbm_batch_admit from host arrays, batched steps, bclbm_batch_stats every "
                         "check block, bclbm_batch_retire"},
         "roofline": {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_kind": peak_kind,
-                     "achieved": head["lattice_updates"] / head["seconds"] * BYTES_PER_UPDATE[args.serving_precision]
-                     / 1e9, "traffic": None,
+                     "achieved": head["lattice_updates"] / head["seconds"]
+                     * BYTES_PER_UPDATE[args.serving_precision.split(">")[0]] / 1e9, "traffic": None,
                      "note": "algorithmic bytes of all lattice updates over the whole serving run (wall clock)"},
     }
     line["roofline"]["frac"] = line["roofline"]["achieved"] / peak
@@ -486,7 +491,10 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--max-steps", type=int, default=50000)
     ap.add_argument("--steps-per-graph", type=int, default=50)
-    ap.add_argument("--serving-precision", default="f16", choices=["f64", "f32", "f16", "bf16"])
+    ap.add_argument("--serving-precision", default="f32",
+                    help="storage format of the batched server, or a ladder such as f16>f32")
+    ap.add_argument("--promote-tol", type=float, default=2e-5,
+                    help="ladder: |dk/k| per check block at which a request moves to the next format")
     ap.add_argument("--baseline-precision", default="f64", choices=["f64", "f32", "f16", "bf16"])
     args = ap.parse_args()
     if args.warmup < 3:

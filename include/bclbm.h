@@ -231,6 +231,15 @@ int bclbm_batch_create(int32_t lattice_q, int32_t collision, int32_t precision, 
  * instance's first time step (the one that reads the initial populations), so
  * its steps_done is 1 on return. */
 int bclbm_batch_admit(bclbm_batch* b, const bclbm_desc* desc, int32_t* id);
+/* bclbm_batch_admit taking first_steps >= 1 steps with the single-instance
+ * kernel before the instance joins (steps_done = first_steps on return); used
+ * to keep the parity of a solve's step count when it moves between batches. */
+int bclbm_batch_admit_steps(bclbm_batch* b, const bclbm_desc* desc, int32_t first_steps, int32_t* id);
+/* Admission of a handle the caller created (bclbm_create + bclbm_step, e.g. on
+ * another host thread while the batch runs): on BCLBM_OK the batch owns h and
+ * destroys it at retirement; on any error h stays the caller's.  h must match
+ * the batch's lattice, collision and precision and have taken >= 1 step. */
+int bclbm_batch_attach(bclbm_batch* b, bclbm_handle* h, int32_t* id);
 /* Frees the instance and its HBM; its id may be reused by a later admission. */
 int bclbm_batch_retire(bclbm_batch* b, int32_t id);
 /* Advances every admitted instance by nsteps steps (asynchronous). */
