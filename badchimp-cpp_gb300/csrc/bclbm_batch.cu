@@ -9,9 +9,10 @@
 //   work[w]     (slot, first fluid slot) of every 256-node block of every
 //               admitted instance, instances contiguous;
 //   n_work, step  the work-list length and the global step counter;
-//   next        the item counter: the persistent kernel's blocks (a fixed
-//               grid, one wave) take items from it in list order; the tick
-//               after each step advances step and rewinds next.
+//   ctr         the item counter, from which the persistent kernel's blocks
+//               (a fixed grid, one wave) take items in list order, and a count
+//               of finished blocks: the last block of a step advances step and
+//               rewinds both, so one launch is one step.
 // The persistent kernel reads all of them at run time, so its launch parameters
 // never change and the graph captured once stays valid while instances are
 // admitted and retired between replays.  An instance's ping-pong parity follows
@@ -87,9 +88,11 @@ constexpr int batch_min_blocks() {
 template <int Q, class S, int MODE, bool TRT>
 __global__ void __launch_bounds__(kBlock, batch_min_blocks<S, MODE>()) k_batch_step(const BatchInst* __restrict__ inst,
                                                        const int2* __restrict__ work, const int* n_work,
-                                                       const long long* step, int* next_item) {
+                                                       long long* step, int* ctr) {
     __shared__ __align__(16) unsigned char smem[sizeof(StepArgs)];
     __shared__ int s_item;
+    __shared__ int s_last;
+    int* next_item = ctr;  // ctr[0]: next item; ctr[1]: blocks finished
     StepArgs& a = *reinterpret_cast<StepArgs*>(smem);
     const long long st = *step;
     const int nw = *n_work;
@@ -112,13 +115,18 @@ __global__ void __launch_bounds__(kBlock, batch_min_blocks<S, MODE>()) k_batch_s
         if (i < a.L.nf) batch_node<Q, S, MODE, TRT>(a, i);
         __syncthreads();  // s_item is rewritten at the next item
     }
-}
-
-// after each step: advance the step counter, rewind the item counter
-__global__ void k_batch_tick(long long* step, int* next_item) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        *step += 1;
-        *next_item = 0;
+    // the last block to finish advances the step and rewinds the counters for the
+    // next launch; every block has read *step before it counts itself finished
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&ctr[1], 1) == static_cast<int>(gridDim.x) - 1;
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        *step = st + 1;
+        ctr[0] = 0;
+        ctr[1] = 0;
+        __threadfence();
     }
 }
 
@@ -169,7 +177,7 @@ __global__ void __launch_bounds__(kBlock) k_batch_final(const double* __restrict
         }
 }
 
-using StepKernel = void (*)(const BatchInst*, const int2*, const int*, const long long*, int*);
+using StepKernel = void (*)(const BatchInst*, const int2*, const int*, long long*, int*);
 using MomKernel = void (*)(const BatchInst*, const int2*, const int*, const long long*, double*);
 
 template <int Q>
@@ -216,7 +224,7 @@ struct bclbm_batch {
     int2* d_work = nullptr;
     int* d_nwork = nullptr;
     long long* d_step = nullptr;
-    int* d_next = nullptr;  // item counter of the step kernel
+    int* d_ctr = nullptr;  // step kernel counters: next item, blocks finished
     double* d_partials = nullptr;
     int* d_first = nullptr;
     int* d_count = nullptr;
@@ -248,7 +256,7 @@ void batch_free(bclbm_batch* b) {
     cudaFree(b->d_work);
     cudaFree(b->d_nwork);
     cudaFree(b->d_step);
-    cudaFree(b->d_next);
+    cudaFree(b->d_ctr);
     cudaFree(b->d_partials);
     cudaFree(b->d_first);
     cudaFree(b->d_count);
@@ -300,9 +308,8 @@ int upload_work(bclbm_batch* b) {
 
 int launch_steps_direct(bclbm_batch* b, int n) {
     for (int k = 0; k < n; ++k) {
-        b->step_kernel<<<b->grid, kBlock, 0, b->stream>>>(b->d_inst, b->d_work, b->d_nwork, b->d_step, b->d_next);
-        k_batch_tick<<<1, 32, 0, b->stream>>>(b->d_step, b->d_next);
-        launch_counter() += 2;
+        b->step_kernel<<<b->grid, kBlock, 0, b->stream>>>(b->d_inst, b->d_work, b->d_nwork, b->d_step, b->d_ctr);
+        launch_counter() += 1;
     }
     BTRY(b, cudaGetLastError());
     return BCLBM_OK;
@@ -313,8 +320,7 @@ int ensure_graph(bclbm_batch* b) {
     cudaGraph_t g = nullptr;
     BTRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < b->graph_steps; ++k) {
-        b->step_kernel<<<b->grid, kBlock, 0, b->stream>>>(b->d_inst, b->d_work, b->d_nwork, b->d_step, b->d_next);
-        k_batch_tick<<<1, 32, 0, b->stream>>>(b->d_step, b->d_next);
+        b->step_kernel<<<b->grid, kBlock, 0, b->stream>>>(b->d_inst, b->d_work, b->d_nwork, b->d_step, b->d_ctr);
     }
     const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
     if (ec != cudaSuccess) return bfail(b, BCLBM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
@@ -377,7 +383,7 @@ int bclbm_batch_create(int32_t lattice_q, int32_t collision, int32_t precision, 
     if (cudaMalloc(&b->d_inst, sizeof(BatchInst) * max_instances) != cudaSuccess ||
         cudaMalloc(&b->d_work, sizeof(int2) * b->max_work) != cudaSuccess ||
         cudaMalloc(&b->d_nwork, sizeof(int)) != cudaSuccess || cudaMalloc(&b->d_step, sizeof(long long)) != cudaSuccess ||
-        cudaMalloc(&b->d_next, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&b->d_ctr, 2 * sizeof(int)) != cudaSuccess ||
         cudaMalloc(&b->d_partials, sizeof(double) * 6 * static_cast<size_t>(b->max_work)) != cudaSuccess ||
         cudaMalloc(&b->d_first, sizeof(int) * max_instances) != cudaSuccess ||
         cudaMalloc(&b->d_count, sizeof(int) * max_instances) != cudaSuccess ||
@@ -386,7 +392,7 @@ int bclbm_batch_create(int32_t lattice_q, int32_t collision, int32_t precision, 
     const int zero = 0;
     const long long zstep = 0;
     if (cudaMemcpyAsync(b->d_nwork, &zero, sizeof(int), cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
-        cudaMemcpyAsync(b->d_next, &zero, sizeof(int), cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
+        cudaMemsetAsync(b->d_ctr, 0, 2 * sizeof(int), b->stream) != cudaSuccess ||
         cudaMemcpyAsync(b->d_step, &zstep, sizeof(long long), cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
         cudaStreamSynchronize(b->stream) != cudaSuccess)
         return cleanup(BCLBM_ERR_CUDA);
@@ -486,7 +492,7 @@ int bclbm_batch_step(bclbm_batch* b, int32_t nsteps) {
         if (rc) return rc;
         while (left >= b->graph_steps) {
             BTRY(b, cudaGraphLaunch(b->graph, b->stream));
-            launch_counter() += 2 * b->graph_steps;
+            launch_counter() += b->graph_steps;
             left -= b->graph_steps;
         }
     }

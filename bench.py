@@ -18,6 +18,13 @@ roofline      algorithmic bytes per launch (fluid nodes x bytes per update) over
               the average step-kernel duration, against MEASURED_PEAKS.json
 cpu_baseline  the oracle (plain-C restatement of the reference step) on the
               host cores, a bounded sample of steps of the same workload
+serving       (rank 0) a sample of the serving workload: --requests permeability
+              requests from the serving distribution, served by the batched
+              server and by sequential single-instance FP64 solves: solves/s,
+              p50/p99 latency, permeability error against FP64
+
+  python bench.py --workload serving [--requests R --rates 0,2,5]
+  prints the serving measurement as the bench line (solves/s).
 """
 
 from __future__ import annotations
@@ -312,6 +319,13 @@ def run_mine(args, world, rank):
                     "definition": "k = nu * sum_fluid(rho u_x) / (V F_x), FP64 reductions on the GPU",
                     "rel_err_vs_f64": {p: abs(ks[p] - ks["f64"]) / abs(ks["f64"]) for p in ("f32", "f16", "bf16")}}
 
+    # ---- serving: continuous batching against sequential FP64 solves -------------
+    serving = None
+    if rank == 0 and not args.no_serving:
+        serving = serving_measure(args, bclbm)
+        for k in ("_head", "_prepared", "_reqs"):
+            serving.pop(k)
+
     # ---- end to end through the C ABI with host buffers -------------------------
     torch.cuda.synchronize()
     barrier(world)
@@ -370,33 +384,28 @@ def run_mine(args, world, rank):
             "launches_total": bclbm.native.launch_count() - launches0,
             "variants": variants,
             "accuracy": accuracy,
+            "serving": serving,
             "check": {"mass": st["mass"][0], "flux_x": st["momentum"][0], "nonfinite": st["nonfinite"]},
         }
         print(json.dumps(line), flush=True)
 
 
-def run_serving(args, world, rank):
-    """--workload serving: continuous batching of permeability requests against
-    sequential single-instance solves of the same requests."""
+def serving_measure(args, bclbm):
+    """Continuous batching of permeability requests against sequential
+    single-instance FP64 solves of the same requests (rank 0, one GPU)."""
     import torch
-    import __graft_entry__ as ge
-    bclbm = ge.load()
+    import concurrent.futures as cf
     S = bclbm.serving
-    if rank != 0:
-        return
     reqs = S.sample_requests(args.requests, rate=0.0, seed=args.seed, size_range=(args.size_min, args.size_max),
                              gx=args.gx)
     t = time.time()
     prepared = {}
-    import concurrent.futures as cf
     with cf.ThreadPoolExecutor(max_workers=8) as pool:
         for r, res in zip(reqs, pool.map(S.prepare, reqs)):
             prepared[r.rid] = res
     log(f"prepared {len(reqs)} requests in {time.time() - t:.1f}s; sides {sorted(r.size for r in reqs)}")
     srv = S.Server(precision=args.serving_precision, check_every=args.check_every, tol=args.tol,
                    max_steps=args.max_steps, steps_per_graph=args.steps_per_graph, promote_tol=args.promote_tol)
-    peak, peak_kind = peaks()
-    gpu_index = 0
     # warm-up: one small request through both paths (graph capture, module load)
     warm = S.sample_requests(1, rate=0.0, seed=1, size_range=(24, 24))
     S.Server(precision=args.serving_precision, check_every=50, max_steps=101).run(warm)
@@ -405,13 +414,12 @@ def run_serving(args, world, rank):
     out = {}
     rates = [float(x) for x in args.rates.split(",")]
     l0 = bclbm.native.launch_count()
-    with ClockSampler(gpu_index) as clk:
+    with ClockSampler(0) as clk:
         base = srv.run_sequential(reqs, precision=args.baseline_precision, prepared=prepared)
         for rate in rates:
             sched = S.sample_requests(args.requests, rate=rate, seed=args.seed,
                                       size_range=(args.size_min, args.size_max), gx=args.gx)
-            rep = srv.run(sched, prepared=prepared)
-            out[rate] = rep
+            out[rate] = srv.run(sched, prepared=prepared)
     launches = bclbm.native.launch_count() - l0
     head = out[rates[0]]
     kb = {r.rid: r.permeability for r in base["results"]}
@@ -421,41 +429,56 @@ def run_serving(args, world, rank):
         return {k: rep[k] for k in ("solves", "seconds", "solves_per_s", "p50_s", "p99_s", "converged",
                                     "lattice_updates")} | {"mlups": rep["lattice_updates"] / rep["seconds"] / 1e6}
 
-    line = {
-        "metric": METRIC, "value": head["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
-        "steps": args.requests, "warmup": 1, "ms_per_step": head["seconds"] / max(1, head["solves"]) * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.serving_precision,
-        "data": "synthetic: seeded periodic sphere packs (numpy default_rng), no dataset",
-        "config": {"workload": f"serving: {args.requests} D3Q19 BGK permeability requests, side log-uniform "
-                               f"[{args.size_min},{args.size_max}], radius U[4,12], porosity U[0.30,0.50], "
-                               f"tau U[0.6,1.2], gx {args.gx:g}; until |dk/k| < {args.tol:g} over "
-                               f"{args.check_every} steps or {args.max_steps} steps",
-                   "arrivals": f"Poisson, rates {rates} /s (0 = all at t=0)",
-                   "host_preparation": "geometry and node tables built before the timed region for both arms",
-                   "l2": "instances of up to several GB against 129 MB L2"},
+    workload = (f"serving: {args.requests} D3Q19 BGK permeability requests, side log-uniform "
+                f"[{args.size_min},{args.size_max}], radius U[4,12], porosity U[0.30,0.50], tau U[0.6,1.2], "
+                f"gx {args.gx:g}; until |dk/k| < {args.tol:g} over {args.check_every} steps or {args.max_steps} steps")
+    return {
+        "workload": workload, "precision": args.serving_precision, "rates": rates,
+        "arrivals": f"Poisson, rates {rates} /s (0 = all at t=0)",
+        "host_preparation": "geometry and node tables built before the timed region for both arms",
+        "solves_per_s": head["solves_per_s"], "p50_s": head["p50_s"], "p99_s": head["p99_s"],
         "serving": {str(r): brief(out[r]) | {"counters": out[r]["counters"]} for r in rates},
+        "sequential_baseline": brief(base) | {"precision": args.baseline_precision},
+        "speedup_solves_per_s": head["solves_per_s"] / base["solves_per_s"],
+        "accuracy": {"max_rel_perm_err_vs_baseline": max(errs) if errs else None,
+                     "median_rel_perm_err_vs_baseline": float(np.median(errs)) if errs else None},
         "requests": [{"rid": q.rid, "side": q.size, "tau": round(q.tau, 4), "radius": round(q.radius, 3),
                       "porosity": round(q.porosity, 4), "fluid": a.n_fluid, "steps": a.steps,
                       "steps_baseline": c.steps, "latency_s": round(a.latency, 4),
                       "latency_baseline_s": round(c.latency, 4), "k": a.permeability, "k_baseline": c.permeability}
                      for q, a, c in zip(reqs, head["results"], base["results"])],
-        "sequential_baseline": brief(base) | {"precision": args.baseline_precision},
-        "speedup_solves_per_s": head["solves_per_s"] / base["solves_per_s"],
-        "accuracy": {"max_rel_perm_err_vs_baseline": max(errs) if errs else None,
-                     "median_rel_perm_err_vs_baseline": float(np.median(errs)) if errs else None},
-        "clocks": clk.summary(), "gpu_launches": launches,
-        "e2e": {"value": head["solves_per_s"], "unit": "solves/s",
+        "clocks": clk.summary(), "gpu_launches": launches, "_head": head, "_prepared": prepared, "_reqs": reqs,
+    }
+
+
+def run_serving(args, world, rank):
+    """--workload serving: the serving measurement as the bench line."""
+    import __graft_entry__ as ge
+    bclbm = ge.load()
+    if rank != 0:
+        return
+    m = serving_measure(args, bclbm)
+    head, prepared, reqs = m.pop("_head"), m.pop("_prepared"), m.pop("_reqs")
+    peak, peak_kind = peaks()
+    achieved = head["lattice_updates"] / head["seconds"] * BYTES_PER_UPDATE[args.serving_precision.split(">")[-1]] / 1e9
+    line = {
+        "metric": METRIC, "value": m["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+        "steps": args.requests, "warmup": 1, "ms_per_step": head["seconds"] / max(1, head["solves"]) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.serving_precision,
+        "data": "synthetic: seeded periodic sphere packs (numpy default_rng), no dataset",
+        "config": {"workload": m["workload"], "arrivals": m["arrivals"], "host_preparation": m["host_preparation"],
+                   "l2": "instances of up to several GB against 129 MB L2"},
+        "clocks": m.pop("clocks"), "gpu_launches": m.pop("gpu_launches"),
+        "e2e": {"value": m["solves_per_s"], "unit": "solves/s",
                 "h2d_bytes_per_step": float(np.mean([prepared[r.rid][1].nbytes + prepared[r.rid][0].neigh.nbytes
                                                      + prepared[r.rid][0].types.nbytes for r in reqs])),
                 "d2h_bytes_per_step": 96.0 * args.max_steps / args.check_every,
-                "path": "per request: bclbm_batch_admit from host arrays, batched steps, bclbm_batch_stats every "
-                        "check block, bclbm_batch_retire"},
-        "roofline": {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_kind": peak_kind,
-                     "achieved": head["lattice_updates"] / head["seconds"]
-                     * BYTES_PER_UPDATE[args.serving_precision.split(">")[0]] / 1e9, "traffic": None,
+                "path": "per request: bclbm_create + first step on a host thread, bclbm_batch_attach, batched "
+                        "steps, bclbm_batch_stats every check block, bclbm_batch_retire"},
+        "roofline": {"bound": "hbm", "peak": peak, "unit": "GB/s", "peak_kind": peak_kind, "achieved": achieved,
+                     "frac": achieved / peak, "traffic": None,
                      "note": "algorithmic bytes of all lattice updates over the whole serving run (wall clock)"},
-    }
-    line["roofline"]["frac"] = line["roofline"]["achieved"] / peak
+    } | m
     print(json.dumps(line), flush=True)
 
 
@@ -481,6 +504,7 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=10000,
                     help="steps of the FP64 / FP32 / FP16 / BF16 permeability comparison (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving sample of the pack workload line")
     ap.add_argument("--workload", default="pack", choices=["pack", "serving"],
                     help="pack: the 256^3 sphere-pack time step; serving: the request loop")
     ap.add_argument("--requests", type=int, default=24)
