@@ -180,6 +180,12 @@ def allreduce_max(world, x: float) -> float:
     return float(t.item())
 
 
+def whole_job_mlups(world: int, units_per_rank: int, steps: int, max_seconds: float) -> float:
+    """Replicas: every rank updates units_per_rank nodes per step; the job took the
+    slowest rank's time (max over ranks)."""
+    return world * units_per_rank * steps / max_seconds / 1e6
+
+
 def cpu_port_rate(lat, steps_target_s: float, nthreads: int, tau: float, force, max_steps: int = 1000):
     """Oracle MLUPS on the host cores for a bounded number of steps."""
     sys.path.insert(0, str(REPO / "oracle"))
@@ -276,7 +282,7 @@ def run_mine(args, world, rank):
         st = s.reduce()
     total_ms = allreduce_max(world, tm["total_ms"])
     kernel_ms = tm["step_kernel_ms"] / args.steps
-    mlups = world * lat.n_bulk * args.steps / (total_ms * 1e-3) / 1e6
+    mlups = whole_job_mlups(world, lat.n_bulk, args.steps, total_ms * 1e-3)
     bpu = BYTES_PER_UPDATE[hp]
     achieved = lat.n_bulk * bpu / (kernel_ms * 1e-3) / 1e9
     arith = "exact" if args.exact else ("fma" if args.fma64 else ("fixed" if hp == "f64" else "fp32"))
@@ -346,7 +352,7 @@ def run_mine(args, world, rank):
         rho, vel, _ = s.download_macros()
     e2e_s = time.perf_counter() - t
     e2e_s = allreduce_max(world, e2e_s)
-    e2e_mlups = world * lat.n_bulk * args.steps / e2e_s / 1e6
+    e2e_mlups = whole_job_mlups(world, lat.n_bulk, args.steps, e2e_s)
     h2d = lat.neigh.nbytes + lat.types.nbytes + lat.bulk.nbytes + f0.nbytes
     d2h = nred * 96 + lat.n_bulk * 19 * 8 + lat.n_bulk * (1 + 3) * 8
 

@@ -1,0 +1,219 @@
+/*
+ * bclbm_lbsolver.hpp: C++ adaptor between the reference's lbsolver objects and
+ * the C ABI of bclbm.h.  Header only; include it after the reference's
+ * LBSOLVER.h (it names Grid, Nodes, LbField, ScalarField and VectorField).
+ *
+ * The reference has no plugin interface: its main files run the per-node loops
+ * themselves.  The adaptor replaces, in those loops, everything between the
+ * start of an iteration and the output step with one call:
+ *
+ *   src/std_case/main.cpp:109-146
+ *     for (int i = 0; i <= nIterations; i++) {
+ *         step.run(1);                        // node loop, swapData, communicate, bounce-back
+ *         if ((i % nItrWrite) == 0) {
+ *             step.download_macros(rho, vel);  // what the node loop stored in rho / vel
+ *             output.write(i);
+ *         }
+ *     }
+ *   with   bclbm::LbStep<LT> step(grid, nodes, bulkNodes, f,
+ *                                 bclbm::SinglePhase{tau, {Fx, Fy, Fz}});
+ *
+ *   src/twophase/main_TWOPHASE.cpp:236-393 likewise, with
+ *          bclbm::LbStep<LT> step(grid, nodes, bulkNodes, f, rho,
+ *                                 bclbm::TwoPhase{tau0, tau1, sigma, beta, {Fx, Fy, Fz}});
+ *   and step.download_macros(rho, vel, cgField) before output.write(i).
+ *
+ * The tables are read through the reference's accessors (Grid::neighbor,
+ * Grid::pos, Nodes::getType: src/lbsolver/LBgrid.h:97-112, LBnodes.h:72) and the
+ * fields through their element references (LBfield.h:59, 170, 298), once, at
+ * construction.  The device keeps its own copies; downloads write back in the
+ * reference's layout and numbering.
+ *
+ * Errors follow the reference's convention (print and exit(1), as in
+ * src/lbsolver/LBvtk.h:230-233); define BCLBM_ADAPTOR_THROW before including this
+ * header to get a std::runtime_error instead.
+ */
+#ifndef BCLBM_LBSOLVER_HPP
+#define BCLBM_LBSOLVER_HPP
+
+#include <array>
+#include <cstdint>
+#include <cstdlib>
+#include <iostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "bclbm.h"
+
+namespace bclbm {
+
+/* std_case: BGK (tau_anti = 0) or TRT with the antisymmetric time tau_anti;
+ * force = bodyForce(0, 0) of the main file. */
+struct SinglePhase {
+    double tau;
+    std::array<double, 3> force;
+    double tau_anti = 0.0;
+    int32_t precision = BCLBM_F64;
+    uint32_t flags = 0;
+    double store_scale = 0.0;
+};
+
+/* twophase: fluid.tau[0], fluid.tau[1], fluid.sigma, fluid.beta and the body
+ * force; flux_control = 1 keeps the flux controller of main_TWOPHASE.cpp:292-308
+ * with target mom_x. */
+struct TwoPhase {
+    double tau0, tau1, sigma, beta;
+    std::array<double, 3> force;
+    int32_t flux_control = 0;
+    double mom_x = 0.0;
+    int32_t precision = BCLBM_F64;
+    uint32_t flags = 0;
+    double store_scale = 0.0;
+};
+
+[[noreturn]] inline void adaptor_fail(const std::string& what) {
+#ifdef BCLBM_ADAPTOR_THROW
+    throw std::runtime_error(what);
+#else
+    std::cout << what << std::endl;
+    std::exit(1);
+#endif
+}
+
+inline void adaptor_check(int rc, const bclbm_handle* h, const char* call) {
+    if (rc == BCLBM_OK) return;
+    std::string msg = std::string("bclbm: ") + call + " failed: " + bclbm_error(rc);
+    if (h) {
+        const std::string detail = bclbm_last_error(h);
+        if (!detail.empty()) msg += " (" + detail + ")";
+    }
+    adaptor_fail(msg);
+}
+
+/* The reference's Grid/Nodes arrays in the layout bclbm_desc takes. */
+template <typename DXQY>
+struct LbTables {
+    std::vector<int32_t> neigh;  // [N*Q]
+    std::vector<int16_t> types;  // [N]
+    std::vector<int32_t> pos;    // [N*nD]
+    std::vector<int32_t> bulk;   // [n_bulk]
+
+    template <class GridT, class NodesT>
+    LbTables(const GridT& grid, const NodesT& nodes, const std::vector<int>& bulkNodes) {
+        const int N = grid.size();
+        neigh.resize(static_cast<size_t>(N) * DXQY::nQ);
+        types.resize(static_cast<size_t>(N));
+        for (int n = 0; n < N; ++n) {
+            for (int q = 0; q < DXQY::nQ; ++q) neigh[static_cast<size_t>(n) * DXQY::nQ + q] = grid.neighbor(q, n);
+            types[static_cast<size_t>(n)] = static_cast<int16_t>(nodes.getType(n));
+        }
+        const std::vector<int>& p = grid.pos();
+        pos.assign(p.begin(), p.end());
+        bulk.assign(bulkNodes.begin(), bulkNodes.end());
+    }
+};
+
+template <typename DXQY>
+class LbStep {
+public:
+    /* std_case */
+    template <class GridT, class NodesT>
+    LbStep(const GridT& grid, const NodesT& nodes, const std::vector<int>& bulkNodes, const LbField<DXQY>& f,
+           const SinglePhase& p)
+        : tab_(grid, nodes, bulkNodes), nfields_(1) {
+        if (f.num_fields() != 1) adaptor_fail("bclbm: the std_case LbField has one field");
+        bclbm_desc d = base_desc(grid.size());
+        d.collision = p.tau_anti > 0.0 ? BCLBM_TRT : BCLBM_BGK;
+        d.precision = p.precision;
+        d.flags = p.flags;
+        d.tau[0] = p.tau;
+        d.tau[1] = p.tau_anti > 0.0 ? p.tau_anti : p.tau;
+        for (int k = 0; k < 3; ++k) d.force[k] = p.force[k];
+        d.store_scale = p.store_scale;
+        d.f_init = &f(0, 0, 0);
+        create(d);
+    }
+
+    /* twophase: rho holds the two phase densities (ScalarField(2, N)); only the
+     * solid boundary entries (the wettability densities) are read */
+    template <class GridT, class NodesT>
+    LbStep(const GridT& grid, const NodesT& nodes, const std::vector<int>& bulkNodes, const LbField<DXQY>& f,
+           const ScalarField& rho, const TwoPhase& p)
+        : tab_(grid, nodes, bulkNodes), nfields_(2) {
+        if (f.num_fields() != 2 || rho.num_fields() != 2)
+            adaptor_fail("bclbm: the twophase LbField and ScalarField have two fields");
+        bclbm_desc d = base_desc(grid.size());
+        d.collision = BCLBM_RK;
+        d.precision = p.precision;
+        d.flags = p.flags;
+        d.tau[0] = p.tau0;
+        d.tau[1] = p.tau1;
+        d.sigma = p.sigma;
+        d.beta = p.beta;
+        d.flux_control = p.flux_control;
+        d.mom_x = p.mom_x;
+        for (int k = 0; k < 3; ++k) d.force[k] = p.force[k];
+        d.store_scale = p.store_scale;
+        d.f_init = &f(0, 0, 0);
+        d.rho_init = &rho(0, 0);
+        create(d);
+    }
+
+    LbStep(const LbStep&) = delete;
+    LbStep& operator=(const LbStep&) = delete;
+    ~LbStep() { bclbm_destroy(h_); }
+
+    /* nsteps iterations of the main-file loop body (asynchronous) */
+    void run(int nsteps) { adaptor_check(bclbm_step(h_, nsteps), h_, "bclbm_step"); }
+
+    /* f after the last iteration (the bulk rows of the reference's LbField) */
+    void download(LbField<DXQY>& f) const { adaptor_check(bclbm_download_f(h_, &f(0, 0, 0)), h_, "bclbm_download_f"); }
+
+    /* rho / vel as the last iteration's node loop stored them */
+    void download_macros(ScalarField& rho, VectorField<DXQY>& vel) const {
+        adaptor_check(bclbm_download_macros(h_, &rho(0, 0), &vel(0, 0, 0), nullptr), h_, "bclbm_download_macros");
+    }
+    /* twophase: also the colour field cgField */
+    void download_macros(ScalarField& rho, VectorField<DXQY>& vel, ScalarField& cg) const {
+        adaptor_check(bclbm_download_macros(h_, &rho(0, 0), &vel(0, 0, 0), &cg(0, 0)), h_, "bclbm_download_macros");
+    }
+
+    /* FP64 sums: mass per field, momentum, flux-controller sum, saturation */
+    bclbm_stats stats() const {
+        bclbm_stats s;
+        adaptor_check(bclbm_reduce(h_, &s), h_, "bclbm_reduce");
+        return s;
+    }
+
+    void set_force(const std::array<double, 3>& F) {
+        adaptor_check(bclbm_set_force(h_, F.data()), h_, "bclbm_set_force");
+    }
+
+    bclbm_handle* handle() const { return h_; }
+    const LbTables<DXQY>& tables() const { return tab_; }
+
+private:
+    bclbm_desc base_desc(int n_nodes) const {
+        bclbm_desc d{};
+        d.lattice_q = DXQY::nQ;
+        d.n_nodes = n_nodes;
+        d.neigh = tab_.neigh.data();
+        d.types = tab_.types.data();
+        d.n_bulk = static_cast<int32_t>(tab_.bulk.size());
+        d.bulk = tab_.bulk.data();
+        d.pos = tab_.pos.data();
+        d.rho_ref = 1.0;
+        return d;
+    }
+
+    void create(const bclbm_desc& d) { adaptor_check(bclbm_create(&d, &h_), nullptr, "bclbm_create"); }
+
+    LbTables<DXQY> tab_;
+    int nfields_;
+    bclbm_handle* h_ = nullptr;
+};
+
+}  // namespace bclbm
+
+#endif

@@ -1,0 +1,63 @@
+// Compile-and-run check of include/bclbm_lbsolver.hpp against the reference's
+// own lbsolver objects (built by tests/test_adaptor.py with the reference
+// headers and the single-rank mpi.h stub of oracle/mpi_stub; test only).
+//
+//   adaptor_check <vtklb> <outdir>
+// reads the .vtklb file into the reference's LBvtk / Grid / Nodes, writes the
+// adaptor's tables (neigh.i32, types.i16, pos.i32, bulk.i32) into outdir, then
+// builds an LbStep from them and runs 3 steps; prints "status <text>" with the
+// adaptor's error message, or "ran <sum of f>" when a GPU ran the steps.
+#include "LBSOLVER.h"
+
+#define BCLBM_ADAPTOR_THROW
+#include "bclbm_lbsolver.hpp"
+
+#include <cstdio>
+#include <fstream>
+#include <string>
+
+#ifndef BCLBM_LT
+#define BCLBM_LT D3Q19
+#endif
+#define LT BCLBM_LT
+
+template <typename T>
+static void dump(const std::string& path, const std::vector<T>& v) {
+    std::ofstream ofs(path, std::ios::binary);
+    ofs.write(reinterpret_cast<const char*>(v.data()), static_cast<std::streamsize>(v.size() * sizeof(T)));
+}
+
+int main(int argc, char** argv) {
+    if (argc < 3) return 2;
+    MPI_Init(NULL, NULL);
+    LBvtk<LT> vtklb(argv[1]);
+    Grid<LT> grid(vtklb);
+    Nodes<LT> nodes(vtklb, grid);
+    BndMpi<LT> mpiBoundary(vtklb, nodes, grid);
+    std::vector<int> bulkNodes = findBulkNodes(nodes);
+    const std::string out(argv[2]);
+    bclbm::LbTables<LT> tab(grid, nodes, bulkNodes);
+    dump(out + "/neigh.i32", tab.neigh);
+    dump(out + "/types.i16", tab.types);
+    dump(out + "/pos.i32", tab.pos);
+    dump(out + "/bulk.i32", tab.bulk);
+    LbField<LT> f(1, grid.size());
+    for (auto n : bulkNodes)
+        for (int q = 0; q < LT::nQ; ++q) f(0, q, n) = LT::w[q] * 1.0;
+    try {
+        bclbm::LbStep<LT> step(grid, nodes, bulkNodes, f, bclbm::SinglePhase{0.8, {1e-5, 0.0, 0.0}});
+        step.run(3);
+        step.download(f);
+        ScalarField rho(1, grid.size());
+        VectorField<LT> vel(1, grid.size());
+        step.download_macros(rho, vel);
+        double s = 0.0;
+        for (auto n : bulkNodes)
+            for (int q = 0; q < LT::nQ; ++q) s += f(0, q, n);
+        std::printf("ran %.17g\n", s);
+    } catch (const std::runtime_error& e) {
+        std::printf("status %s\n", e.what());
+    }
+    MPI_Finalize();
+    return 0;
+}
