@@ -446,6 +446,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     h->trt = d->collision == BCLBM_TRT;
     h->fma64 = (d->flags & BCLBM_FLAG_FP64_FMA) != 0;
     h->flux = d->collision == BCLBM_RK && d->flux_control != 0;
+    h->mass_fix = d->collision == BCLBM_RK && d->precision != BCLBM_F64 && !(d->flags & BCLBM_FLAG_NO_MASS_FIX);
     h->n_nodes = d->n_nodes;
     h->footprint = footprint_bytes(d, p);
     h->nf = p.nf;
@@ -564,6 +565,26 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         prm.force[k] = h->force[k];
         prm.forcef[k] = static_cast<float>(h->force[k]);
     }
+    if (h->mass_fix) {
+        // the conserved totals of the uploaded state, sum over bulk nodes of
+        // sum_q (f0 + f1) and sum_q (f0 - f1), in FP64 (fixed order per chunk)
+        const size_t nb = static_cast<size_t>(d->n_bulk), Qs = static_cast<size_t>(h->q);
+        std::vector<double> pt(64, 0.0), pc(64, 0.0);
+        parallel_for(64, [&](size_t c0, size_t c1) {
+            for (size_t c = c0; c < c1; ++c)
+                for (size_t b = nb * c / 64; b < nb * (c + 1) / 64; ++b) {
+                    const double* fb = d->f_init + static_cast<size_t>(d->bulk[b]) * 2 * Qs;
+                    for (size_t q = 0; q < Qs; ++q) {
+                        pt[c] += fb[q] + fb[Qs + q];
+                        pc[c] += fb[q] - fb[Qs + q];
+                    }
+                }
+        }, 1);
+        for (int c = 0; c < 64; ++c) {
+            prm.mass_target[0] += pt[c];
+            prm.mass_target[1] += pc[c];
+        }
+    }
     CREATE_TRY(cudaMemcpyAsync(h->d_params, &prm, sizeof(prm), cudaMemcpyHostToDevice, h->stream));
 
     // colour field: fluid slots (written every step), stored solids (fixed), ghost (0)
@@ -656,12 +677,13 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
             StepArgs ad = a;
             ad.rho_out = nullptr;
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 0], h->stream));
-            if (h->precision == BCLBM_F64) CUDA_TRY(h, launch_rk_f64(h->q, local, h->flux, ad, h->stream, true));
-            else CUDA_TRY(h, launch_rk_shift(h->q, h->precision, local, h->flux, ad, h->stream, true));
-            if (h->flux) {
-                CUDA_TRY(h, launch_reduce_final(1, h->d_partials, grid_for(h->nf), h->d_red, false, h->stream));
-                CUDA_TRY(h, launch_flux_force(h->d_red, 1.0 / static_cast<double>(h->nf), h->mom_x, h->d_params,
-                                              h->stream));
+            const bool sums = h->flux || h->mass_fix;
+            if (h->precision == BCLBM_F64) CUDA_TRY(h, launch_rk_f64(h->q, local, sums, ad, h->stream, true));
+            else CUDA_TRY(h, launch_rk_shift(h->q, h->precision, local, sums, ad, h->stream, true));
+            if (sums) {
+                CUDA_TRY(h, launch_reduce_final(3, h->d_partials, grid_for(h->nf), h->d_red, false, h->stream));
+                CUDA_TRY(h, launch_rk_fix(h->d_red, static_cast<double>(h->nf), h->rho_ref, h->mom_x, h->flux,
+                                          h->mass_fix, h->d_params, h->stream));
             }
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 1], h->stream));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));

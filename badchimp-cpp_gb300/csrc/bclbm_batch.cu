@@ -154,27 +154,13 @@ __global__ void __launch_bounds__(kBlock) k_batch_moments(const BatchInst* __res
     }
 }
 
-// one block per requested instance: its work items' partials in work order
-__global__ void __launch_bounds__(kBlock) k_batch_final(const double* __restrict__ partials,
-                                                        const int* __restrict__ first, const int* __restrict__ count,
-                                                        double* out) {
-    __shared__ double sh[kBlock][6];
+// one block per requested instance: its work items' partials, summed exactly as
+// bclbm_reduce sums a handle's block partials (final_sum)
+__global__ void __launch_bounds__(kFinalThreads) k_batch_final(const double* __restrict__ partials,
+                                                              const int* __restrict__ first,
+                                                              const int* __restrict__ count, double* out) {
     const int j = blockIdx.x;
-    const int w0 = first[j], nw = count[j];
-    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int b = threadIdx.x; b < nw; b += kBlock)
-        for (int k = 0; k < 6; ++k) {
-            const double v = partials[static_cast<size_t>(w0 + b) * 6 + k];
-            acc[k] = k == 5 ? fmax(acc[k], v) : acc[k] + v;
-        }
-    for (int k = 0; k < 6; ++k) sh[threadIdx.x][k] = acc[k];
-    __syncthreads();
-    if (threadIdx.x == 0)
-        for (int k = 0; k < 6; ++k) {
-            double s = sh[0][k];
-            for (int t = 1; t < kBlock; ++t) s = k == 5 ? fmax(s, sh[t][k]) : s + sh[t][k];
-            out[static_cast<size_t>(j) * 6 + k] = s;
-        }
+    final_sum<6>(partials + static_cast<size_t>(first[j]) * 6, count[j], out + static_cast<size_t>(j) * 6, true);
 }
 
 using StepKernel = void (*)(const BatchInst*, const int2*, const int*, long long*, int*);
@@ -517,7 +503,7 @@ int bclbm_batch_stats(bclbm_batch* b, int32_t n, const int32_t* ids, bclbm_stats
     launch_counter()++;
     BTRY(b, cudaMemcpyAsync(b->d_first, first.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
     BTRY(b, cudaMemcpyAsync(b->d_count, count.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
-    k_batch_final<<<n, kBlock, 0, b->stream>>>(b->d_partials, b->d_first, b->d_count, b->d_out);
+    k_batch_final<<<n, kFinalThreads, 0, b->stream>>>(b->d_partials, b->d_first, b->d_count, b->d_out);
     launch_counter()++;
     BTRY(b, cudaGetLastError());
     std::vector<double> res(static_cast<size_t>(n) * 6);

@@ -15,6 +15,7 @@ struct bclbm_handle {
     int q = 0, nd = 0, nfields = 1, collision = 0, precision = 0;
     uint32_t flags = 0;
     bool exact = false, trt = false, flux = false, fma64 = false;
+    bool mass_fix = false;  // two-phase shifted storage: per-step mass-drift correction
     int n_nodes = 0, nf = 0, nf_pad = 0, ns = 0;
     double tau[2] = {1.0, 1.0};
     double sigma = 0.0, beta = 0.0, mom_x = 0.0, rho_ref = 1.0, scale = 1.0;

@@ -18,6 +18,25 @@ __global__ void k_flux_force(const double* sum, double inv_n, double mom_x, DevP
     }
 }
 
+__global__ void k_rk_fix(const double* sum, double n, double rho_ref, double mom_x, int flux, int fix,
+                         DevParams* params) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        if (flux) {
+            params->force[0] = 2 * (mom_x - sum[0] / n);
+            params->forcef[0] = static_cast<float>(params->force[0]);
+        }
+        if (fix) {
+            // totals now: n rho_ref + sum[1] and sum[2]; the deficit spread over the nodes
+            const double dt = (params->mass_target[0] - (n * rho_ref + sum[1])) / n;
+            const double dc = (params->mass_target[1] - sum[2]) / n;
+            params->mass_fix[0] = dt;
+            params->mass_fix[1] = dc;
+            params->mass_fixf[0] = static_cast<float>(dt);
+            params->mass_fixf[1] = static_cast<float>(dc);
+        }
+    }
+}
+
 namespace {
 
 template <int Q, class S>
@@ -158,6 +177,13 @@ cudaError_t launch_flux_force(const double* sum, double inv_n, double mom_x, Dev
     return cudaGetLastError();
 }
 
+cudaError_t launch_rk_fix(const double* sum, double n, double rho_ref, double mom_x, bool flux, bool fix,
+                          DevParams* params, cudaStream_t s) {
+    k_rk_fix<<<1, 32, 0, s>>>(sum, n, rho_ref, mom_x, flux ? 1 : 0, fix ? 1 : 0, params);
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_gather(int Q, int precision, int nfields, bool local, const StepArgs& a, const int32_t* slot_bulk,
                           double* out, cudaStream_t s) {
     return Q == 9 ? gather_q<9>(precision, nfields, local, a, slot_bulk, out, s)
@@ -170,8 +196,9 @@ cudaError_t launch_moments(int Q, int precision, int nfields, bool local, const 
 
 cudaError_t launch_reduce_final(int nv, const double* partials, int nblocks, double* out, bool max_last,
                                 cudaStream_t s) {
-    if (nv == 1) k_reduce_final<1><<<1, kBlock, 0, s>>>(partials, nblocks, out, max_last ? 1 : 0);
-    else if (nv == 6) k_reduce_final<6><<<1, kBlock, 0, s>>>(partials, nblocks, out, max_last ? 1 : 0);
+    if (nv == 1) k_reduce_final<1><<<1, kFinalThreads, 0, s>>>(partials, nblocks, out, max_last ? 1 : 0);
+    else if (nv == 3) k_reduce_final<3><<<1, kFinalThreads, 0, s>>>(partials, nblocks, out, max_last ? 1 : 0);
+    else if (nv == 6) k_reduce_final<6><<<1, kFinalThreads, 0, s>>>(partials, nblocks, out, max_last ? 1 : 0);
     else return cudaErrorInvalidValue;
     launch_counter()++;
     return cudaGetLastError();

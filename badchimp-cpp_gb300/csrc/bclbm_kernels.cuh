@@ -28,6 +28,12 @@ struct DevParams {
     double force[3];
     float forcef[3];  // the same force rounded to FP32, for the FP32-arithmetic kernels
     int fx_overflow;  // set by the fixed-point kernel when a value left its range
+    // two-phase shifted storage: the conserved totals sum f0 + f1 and sum f0 - f1
+    // (set at create) and the uniform per-node correction the collision adds this
+    // step to put the totals back (mass-drift correction)
+    double mass_target[2];
+    double mass_fix[2];
+    float mass_fixf[2];
 };
 
 struct StepArgs {
@@ -432,32 +438,78 @@ __device__ __forceinline__ void block_reduce_store(double* vals, double* partial
     }
 }
 
-// Sums nblocks rows of NV partials in block order with one block; result to out[NV].
+// The same tree in FP32 (for the per-step sums of the FP32-arithmetic two-phase
+// kernels, where FP64 shuffle trees would cost more than the pass itself; the
+// block sums go on in FP64).  Deterministic.
 template <int NV>
-__global__ void __launch_bounds__(kBlock) k_reduce_final(const double* __restrict__ partials, int nblocks,
-                                                        double* out, int max_last) {
-    __shared__ double sh[kBlock][NV];
+__device__ __forceinline__ void block_reduce_store_f32(float* vals, double* partials) {
+    __shared__ float shf[kBlock / 32][NV];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        float v = vals[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) shf[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            float s = shf[0][k];
+            for (int w = 1; w < kBlock / 32; ++w) s += shf[w][k];
+            partials[static_cast<size_t>(blockIdx.x) * NV + k] = static_cast<double>(s);
+        }
+    }
+}
+
+// Final sum of nrows rows of NV partials by one block of kFinalThreads threads,
+// in a fixed order: thread t takes rows t, t + kFinalThreads, ... (loads issued
+// four at a time, added in row order), then a fixed pairwise tree over the
+// threads.  With max_last the last value is a max instead of a sum.
+constexpr int kFinalThreads = 512;
+
+template <int NV>
+__device__ __forceinline__ void final_sum(const double* __restrict__ p, int nrows, double* out, bool max_last) {
+    __shared__ double sh[NV][kFinalThreads];
+    const int t = threadIdx.x;
     double acc[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = 0.0;
-    // thread t sums blocks t, t+256, ... in order
-    for (int b = threadIdx.x; b < nblocks; b += kBlock) {
+    auto add = [&](int k, double v) { acc[k] = (max_last && k == NV - 1) ? fmax(acc[k], v) : acc[k] + v; };
+    int b = t;
+    for (; b + 3 * kFinalThreads < nrows; b += 4 * kFinalThreads) {
+        double v[4][NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            const double v = partials[static_cast<size_t>(b) * NV + k];
-            acc[k] = (max_last && k == NV - 1) ? fmax(acc[k], v) : acc[k] + v;
-        }
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int k = 0; k < NV; ++k) v[r][k] = p[static_cast<size_t>(b + r * kFinalThreads) * NV + k];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int k = 0; k < NV; ++k) add(k, v[r][k]);
     }
+    for (; b < nrows; b += kFinalThreads)
 #pragma unroll
-    for (int k = 0; k < NV; ++k) sh[threadIdx.x][k] = acc[k];
+        for (int k = 0; k < NV; ++k) add(k, p[static_cast<size_t>(b) * NV + k]);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) sh[k][t] = acc[k];
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < NV; ++k) {
-            double s = sh[0][k];
-            for (int t = 1; t < kBlock; ++t) s = (max_last && k == NV - 1) ? fmax(s, sh[t][k]) : s + sh[t][k];
-            out[k] = s;
-        }
+    for (int st = kFinalThreads / 2; st > 0; st >>= 1) {
+        if (t < st)
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                sh[k][t] = (max_last && k == NV - 1) ? fmax(sh[k][t], sh[k][t + st]) : sh[k][t] + sh[k][t + st];
+        __syncthreads();
     }
+    if (t < NV) out[t] = sh[t][0];
+}
+
+// Sums nblocks rows of NV partials with one block of kFinalThreads; result to out[NV].
+template <int NV>
+__global__ void __launch_bounds__(kFinalThreads) k_reduce_final(const double* __restrict__ partials, int nblocks,
+                                                               double* out, int max_last) {
+    final_sum<NV>(partials, nblocks, out, max_last != 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -491,12 +543,15 @@ __device__ __forceinline__ void load_rk(const S* __restrict__ g, const LatticeVi
     }
 }
 
-// PASS 1 (main_TWOPHASE.cpp:238-246): densities, colour field; FLUX adds the
-// per-block sums of qSumC(f0 + f1)[0] for the flux controller (:292-298).
-template <int Q, class S, bool LOCAL, bool FLUX>
+// PASS 1 (main_TWOPHASE.cpp:238-246): densities, colour field; SUMS writes the
+// per-block sums of qSumC(f0 + f1)[0] for the flux controller (:292-298) and,
+// for shifted storage, of the node totals sum_q (f0 + f1) - rho_ref and
+// sum_q (f0 - f1) for the mass-drift correction.
+template <int Q, class S, bool LOCAL, bool SUMS>
 __global__ void __launch_bounds__(kBlock) k_rk_density(StepArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double fx = 0.0;
+    float fxf = 0.f, mt = 0.f, mc = 0.f;
     if (i < a.L.nf) {
         using T = typename Store<S>::T;
         const S* g = static_cast<const S*>(a.src);
@@ -511,7 +566,7 @@ __global__ void __launch_bounds__(kBlock) k_rk_density(StepArgs a) {
 #pragma unroll
             for (int q = 0; q < Q; ++q) r1 += v1[q];
             a.cg[i] = (r0 - r1) / (r0 + r1);
-            if (FLUX) {
+            if (SUMS) {
                 double ft[Q], j[3];
 #pragma unroll
                 for (int q = 0; q < Q; ++q) ft[q] = v0[q] + v1[q];
@@ -535,14 +590,27 @@ __global__ void __launch_bounds__(kBlock) k_rk_density(StepArgs a) {
             }
             const float rho = a.f_rho_ref + rs;
             a.cgf[i] = dr / rho;
-            fx = jx;
+            fxf = jx;
+            mt = rs;
+            mc = dr;
         }
     }
-    if constexpr (FLUX) {
-        double vals[1] = {fx};
-        block_reduce_store<1>(vals, a.partials, false);
+    if constexpr (SUMS) {
+        if constexpr (Store<S>::shifted) {
+            float vals[3] = {fxf, mt, mc};
+            block_reduce_store_f32<3>(vals, a.partials);
+        } else {
+            double vals[3] = {fx, 0.0, 0.0};
+            block_reduce_store<3>(vals, a.partials, false);
+        }
     }
 }
+
+// After the PASS 1 sums (sum[0] flux, sum[1] total deviation, sum[2] colour
+// difference, over n fluid nodes): the flux controller's force and the
+// mass-drift correction of this step.
+__global__ void k_rk_fix(const double* sum, double n, double rho_ref, double mom_x, int flux, int fix,
+                         DevParams* params);
 
 // Flux controller (main_TWOPHASE.cpp:301-308): force_x = 2 (mom_x - mean).
 __global__ void k_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params);
@@ -686,6 +754,8 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_shift(StepArgs a) {
     const float rfb = a.f_beta * rho0 * rho1 * inv;
     const float dcf = dr * inv;  // c0 - c1
     const float sc_out = a.f_scale;
+    // mass-drift correction: + w_q delta to every population of the node
+    const float fix_t = a.params->mass_fixf[0] * sc_out, fix_c = a.params->mass_fixf[1] * sc_out;
     S* out = static_cast<S*>(a.dst);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -701,8 +771,8 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_shift(StepArgs a) {
         const float dRC = (q == R) ? 0.f : rfb * w * cn * (Lat<Q>::wclass(q) == 1 ? 1.f : 0.70710678118654752f);
         const float X = Xd + w * rho_ref;
         const float s = sc_out / w;
-        Store<S>::store(out + q * a.L.nf_pad + i, Xd * s);
-        Store<S>::store(out + fs + q * a.L.nf_pad + i, (dcf * X + 2.f * dRC) * s);
+        Store<S>::store(out + q * a.L.nf_pad + i, Xd * s + fix_t);
+        Store<S>::store(out + fs + q * a.L.nf_pad + i, (dcf * X + 2.f * dRC) * s + fix_c);
     }
     if (MACROS) {
         a.rho_out[i] = rho0;

@@ -21,14 +21,17 @@ std::atomic<int64_t>& launch_counter();
 
 // bclbm_exact.cu (-fmad=false)
 cudaError_t launch_single_exact(int Q, bool trt, bool local, const StepArgs& a, cudaStream_t s);
-cudaError_t launch_rk_f64(int Q, bool local, bool flux, const StepArgs& a, cudaStream_t s, bool density);
+// sums: PASS 1 writes the per-block flux / mass sums (3 per block)
+cudaError_t launch_rk_f64(int Q, bool local, bool sums, const StepArgs& a, cudaStream_t s, bool density);
 
 // bclbm_kernels.cu
 cudaError_t launch_single_fast(int Q, int precision, bool trt, bool local, const StepArgs& a, cudaStream_t s);
 cudaError_t launch_single_fixed(int Q, bool trt, bool local, const StepArgs& a, cudaStream_t s);
-cudaError_t launch_rk_shift(int Q, int precision, bool local, bool flux, const StepArgs& a, cudaStream_t s,
+cudaError_t launch_rk_shift(int Q, int precision, bool local, bool sums, const StepArgs& a, cudaStream_t s,
                             bool density);
 cudaError_t launch_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params, cudaStream_t s);
+cudaError_t launch_rk_fix(const double* sum, double n, double rho_ref, double mom_x, bool flux, bool fix,
+                          DevParams* params, cudaStream_t s);
 cudaError_t launch_gather(int Q, int precision, int nfields, bool local, const StepArgs& a, const int32_t* slot_bulk,
                           double* out, cudaStream_t s);
 cudaError_t launch_moments(int Q, int precision, int nfields, bool local, const StepArgs& a, cudaStream_t s);

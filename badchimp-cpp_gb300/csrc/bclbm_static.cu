@@ -71,7 +71,7 @@ cudaError_t launch(int nfields, const bclbm::StepArgs& a, int nblocks, double* o
     if (nfields == 1) k_moments<Q, S, 1, true><<<nblocks, kBlock, 0, s>>>(a);
     else k_moments<Q, S, 2, true><<<nblocks, kBlock, 0, s>>>(a);
     launch_counter()++;
-    k_reduce_final<kStaticNV><<<1, kBlock, 0, s>>>(a.partials, nblocks, out, 1);
+    k_reduce_final<kStaticNV><<<1, kFinalThreads, 0, s>>>(a.partials, nblocks, out, 1);
     launch_counter()++;
     return cudaGetLastError();
 }

@@ -31,6 +31,7 @@ PRECISION = {"f64": F64, "f32": F32, "f16": F16, "bf16": BF16}
 FLAG_EXACT = 1
 FLAG_SFC_ORDER = 2
 FLAG_FP64_FMA = 4
+FLAG_NO_MASS_FIX = 8
 
 
 def weights(nq: int) -> np.ndarray:
@@ -128,12 +129,13 @@ class Solver:
 
     def __init__(self, lat: Lattice, f_init, collision=BGK, precision=F64, tau=(1.0, 1.0), force=(0.0, 0.0, 0.0),
                  sigma=0.0, beta=0.0, flux_control=False, mom_x=0.0, rho_init=None, exact=False, sfc=False,
-                 rho_ref=1.0, store_scale=0.0, fma64=False):
+                 rho_ref=1.0, store_scale=0.0, fma64=False, mass_fix=True):
         if isinstance(precision, str):
             precision = PRECISION[precision]
         self.lat = lat
         self.nfields = 2 if collision == RK else 1
-        flags = (FLAG_EXACT if exact else 0) | (FLAG_SFC_ORDER if sfc else 0) | (FLAG_FP64_FMA if fma64 else 0)
+        flags = (FLAG_EXACT if exact else 0) | (FLAG_SFC_ORDER if sfc else 0) | (FLAG_FP64_FMA if fma64 else 0) | \
+            (0 if mass_fix else FLAG_NO_MASS_FIX)
         F = np.zeros(3)
         F[:len(force)] = force
         self._h = _native.create(lat, np.ascontiguousarray(f_init, dtype=np.float64), collision, precision, flags,

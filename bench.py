@@ -488,6 +488,93 @@ def run_serving(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+# two-phase algorithmic bytes per fluid-node update: two population sets read and
+# written, the neighbour table, the colour scalar read and written
+BYTES_PER_UPDATE_RK = {"f64": 4 * 19 * 8 + 18 * 4 + 2 * 8, "f16": 4 * 19 * 2 + 18 * 4 + 2 * 4,
+                       "bf16": 4 * 19 * 2 + 18 * 4 + 2 * 4, "f32": 4 * 19 * 4 + 18 * 4 + 2 * 4}
+
+
+def run_twophase(args, world, rank):
+    """--workload twophase: the Rothman-Keller step on a seeded sphere pack, FP64
+    against shifted FP16 storage (time per step, saturation and phase-flux error)."""
+    import torch
+    import __graft_entry__ as ge
+    bclbm = ge.load()
+    L = bclbm.lbsolver
+    if rank != 0:
+        return
+    t = time.time()
+    geo, centres, phi = bclbm.geometry.sphere_pack((args.size,) * 3, radius=args.radius, porosity=args.porosity,
+                                                   seed=args.seed)
+    lat = L.Lattice.from_geometry(geo, "D3Q19", "xyz")
+    rng = np.random.default_rng(args.seed + 1)
+    red = rng.random(geo.shape) < args.saturation
+    rho0 = np.where(geo == 1, red, 0.0)
+    rho1 = np.where(geo == 1, ~red, 0.0).astype(np.float64)
+    f0, rho = L.initiate_twophase(lat, lat.attribute(rho0), lat.attribute(rho1),
+                                  lat.attribute(np.full(geo.shape, 0.5)))
+    log(f"two-phase geometry {args.size}^3: porosity {phi:.4f}, fluid {lat.n_bulk}, nodes {lat.n_nodes} "
+        f"({time.time() - t:.1f}s)")
+    peak, peak_kind = peaks()
+    cx = np.array([1, 0, 0, 1, 1, 1, 1, 0, 0, -1, 0, 0, -1, -1, -1, -1, 0, 0, 0], dtype=np.float64)
+    res = {}
+    l0 = bclbm.native.launch_count()
+    with ClockSampler(0) as clk:
+        for prec in args.tp_precisions.split(","):
+            with L.Solver(lat, f0, collision=L.RK, precision=prec, tau=(1.0, 1.0), force=(args.gx, 0.0, 0.0),
+                          sigma=args.sigma, beta=args.beta, rho_init=rho) as s:
+                s.step(args.warmup)
+                s.sync()
+                tm = s.step_timed(args.steps)
+                done = args.warmup + args.steps
+                t0 = time.time()
+                if args.tp_steps > done:
+                    s.step(args.tp_steps - done)
+                st = s.reduce()
+                t_acc = time.time() - t0
+                f = s.download_f()
+            F = f.reshape(-1, 2, 19)[lat.bulk]
+            flux = [(F[:, k, :] * cx[None, :]).sum() for k in range(2)]
+            mlups = lat.n_bulk * args.steps / (tm["total_ms"] * 1e-3) / 1e6
+            kernel_ms = (tm["step_kernel_ms"] + tm["density_ms"]) / args.steps
+            ach = lat.n_bulk * BYTES_PER_UPDATE_RK[prec] / (kernel_ms * 1e-3) / 1e9
+            res[prec] = {"mlups": mlups, "ms_per_step": tm["total_ms"] / args.steps, "collide_ms": tm["step_kernel_ms"] /
+                         args.steps, "density_ms": tm["density_ms"] / args.steps, "achieved_gbs": ach,
+                         "frac": ach / peak, "bytes_per_update": BYTES_PER_UPDATE_RK[prec],
+                         "saturation": st["saturation"], "mass": st["mass"], "phase_flux_x": flux,
+                         "steps_total": max(done, args.tp_steps), "seconds_after_timing": t_acc}
+            log(f"{prec}: {mlups:.0f} MLUPS, S = {st['saturation']:.9f}, flux {flux}")
+    launches = bclbm.native.launch_count() - l0
+    ref = res.get("f64")
+    errs = {}
+    if ref:
+        for prec, r in res.items():
+            if prec == "f64":
+                continue
+            errs[prec] = {"saturation_abs": abs(r["saturation"] - ref["saturation"]),
+                          "phase_flux_rel": [abs(a - b) / abs(b) if b else None for a, b in
+                                             zip(r["phase_flux_x"], ref["phase_flux_x"])]}
+    head = res[args.tp_precisions.split(",")[0]]
+    line = {
+        "metric": METRIC, "value": head["mlups"], "unit": "MLUPS", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.tp_precisions.split(",")[0],
+        "data": "synthetic: seeded periodic sphere pack and i.i.d. phase field (numpy default_rng), no dataset",
+        "config": {"workload": f"D3Q19 Rothman-Keller two-phase, periodic {args.size}^3 sphere pack, radius "
+                               f"{args.radius:g}, porosity {phi:.4f} (target {args.porosity:g}), fluid nodes red with "
+                               f"p={args.saturation:g}, tau_r = tau_b = 1, A = {args.sigma:g}, beta = {args.beta:g}, "
+                               f"neutral wetting, gx {args.gx:g}; {args.tp_steps} steps for the errors",
+                   "fluid_nodes": lat.n_bulk, "lattice_nodes": lat.n_nodes,
+                   "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "achieved": head["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": head["frac"], "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "k_rk_density + k_rk_collide (both passes of a step)",
+                     "bytes_per_update": head["bytes_per_update"], "units_per_launch": lat.n_bulk},
+        "precisions": res, "errors_vs_f64": errs, "clocks": clk.summary(), "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -511,8 +598,14 @@ def main():
                     help="steps of the FP64 / FP32 / FP16 / BF16 permeability comparison (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sample of the pack workload line")
-    ap.add_argument("--workload", default="pack", choices=["pack", "serving"],
-                    help="pack: the 256^3 sphere-pack time step; serving: the request loop")
+    ap.add_argument("--workload", default="pack", choices=["pack", "serving", "twophase"],
+                    help="pack: the 256^3 sphere-pack time step; serving: the request loop; twophase: the "
+                         "Rothman-Keller step (use --size 192 --radius 8 for the 192^3 case)")
+    ap.add_argument("--tp-steps", type=int, default=20000, help="twophase: total steps of the accuracy run")
+    ap.add_argument("--tp-precisions", default="f64,f16")
+    ap.add_argument("--saturation", type=float, default=0.5)
+    ap.add_argument("--sigma", type=float, default=0.01)
+    ap.add_argument("--beta", type=float, default=0.99)
     ap.add_argument("--requests", type=int, default=24)
     ap.add_argument("--rates", default="0", help="comma-separated Poisson arrival rates (/s) of the serving runs")
     ap.add_argument("--size-min", type=int, default=32)
@@ -537,6 +630,8 @@ def main():
         ge._load_build_module().build()
         if args.workload == "serving":
             run_serving(args, world, rank)
+        elif args.workload == "twophase":
+            run_twophase(args, world, rank)
         else:
             run_mine(args, world, rank)
     if world > 1:
