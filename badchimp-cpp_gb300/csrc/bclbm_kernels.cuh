@@ -366,8 +366,16 @@ __device__ __forceinline__ void single_node(const StepArgs& a, int i) {
     }
 }
 
+// resident blocks per SM asked of the register allocator: the shifted formats
+// are HBM-latency bound, and 5 blocks (51 registers, no spills) keep more loads in
+// flight than the 4 the allocator picks by itself (FP16 256^3: 38.2 -> 39.6 GLUPS)
+template <class S>
+constexpr int single_min_blocks() {
+    return std::is_same<S, double>::value ? 1 : 5;
+}
+
 template <int Q, class S, int MODE, bool TRT, bool LOCAL>
-__global__ void __launch_bounds__(kBlock) k_single(StepArgs a) {
+__global__ void __launch_bounds__(kBlock, single_min_blocks<S>()) k_single(StepArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.L.nf) single_node<Q, S, MODE, TRT, LOCAL>(a, i);
 }

@@ -538,7 +538,9 @@ def run_twophase(args, world, rank):
             mlups = lat.n_bulk * args.steps / (tm["total_ms"] * 1e-3) / 1e6
             kernel_ms = (tm["step_kernel_ms"] + tm["density_ms"]) / args.steps
             ach = lat.n_bulk * BYTES_PER_UPDATE_RK[prec] / (kernel_ms * 1e-3) / 1e9
-            res[prec] = {"mlups": mlups, "ms_per_step": tm["total_ms"] / args.steps, "collide_ms": tm["step_kernel_ms"] /
+            fp = bclbm.native.footprint(lat, L.RK, L.PRECISION[prec])
+            res[prec] = {"footprint_bytes": fp, "mlups": mlups, "ms_per_step": tm["total_ms"] / args.steps,
+                         "collide_ms": tm["step_kernel_ms"] /
                          args.steps, "density_ms": tm["density_ms"] / args.steps, "achieved_gbs": ach,
                          "frac": ach / peak, "bytes_per_update": BYTES_PER_UPDATE_RK[prec],
                          "saturation": st["saturation"], "mass": st["mass"], "phase_flux_x": flux,
