@@ -82,7 +82,7 @@ __device__ __forceinline__ void load_inst(const BatchInst* __restrict__ inst, in
 // single-instance kernel, one block per SM fewer)
 template <class S, int MODE>
 constexpr int batch_min_blocks() {
-    return std::is_same<S, double>::value ? 2 : 4;
+    return MODE == 2 ? 3 : (std::is_same<S, double>::value ? 2 : 4);
 }
 
 template <int Q, class S, int MODE, bool TRT>

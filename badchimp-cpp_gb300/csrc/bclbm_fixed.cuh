@@ -270,9 +270,13 @@ struct Consts {
 // -3 w_c tsf u.F are exact integer multiples of the diagonal one.
 // Populations of a pair enter through P = f_q + f_rq and M = f_q - f_rq:
 //   alpha f_q + beta f_rq = (alpha + beta)/2 P + (alpha - beta)/2 M.
-template <int Q, bool TRT>
-__host__ __device__ __forceinline__ void collide(int64_t* F, const Consts& K, int64_t& rho_o, int64_t* u_o,
-                                                 int& ovf) {
+// The collision of one node.  F holds the node's 19 (or 9) populations on entry;
+// each post-collision population is handed to sink(q, value) as soon as it is
+// known (pairs in order, the rest direction last), so a kernel can convert and
+// store it and free its registers while the remaining pairs are computed.
+template <int Q, bool TRT, class Sink>
+__host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K, int64_t& rho_o, int64_t* u_o,
+                                                    int& ovf, Sink&& sink) {
     constexpr int D = Lat<Q>::D, NP = Lat<Q>::NP, R = Lat<Q>::REST;
     constexpr int SH1 = Q == 19 ? 1 : 2;  // w_axis / w_diag = 2 or 4
     {
@@ -327,11 +331,12 @@ __host__ __device__ __forceinline__ void collide(int64_t* F, const Consts& K, in
     const int64_t A2 = mul_uu(rho, K.oms_w[2]);
     const int64_t B2 = mul_uu(rho, K.oma3_w[2]);
     const int64_t K2 = mul_ss(uF, K.ktsf_w[2]);
-    const int64_t Aw[3] = {Q == 19 ? (A2 << 3) + (A2 << 2) : (A2 << 4), A2 << SH1, A2};
-    const int64_t Bw[3] = {0, B2 << SH1, B2};
-    const int64_t Kw[3] = {Q == 19 ? (K2 << 3) + (K2 << 2) : (K2 << 4), K2 << SH1, K2};
     const int64_t AB2 = mul_uu(A2, base);
-    const int64_t ABw[3] = {Q == 19 ? (AB2 << 3) + (AB2 << 2) : (AB2 << 4), AB2 << SH1, AB2};
+    // class c values (rest 0, axis 1, diagonal 2) by the exact weight ratios, formed
+    // where they are used rather than held in registers
+    auto by_class = [](int64_t v2, int c) -> int64_t {
+        return c == 2 ? v2 : (c == 1 ? (v2 << SH1) : (Q == 19 ? (v2 << 3) + (v2 << 2) : (v2 << 4)));
+    };
     const int64_t hs = TRT ? (K.alpha + K.beta) >> 1 : K.alpha >> 1;  // (alpha + beta) / 2
     const int64_t ha = TRT ? (K.alpha - K.beta) >> 1 : K.alpha >> 1;  // (alpha - beta) / 2
 #pragma unroll
@@ -341,19 +346,26 @@ __host__ __device__ __forceinline__ void collide(int64_t* F, const Consts& K, in
         const int64_t cua = cu < 0 ? -cu : cu;
         const int64_t cu2 = mul_uu(cua, cua);
         // X = Aw (4.5 cu^2 + base) + kf9 cu + Kw;  Y = Bw cu + ka3
-        int64_t X = ABw[c] + mul_uu(Aw[c], (cu2 << 2) + (cu2 >> 1)) + Kw[c];
+        int64_t X = by_class(AB2, c) + mul_uu(by_class(A2, c), (cu2 << 2) + (cu2 >> 1)) + by_class(K2, c);
         // the force product vanishes for directions normal to the force; the
         // (warp-uniform) branch also bounds how far the compiler interleaves the
         // pairs, which keeps the kernel at ~114 registers and 2 blocks per SM
         if (K.kf9[k] != 0) X += mul_ss(K.kf9[k], cu);
-        const int64_t Y = mul_su(cu, Bw[c]) + K.ka3[k];
+        const int64_t Y = mul_su(cu, by_class(B2, c)) + K.ka3[k];
         // alpha f_q + beta f_rq = hs P + ha M
         const int64_t sp = mul_ss(hs, F[k] + F[k + NP]);
         const int64_t sm = mul_ss(ha, F[k] - F[k + NP]);
-        F[k] = sp + sm + X + Y;
-        F[k + NP] = sp - sm + X - Y;
+        sink(k, sp + sm + X + Y);
+        sink(k + NP, sp - sm + X - Y);
     }
-    F[R] = mul_ss(K.alpha_rest, F[R]) + ABw[0] + Kw[0];
+    sink(R, mul_ss(K.alpha_rest, F[R]) + by_class(AB2, 0) + by_class(K2, 0));
+}
+
+// collide_to with the results written back into F
+template <int Q, bool TRT>
+__host__ __device__ __forceinline__ void collide(int64_t* F, const Consts& K, int64_t& rho_o, int64_t* u_o,
+                                                 int& ovf) {
+    collide_to<Q, TRT>(F, K, rho_o, u_o, ovf, [F](int q, int64_t v) { F[q] = v; });
 }
 
 }  // namespace fx
