@@ -210,10 +210,27 @@ __host__ __device__ __forceinline__ int64_t load_f64(double d, int& ovf) {
 #endif
 }
 
+#ifdef __CUDACC__
+// The kernel's load: hardware F2I of 2^60 d, the scaling an add to the exponent
+// field of the high word.  Zero and subnormal inputs become values below 2^-900,
+// which convert to 0.  The largest exponent field seen goes to emax: >= 1026
+// (|d| >= 8, Inf, NaN) is out of range, and is also where the add can wrap.
+__device__ __forceinline__ int64_t load_f64_hw(double d, unsigned& emax) {
+    const unsigned hi = static_cast<unsigned>(__double2hiint(d));
+    emax = max(emax, hi & 0x7FF00000u);
+    return __double2ll_rn(__hiloint2double(static_cast<int>(hi + (60u << 20)), __double2loint(d)));
+}
+constexpr unsigned kLoadEmaxLimit = 1026u << 20;
+#endif
+
 __host__ __device__ __forceinline__ double store_f64(int64_t x) {
 #if BCLBM_FX_CONV_STORE == 2 && defined(__CUDA_ARCH__)
-    const long long b = __double_as_longlong(__ll2double_rn(x));
-    return __longlong_as_double(b == 0 ? 0ll : b - (60ll << 52));
+    // 2^-60 of the hardware I2F result: exponent - 60 on the high word.  Nonzero
+    // results have exponent >= 963 or the sign bit set, so the unsigned max leaves
+    // them alone and maps 0 to 0.
+    const double r = __ll2double_rn(x);
+    const unsigned hi = static_cast<unsigned>(__double2hiint(r));
+    return __hiloint2double(static_cast<int>(max(hi, 60u << 20) - (60u << 20)), __double2loint(r));
 #elif BCLBM_FX_CONV_STORE == 1 && defined(__CUDA_ARCH__)
     const int64_t sm = x >> 63;
     const uint64_t a = static_cast<uint64_t>((x ^ sm) - sm);

@@ -400,8 +400,15 @@ __device__ __forceinline__ void fixed_node(const StepArgs& a, int i) {
     load_field<Q, double, LOCAL, true>(static_cast<const double*>(a.src), a.L, i, v);
     int ovf = 0;
     int64_t X[Q];
+#if BCLBM_FX_CONV == 2
+    unsigned emax = 0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) X[q] = fx::load_f64_hw(v[q], emax);
+    if (emax >= fx::kLoadEmaxLimit) ovf = 1;
+#else
 #pragma unroll
     for (int q = 0; q < Q; ++q) X[q] = fx::load_f64(v[q], ovf);
+#endif
     int64_t rho, u[3];
     double* out = static_cast<double*>(a.dst) + i;
     const size_t pad = static_cast<size_t>(a.L.nf_pad);
