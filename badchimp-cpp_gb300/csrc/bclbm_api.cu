@@ -374,6 +374,9 @@ void free_all(bclbm_handle* h) {
     cudaFree(h->d_partials);
     cudaFree(h->d_red);
     cudaFree(h->d_gather);
+    if (h->stage) cudaFreeHost(h->stage);
+    if (h->stage_cgf) cudaFreeHost(h->stage_cgf);
+    if (h->stage_event) cudaEventDestroy(h->stage_event);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -764,28 +767,46 @@ int bclbm_download_f(bclbm_handle* h, double* f) {
     return BCLBM_OK;
 }
 
-int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg) {
+int bclbm_macros_begin(bclbm_handle* h) {
     if (!h) return BCLBM_ERR_INVALID;
     if (!h->macros_valid) return fail(h, BCLBM_ERR_INVALID, "no step has run yet");
+    if (h->stage_pending) return fail(h, BCLBM_ERR_INVALID, "a macro download is pending: collect it first");
     CUDA_TRY(h, cudaSetDevice(h->device));
     const size_t pad = static_cast<size_t>(h->nf_pad);
-    std::vector<double> r(static_cast<size_t>(h->nfields) * pad), v(static_cast<size_t>(h->nd) * pad), c;
-    CUDA_TRY(h, cudaMemcpyAsync(r.data(), h->d_rho, r.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    CUDA_TRY(h, cudaMemcpyAsync(v.data(), h->d_vel, v.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    std::vector<float> cf;
-    if (cg && h->collision == BCLBM_RK) {
-        c.resize(h->nf);
-        if (h->d_cgf) {
-            cf.resize(h->nf);
-            CUDA_TRY(h, cudaMemcpyAsync(cf.data(), h->d_cgf, cf.size() * sizeof(float), cudaMemcpyDeviceToHost,
-                                        h->stream));
-        } else {
-            CUDA_TRY(h, cudaMemcpyAsync(c.data(), h->d_cg, c.size() * sizeof(double), cudaMemcpyDeviceToHost,
-                                        h->stream));
-        }
+    const size_t nr = static_cast<size_t>(h->nfields) * pad, nv = static_cast<size_t>(h->nd) * pad;
+    const bool rk = h->collision == BCLBM_RK;
+    if (!h->stage) {
+        // pinned, so the copies run asynchronously to the host
+        CUDA_TRY(h, cudaMallocHost(&h->stage, (nr + nv + (rk ? static_cast<size_t>(h->nf) : 0)) * sizeof(double)));
+        if (rk && h->d_cgf) CUDA_TRY(h, cudaMallocHost(&h->stage_cgf, static_cast<size_t>(h->nf) * sizeof(float)));
+        CUDA_TRY(h, cudaEventCreateWithFlags(&h->stage_event, cudaEventDisableTiming));
     }
-    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-    for (size_t k = 0; k < cf.size(); ++k) c[k] = cf[k];
+    CUDA_TRY(h, cudaMemcpyAsync(h->stage, h->d_rho, nr * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->stage + nr, h->d_vel, nv * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (rk) {
+        if (h->d_cgf)
+            CUDA_TRY(h, cudaMemcpyAsync(h->stage_cgf, h->d_cgf, h->nf * sizeof(float), cudaMemcpyDeviceToHost,
+                                        h->stream));
+        else
+            CUDA_TRY(h, cudaMemcpyAsync(h->stage + nr + nv, h->d_cg, h->nf * sizeof(double), cudaMemcpyDeviceToHost,
+                                        h->stream));
+    }
+    CUDA_TRY(h, cudaEventRecord(h->stage_event, h->stream));
+    h->stage_pending = true;
+    return BCLBM_OK;
+}
+
+int bclbm_macros_collect(bclbm_handle* h, double* rho, double* vel, double* cg) {
+    if (!h) return BCLBM_ERR_INVALID;
+    if (!h->stage_pending) return fail(h, BCLBM_ERR_INVALID, "no macro download to collect");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    h->stage_pending = false;
+    CUDA_TRY(h, cudaEventSynchronize(h->stage_event));
+    const size_t pad = static_cast<size_t>(h->nf_pad);
+    const double* r = h->stage;
+    const double* v = h->stage + static_cast<size_t>(h->nfields) * pad;
+    const double* c = v + static_cast<size_t>(h->nd) * pad;
+    const bool rk = h->collision == BCLBM_RK;
     parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
         for (size_t s = s0; s < s1; ++s) {
             const size_t n = static_cast<size_t>(h->slot_node[s]);
@@ -793,12 +814,17 @@ int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg)
                 for (int k = 0; k < h->nfields; ++k) rho[n * h->nfields + k] = r[k * pad + s];
             if (vel)
                 for (int dd = 0; dd < h->nd; ++dd) vel[n * h->nd + dd] = v[dd * pad + s];
-            if (cg && h->collision == BCLBM_RK) cg[n] = c[s];
+            if (cg && rk) cg[n] = h->stage_cgf ? static_cast<double>(h->stage_cgf[s]) : c[s];
         }
     });
-    if (cg && h->collision == BCLBM_RK)
+    if (cg && rk)
         for (int k = 0; k < h->ns; ++k) cg[h->solid_node[k]] = h->solid_cg[k];
     return BCLBM_OK;
+}
+
+int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg) {
+    const int rc = bclbm_macros_begin(h);
+    return rc ? rc : bclbm_macros_collect(h, rho, vel, cg);
 }
 
 int bclbm_reduce(bclbm_handle* h, bclbm_stats* out) {

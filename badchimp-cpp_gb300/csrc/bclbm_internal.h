@@ -45,6 +45,13 @@ struct bclbm_handle {
     int32_t ghost_src[19] = {0};
     int64_t steps_done = 0;
     size_t footprint = 0;             // device bytes (bclbm_footprint of the descriptor)
+    // asynchronous macro download: pinned staging of rho, vel (slot order) and the
+    // colour, and the event recorded after the copies
+    double* stage = nullptr;
+    float* stage_cgf = nullptr;
+    cudaEvent_t stage_event = nullptr;
+    bool stage_pending = false;
+    bool stage_cg = false;
     std::string last_error;
 };
 

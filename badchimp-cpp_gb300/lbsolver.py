@@ -164,6 +164,19 @@ class Solver:
                                                           _native.dp(cg)), self._h)
         return rho, vel, cg
 
+    def macros_begin(self):
+        """Starts the download of the last step's rho / vel / cg (bclbm_macros_begin)."""
+        _native.check(_native.lib().bclbm_macros_begin(self._h), self._h)
+
+    def macros_collect(self):
+        """Waits for the download started by macros_begin and returns (rho, vel, cg)."""
+        rho = np.zeros(self.lat.n_nodes * self.nfields)
+        vel = np.zeros(self.lat.n_nodes * self.lat.nd)
+        cg = np.zeros(self.lat.n_nodes) if self.nfields == 2 else None
+        _native.check(_native.lib().bclbm_macros_collect(self._h, _native.dp(rho), _native.dp(vel),
+                                                         _native.dp(cg)), self._h)
+        return rho, vel, cg
+
     def reduce(self) -> dict:
         return _native.reduce(self._h)
 

@@ -64,12 +64,13 @@ class Timing(ctypes.Structure):
 
 
 EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_step_timed", "bclbm_download_f", "bclbm_download_macros",
-           "bclbm_reduce", "bclbm_set_force", "bclbm_node_perm", "bclbm_footprint", "bclbm_sync", "bclbm_destroy",
-           "bclbm_error", "bclbm_last_error", "bclbm_launch_count", "bclbm_moments_static", "bclbm_batch_create",
-           "bclbm_batch_admit", "bclbm_batch_admit_steps", "bclbm_batch_attach", "bclbm_batch_retire",
-           "bclbm_batch_step", "bclbm_batch_stats", "bclbm_batch_download_f", "bclbm_batch_info", "bclbm_batch_sync",
-           "bclbm_batch_last_error", "bclbm_batch_destroy", "bclbm_lattice_build", "bclbm_lattice_info",
-           "bclbm_lattice_export", "bclbm_lattice_free"]
+           "bclbm_macros_begin", "bclbm_macros_collect", "bclbm_reduce", "bclbm_set_force", "bclbm_node_perm",
+           "bclbm_footprint", "bclbm_sync", "bclbm_destroy", "bclbm_error", "bclbm_last_error", "bclbm_launch_count",
+           "bclbm_moments_static", "bclbm_batch_create", "bclbm_batch_admit", "bclbm_batch_admit_steps",
+           "bclbm_batch_attach", "bclbm_batch_retire", "bclbm_batch_step", "bclbm_batch_stats",
+           "bclbm_batch_download_f", "bclbm_batch_info", "bclbm_batch_sync", "bclbm_batch_last_error",
+           "bclbm_batch_destroy", "bclbm_lattice_build", "bclbm_lattice_info", "bclbm_lattice_export",
+           "bclbm_lattice_free"]
 
 
 def lib_path() -> Path:
@@ -96,6 +97,10 @@ def lib():
     L.bclbm_download_f.restype = ctypes.c_int
     L.bclbm_download_macros.argtypes = [vp, vp, vp, vp]
     L.bclbm_download_macros.restype = ctypes.c_int
+    L.bclbm_macros_begin.argtypes = [vp]
+    L.bclbm_macros_begin.restype = ctypes.c_int
+    L.bclbm_macros_collect.argtypes = [vp, vp, vp, vp]
+    L.bclbm_macros_collect.restype = ctypes.c_int
     L.bclbm_reduce.argtypes = [vp, ctypes.POINTER(Stats)]
     L.bclbm_reduce.restype = ctypes.c_int
     L.bclbm_set_force.argtypes = [vp, vp]

@@ -142,6 +142,13 @@ int bclbm_step_timed(bclbm_handle* h, int nsteps, bclbm_timing* out);
 int bclbm_download_f(bclbm_handle* h, double* f);
 /* rho [N*nF], vel [N*nD], cg [N] (RK only); any may be NULL; bulk rows only. */
 int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg);
+/* The same download in two halves, so the host can write output while the GPU
+ * goes on stepping: begin enqueues the copies of the last step's rho / vel / cg
+ * into pinned staging on the handle's stream and returns; later bclbm_step calls
+ * queue behind the copies; collect waits for the copies only and writes the
+ * arrays as bclbm_download_macros does.  One download may be pending at a time. */
+int bclbm_macros_begin(bclbm_handle* h);
+int bclbm_macros_collect(bclbm_handle* h, double* rho, double* vel, double* cg);
 /* FP64 reductions over the current populations (deterministic order). */
 int bclbm_reduce(bclbm_handle* h, bclbm_stats* out);
 int bclbm_set_force(bclbm_handle* h, const double force[3]);

@@ -179,6 +179,16 @@ public:
         adaptor_check(bclbm_download_macros(h_, &rho(0, 0), &vel(0, 0, 0), &cg(0, 0)), h_, "bclbm_download_macros");
     }
 
+    /* the same download in two halves: begin after the step to be written, run the
+     * next steps, collect before Output::write (the host writes while the GPU steps) */
+    void macros_begin() { adaptor_check(bclbm_macros_begin(h_), h_, "bclbm_macros_begin"); }
+    void macros_collect(ScalarField& rho, VectorField<DXQY>& vel) const {
+        adaptor_check(bclbm_macros_collect(h_, &rho(0, 0), &vel(0, 0, 0), nullptr), h_, "bclbm_macros_collect");
+    }
+    void macros_collect(ScalarField& rho, VectorField<DXQY>& vel, ScalarField& cg) const {
+        adaptor_check(bclbm_macros_collect(h_, &rho(0, 0), &vel(0, 0, 0), &cg(0, 0)), h_, "bclbm_macros_collect");
+    }
+
     /* FP64 sums: mass per field, momentum, flux-controller sum, saturation */
     bclbm_stats stats() const {
         bclbm_stats s;
