@@ -414,11 +414,46 @@ const char* bclbm_last_error(const bclbm_handle* h) { return h ? h->last_error.c
 int64_t bclbm_launch_count(void) { return launch_counter().load(); }
 
 int bclbm_footprint(const bclbm_desc* desc, size_t* bytes) {
-    if (!bytes) return BCLBM_ERR_INVALID;
+    // sizes only (admission control is called often): the bulk count fixes every
+    // buffer of a single-phase instance; two-phase instances also hold the colour of
+    // the solids their fluid nodes see.  bclbm_create validates the tables.
+    if (!bytes || !desc) return BCLBM_ERR_INVALID;
+    const int Q = desc->lattice_q;
+    if ((Q != 9 && Q != 19) || desc->n_nodes < 2 || desc->n_bulk < 1 || desc->n_bulk >= desc->n_nodes ||
+        desc->collision < BCLBM_BGK || desc->collision > BCLBM_RK || desc->precision < BCLBM_F64 ||
+        desc->precision > BCLBM_BF16)
+        return BCLBM_ERR_INVALID;
     Plan p;
-    std::string err;
-    const int rc = validate_and_plan(desc, p, err, false);
-    if (rc) return rc;
+    p.nf = desc->n_bulk;
+    p.nf_pad = (p.nf + 63) / 64 * 64;
+    p.nfields = desc->collision == BCLBM_RK ? 2 : 1;
+    if (desc->collision == BCLBM_RK) {
+        if (!desc->neigh || !desc->types || !desc->bulk) return BCLBM_ERR_INVALID;
+        const int N = desc->n_nodes;
+        std::vector<uint8_t> used(N, 0);
+        FirstBad bad;
+        parallel_for(static_cast<size_t>(p.nf), [&](size_t b0, size_t b1) {
+            for (size_t b = b0; b < b1; ++b) {
+                const int n = desc->bulk[b];
+                if (n < 1 || n >= N) {
+                    bad.set(static_cast<int64_t>(b));
+                    return;
+                }
+                for (int q = 0; q < Q; ++q) {
+                    const int y = desc->neigh[static_cast<size_t>(n) * Q + q];
+                    if (y < 0 || y >= N) {
+                        bad.set(static_cast<int64_t>(b));
+                        return;
+                    }
+                    if (y != 0 && desc->types[y] < 2) __atomic_store_n(&used[y], static_cast<uint8_t>(1), __ATOMIC_RELAXED);
+                }
+            }
+        });
+        if (bad.any()) return BCLBM_ERR_TABLE;
+        int64_t ns = 0;
+        for (int n = 1; n < N; ++n) ns += used[n];
+        p.ns = static_cast<int>(ns);
+    }
     *bytes = footprint_bytes(desc, p);
     return BCLBM_OK;
 }

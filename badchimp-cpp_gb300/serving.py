@@ -268,6 +268,9 @@ class Server:
         results = []
         cnt = {"admitted": 0, "retired": 0, "promoted": 0, "refused_budget": 0, "rejected_too_large": 0,
                "blocks": 0, "peak_active": 0, "peak_bytes": 0}
+        # seconds of the loop in: launching steps + waiting for the statistics (the GPU's
+        # share), attaching, retiring, and waiting with nothing admitted
+        tm = {"step_and_stats_s": 0.0, "attach_s": 0.0, "retire_s": 0.0, "idle_s": 0.0}
         prep_pool = cf.ThreadPoolExecutor(max_workers=self.prep_workers)
         make_pool = cf.ThreadPoolExecutor(max_workers=2)
         budget = self.hbm_budget
@@ -291,6 +294,14 @@ class Server:
             def committed():
                 return used() + sum(c[2] for c in creating)
 
+            fp_cache = {}
+
+            def footprint(st, rid, lat):
+                # bclbm_footprint plans the whole lattice: once per request and format
+                if (st, rid) not in fp_cache:
+                    fp_cache[(st, rid)] = batches[st].footprint(lat)
+                return fp_cache[(st, rid)]
+
             def in_stage(st):
                 return sum(1 for k in active if k[0] == st) + sum(1 for c in creating if c[0] == st)
 
@@ -310,12 +321,12 @@ class Server:
                 while ready:
                     rid, lat, f0 = ready[0]
                     r = by_id[rid]
-                    if max(b.footprint(lat) for b in batches) > budget:
+                    if max(footprint(j, rid, lat) for j in range(len(batches))) > budget:
                         ready.popleft()
                         cnt["rejected_too_large"] += 1
                         results.append(Result(rid, float("nan"), 0, False, r.arrival, clock(), clock(), lat.n_bulk))
                         continue
-                    need = batches[0].footprint(lat)
+                    need = footprint(0, rid, lat)
                     if committed() + need > budget or in_stage(0) >= self.max_instances:
                         cnt["refused_budget"] += 1
                         break
@@ -324,6 +335,7 @@ class Server:
                            "offset": 0}
                     creating.append([0, make_pool.submit(self._create, 0, lat, f0, r, 1), need, rec])
                 # attach the instances whose set-up has finished
+                t_a = time.perf_counter()
                 for c in [c for c in creating if c[1].done()]:
                     st, fut, need, rec = c
                     iid = batches[st].attach(fut.result())
@@ -333,21 +345,29 @@ class Server:
                     active[(st, iid)] = rec
                     if st == 0:
                         cnt["admitted"] += 1
+                tm["attach_s"] += time.perf_counter() - t_a
                 if not active:
+                    t_i = time.perf_counter()
                     if creating:
                         cf.wait([c[1] for c in creating], timeout=0.05, return_when=cf.FIRST_COMPLETED)
                     else:
                         time.sleep(0.0005)
+                    tm["idle_s"] += time.perf_counter() - t_i
                     continue
                 cnt["peak_active"] = max(cnt["peak_active"], len(active))
                 cnt["peak_bytes"] = max(cnt["peak_bytes"], used())
                 live = sorted({st for st, _ in active})
+                t_s = time.perf_counter()
                 for st in live:
                     batches[st].step(self.check_every)
                 cnt["blocks"] += 1
+                all_stats = {}
                 for st in live:
                     keys = sorted(k for k in active if k[0] == st)
-                    stats = batches[st].stats([k[1] for k in keys])
+                    all_stats[st] = (keys, batches[st].stats([k[1] for k in keys]))
+                tm["step_and_stats_s"] += time.perf_counter() - t_s
+                for st in live:
+                    keys, stats = all_stats[st]
                     now = clock()
                     for key, sd in zip(keys, stats):
                         a = active[key]
@@ -362,8 +382,8 @@ class Server:
                             if not done and a["k"] is not None and k != 0.0 \
                                     and abs(k - a["k"]) / abs(k) < self.promote_tol:
                                 lat = a["lat"]
-                                need = batches[st + 1].footprint(lat)
-                                if committed() - batches[st].footprint(lat) + need <= budget:
+                                need = footprint(st + 1, a["rid"], lat)
+                                if committed() - footprint(st, a["rid"], lat) + need <= budget:
                                     f = batches[st].download_f(key[1])
                                     batches[st].retire(key[1])
                                     del active[key]
@@ -379,7 +399,9 @@ class Server:
                             done, conv = self._done(a["k"], k, steps)
                         a["k"] = k
                         if done:
+                            t_r = time.perf_counter()
                             batches[st].retire(key[1])
+                            tm["retire_s"] += time.perf_counter() - t_r
                             cnt["retired"] += 1
                             results.append(Result(a["rid"], k, steps, conv, r.arrival, a["admitted"], now, a["n"],
                                                   a["hist"]))
@@ -397,7 +419,7 @@ class Server:
             make_pool.shutdown(wait=True)
         results.sort(key=lambda x: x.rid)
         rep = summarize(results, 0.0, t_end)
-        rep["counters"] = cnt
+        rep["counters"] = cnt | {k: round(v, 4) for k, v in tm.items()}
         rep["results"] = results
         return rep
 
