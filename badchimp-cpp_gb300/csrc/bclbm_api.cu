@@ -480,7 +480,8 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     h->collision = d->collision;
     h->precision = d->precision;
     h->flags = d->flags;
-    h->exact = (d->flags & BCLBM_FLAG_EXACT) != 0 || (d->collision == BCLBM_RK && d->precision == BCLBM_F64);
+    h->exact = (d->flags & BCLBM_FLAG_EXACT) != 0 ||
+               (d->collision == BCLBM_RK && d->precision == BCLBM_F64 && !(d->flags & BCLBM_FLAG_FP64_FMA));
     h->trt = d->collision == BCLBM_TRT;
     h->fma64 = (d->flags & BCLBM_FLAG_FP64_FMA) != 0;
     h->flux = d->collision == BCLBM_RK && d->flux_control != 0;
@@ -725,7 +726,8 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
             }
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 1], h->stream));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
-            if (h->precision == BCLBM_F64) CUDA_TRY(h, launch_rk_f64(h->q, local, false, a, h->stream, false));
+            if (h->precision == BCLBM_F64 && !h->exact) CUDA_TRY(h, launch_rk_collide_f64_fma(h->q, local, a, h->stream));
+            else if (h->precision == BCLBM_F64) CUDA_TRY(h, launch_rk_f64(h->q, local, false, a, h->stream, false));
             else CUDA_TRY(h, launch_rk_shift(h->q, h->precision, local, false, a, h->stream, false));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
         }

@@ -34,8 +34,8 @@ cudaError_t rk_f64_q(bool local, bool flux, const StepArgs& a, cudaStream_t s, b
             else k_rk_density<Q, double, false, false><<<g, kBlock, 0, s>>>(a);
         }
     } else {
-        if (local) k_rk_collide_f64<Q, true><<<g, kBlock, 0, s>>>(a);
-        else k_rk_collide_f64<Q, false><<<g, kBlock, 0, s>>>(a);
+        if (local) k_rk_collide_f64<Q, true, false><<<g, kBlock, 0, s>>>(a);
+        else k_rk_collide_f64<Q, false, false><<<g, kBlock, 0, s>>>(a);
     }
     launch_counter()++;
     return cudaGetLastError();

@@ -177,6 +177,19 @@ cudaError_t launch_flux_force(const double* sum, double inv_n, double mom_x, Dev
     return cudaGetLastError();
 }
 
+cudaError_t launch_rk_collide_f64_fma(int Q, bool local, const StepArgs& a, cudaStream_t s) {
+    const int g = grid_for(a.L.nf);
+    if (Q == 9) {
+        if (local) k_rk_collide_f64<9, true, true><<<g, kBlock, 0, s>>>(a);
+        else k_rk_collide_f64<9, false, true><<<g, kBlock, 0, s>>>(a);
+    } else {
+        if (local) k_rk_collide_f64<19, true, true><<<g, kBlock, 0, s>>>(a);
+        else k_rk_collide_f64<19, false, true><<<g, kBlock, 0, s>>>(a);
+    }
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_rk_fix(const double* sum, double n, double rho_ref, double mom_x, bool flux, bool fix,
                           DevParams* params, cudaStream_t s) {
     k_rk_fix<<<1, 32, 0, s>>>(sum, n, rho_ref, mom_x, flux ? 1 : 0, fix ? 1 : 0, params);

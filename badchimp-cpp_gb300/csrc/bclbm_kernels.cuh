@@ -635,8 +635,10 @@ __global__ void k_rk_fix(const double* sum, double n, double rho_ref, double mom
 __global__ void k_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params);
 
 // PASS 2 (main_TWOPHASE.cpp:312-376): RK collision, perturbation and
-// recolouring of F64 populations, in the reference's expression order.
-template <int Q, bool LOCAL>
+// recolouring of F64 populations, in the reference's expression order.  FMA
+// tells the instantiations apart: false in the -fmad=false unit (rounding as the
+// reference), true in the contracting unit (BCLBM_FLAG_FP64_FMA).
+template <int Q, bool LOCAL, bool FMA>
 __global__ void __launch_bounds__(kBlock) k_rk_collide_f64(StepArgs a) {
     const bool MACROS = a.rho_out != nullptr;
     constexpr int D = Lat<Q>::D, R = Lat<Q>::REST;

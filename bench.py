@@ -521,8 +521,9 @@ def run_twophase(args, world, rank):
     l0 = bclbm.native.launch_count()
     with ClockSampler(0) as clk:
         for prec in args.tp_precisions.split(","):
-            with L.Solver(lat, f0, collision=L.RK, precision=prec, tau=(1.0, 1.0), force=(args.gx, 0.0, 0.0),
-                          sigma=args.sigma, beta=args.beta, rho_init=rho) as s:
+            base = prec.split("-")[0]  # "f64-fma": FP64 with FMA contraction
+            with L.Solver(lat, f0, collision=L.RK, precision=base, tau=(1.0, 1.0), force=(args.gx, 0.0, 0.0),
+                          sigma=args.sigma, beta=args.beta, rho_init=rho, fma64=prec.endswith("-fma")) as s:
                 s.step(args.warmup)
                 s.sync()
                 tm = s.step_timed(args.steps)
@@ -537,12 +538,12 @@ def run_twophase(args, world, rank):
             flux = [(F[:, k, :] * cx[None, :]).sum() for k in range(2)]
             mlups = lat.n_bulk * args.steps / (tm["total_ms"] * 1e-3) / 1e6
             kernel_ms = (tm["step_kernel_ms"] + tm["density_ms"]) / args.steps
-            ach = lat.n_bulk * BYTES_PER_UPDATE_RK[prec] / (kernel_ms * 1e-3) / 1e9
-            fp = bclbm.native.footprint(lat, L.RK, L.PRECISION[prec])
+            ach = lat.n_bulk * BYTES_PER_UPDATE_RK[base] / (kernel_ms * 1e-3) / 1e9
+            fp = bclbm.native.footprint(lat, L.RK, L.PRECISION[base])
             res[prec] = {"footprint_bytes": fp, "mlups": mlups, "ms_per_step": tm["total_ms"] / args.steps,
                          "collide_ms": tm["step_kernel_ms"] /
                          args.steps, "density_ms": tm["density_ms"] / args.steps, "achieved_gbs": ach,
-                         "frac": ach / peak, "bytes_per_update": BYTES_PER_UPDATE_RK[prec],
+                         "frac": ach / peak, "bytes_per_update": BYTES_PER_UPDATE_RK[base],
                          "saturation": st["saturation"], "mass": st["mass"], "phase_flux_x": flux,
                          "steps_total": max(done, args.tp_steps), "seconds_after_timing": t_acc}
             log(f"{prec}: {mlups:.0f} MLUPS, S = {st['saturation']:.9f}, flux {flux}")

@@ -75,7 +75,9 @@ extern "C" {
                                    contraction: results bit-identical to the reference */
 #define BCLBM_FLAG_SFC_ORDER 2u /* reorder fluid nodes along a Morton curve of their
                                    positions (needs pos); downloads keep reference order */
-#define BCLBM_FLAG_FP64_FMA 4u  /* BCLBM_F64 single phase: native FP64 arithmetic with FMA */
+#define BCLBM_FLAG_FP64_FMA 4u  /* BCLBM_F64: native FP64 arithmetic with FMA (single phase:
+                                   instead of the fixed point; two-phase: instead of the
+                                   reference's rounding order) */
 #define BCLBM_FLAG_NO_MASS_FIX 8u /* two-phase shifted storage: switch off the per-step correction
                                      that restores the two conserved totals, sum (f0 + f1) and
                                      sum (f0 - f1), from an FP64 reduction (rounding of the
