@@ -101,19 +101,25 @@ __global__ void __launch_bounds__(kBlock, batch_min_blocks<S, MODE>()) k_batch_s
     // the node list, whose upstream neighbours are still in L2 (a static
     // grid-stride split lets the blocks drift apart: 20% slower on 256^3).
     int cur = -1;
+    // Items are taken two at a time (one counter operation and one pair of barriers
+    // per 512 nodes: +3-6% over single items, less with four).
+    constexpr int kTake = 2;
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(next_item, 1);
         __syncthreads();
-        const int w = s_item;
-        if (w >= nw) break;
-        const int2 wk = work[w];
-        if (wk.x != cur) {
-            load_inst(inst, wk.x, st, a);
-            cur = wk.x;
+        const int w0 = kTake * s_item;
+        if (w0 >= nw) break;
+        const int wend = min(w0 + kTake, nw);
+        for (int w = w0; w < wend; ++w) {
+            const int2 wk = work[w];
+            if (wk.x != cur) {
+                load_inst(inst, wk.x, st, a);
+                cur = wk.x;
+            }
+            const int i = wk.y + threadIdx.x;
+            if (i < a.L.nf) batch_node<Q, S, MODE, TRT>(a, i);
         }
-        const int i = wk.y + threadIdx.x;
-        if (i < a.L.nf) batch_node<Q, S, MODE, TRT>(a, i);
-        __syncthreads();  // s_item is rewritten at the next item
+        __syncthreads();  // s_item is rewritten at the next take
     }
     // the last block to finish advances the step and rewinds the counters for the
     // next launch; every block has read *step before it counts itself finished
