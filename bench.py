@@ -216,11 +216,10 @@ def run_reference(args, world, rank):
     F = (args.gx, 0.0, 0.0)
     runner = oracle.SingleRunner(g, bclbm.lbsolver.initiate_single(lat, np.ones(lat.n_nodes)), args.tau, F,
                                  nthreads=nthreads)
-    for _ in range(args.warmup):
-        runner.run(1)
+    # one call per block of steps: the oracle's threads start once per call
+    runner.run(args.warmup)
     t = time.time()
-    for _ in range(args.steps):
-        runner.run(1)
+    runner.run(args.steps)
     dt = time.time() - t
     mlups = lat.n_bulk * args.steps / dt / 1e6
     line = {
