@@ -8,6 +8,7 @@ Translation units are compiled in parallel:
   csrc/bclbm_static.cu   bclbm_moments_static, the entry point that allocates nothing
   csrc/bclbm_batch.cu    the multi-instance batch (persistent kernel, CUDA graph)
   csrc/bclbm_geometry.cu the host-side lattice builder (voxel mask to node tables)
+  csrc/bclbm_vtklb.cu    the .vtklb geometry-file reader (host)
 Host code is compiled with -ffp-contract=off so that host-side arithmetic is
 the same on x86-64 and aarch64.
 """
@@ -34,6 +35,7 @@ UNITS = {
     "bclbm_static.cu": [],
     "bclbm_batch.cu": [],
     "bclbm_geometry.cu": [],
+    "bclbm_vtklb.cu": [],
 }
 
 

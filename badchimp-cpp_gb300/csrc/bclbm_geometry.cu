@@ -21,16 +21,10 @@
 #include "bclbm.h"
 #include "bclbm_device.cuh"
 #include "bclbm_host.h"
+#include "bclbm_lattice.h"
 
 using bclbm::host::parallel_for;
 
-struct bclbm_lattice {
-    int q = 0, nd = 0;
-    int64_t nf = 0, ns = 0;
-    std::vector<int32_t> neigh;  // [n_nodes * q]
-    std::vector<int16_t> types;  // [n_nodes]
-    std::vector<int32_t> pos;    // [n_nodes * nd], -1 for node 0
-};
 
 namespace {
 

@@ -126,6 +126,19 @@ def build_lattice(geo: np.ndarray, lattice: str, periodic: str = "") -> dict:
     return {"neigh": neigh, "types": types, "pos": pos, "nf": nf, "ns": ns, "nq": nq, "nd": nd, "lattice": lattice}
 
 
+def read_vtklb(path, lattice: str, attributes=()) -> dict:
+    """The tables of a .vtklb file (written by the reference's vtklb.py) as
+    ``build_lattice`` returns them, read by the library's bclbm_lattice_read_vtklb
+    (one rank, ASCII, no 2 GiB limit); ``attributes`` names SCALARS to return
+    as per-node arrays (key ``attributes``)."""
+    from . import native
+
+    nq = LATTICE_Q[lattice]
+    neigh, types, pos, nf, ns, attrs = native.read_vtklb(path, nq, tuple(attributes))
+    return {"neigh": neigh, "types": types, "pos": pos, "nf": nf, "ns": ns, "nq": nq, "nd": 2 if nq == 9 else 3,
+            "lattice": lattice, "attributes": attrs}
+
+
 def build_lattice_numpy(geo: np.ndarray, lattice: str, periodic: str = "") -> dict:
     """``build_lattice`` in plain numpy (the same arrays, bit for bit)."""
     c = LATTICE_C[lattice]

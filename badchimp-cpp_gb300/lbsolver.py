@@ -70,6 +70,12 @@ class Lattice:
         return cls(lat["nq"], lat["neigh"], lat["types"], lat["pos"], shape=np.asarray(geo).shape,
                    periodic=periodic)
 
+    @classmethod
+    def from_vtklb(cls, path, lattice: str):
+        """Grid + Nodes of one rank from a .vtklb file (bclbm_lattice_read_vtklb)."""
+        lat = _geometry.read_vtklb(path, lattice)
+        return cls(lat["nq"], lat["neigh"], lat["types"], lat["pos"])
+
     @property
     def n_bulk(self) -> int:
         return int(self.bulk.size)

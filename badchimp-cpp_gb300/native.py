@@ -70,7 +70,7 @@ EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_step_timed", "bclbm_download_f",
            "bclbm_batch_attach", "bclbm_batch_retire", "bclbm_batch_step", "bclbm_batch_stats",
            "bclbm_batch_download_f", "bclbm_batch_info", "bclbm_batch_sync", "bclbm_batch_last_error",
            "bclbm_batch_destroy", "bclbm_lattice_build", "bclbm_lattice_info", "bclbm_lattice_export",
-           "bclbm_lattice_free"]
+           "bclbm_lattice_free", "bclbm_lattice_read_vtklb", "bclbm_lattice_attribute"]
 
 
 def lib_path() -> Path:
@@ -151,6 +151,10 @@ def lib():
     L.bclbm_lattice_export.restype = ctypes.c_int
     L.bclbm_lattice_free.argtypes = [vp]
     L.bclbm_lattice_free.restype = None
+    L.bclbm_lattice_read_vtklb.argtypes = [ctypes.c_char_p, i32, ctypes.POINTER(vp)]
+    L.bclbm_lattice_read_vtklb.restype = ctypes.c_int
+    L.bclbm_lattice_attribute.argtypes = [vp, ctypes.c_char_p, vp]
+    L.bclbm_lattice_attribute.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -240,6 +244,28 @@ def step_timed(h, nsteps: int) -> dict:
 
 def launch_count() -> int:
     return int(lib().bclbm_launch_count())
+
+
+def read_vtklb(path, nq: int, attributes=()):
+    """bclbm_lattice_read_vtklb: (neigh, types, pos, nf, ns, {name: [N] doubles})."""
+    h = ctypes.c_void_p()
+    check(lib().bclbm_lattice_read_vtklb(str(path).encode(), nq, ctypes.byref(h)))
+    try:
+        n, nf, ns = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        check(lib().bclbm_lattice_info(h, ctypes.byref(n), ctypes.byref(nf), ctypes.byref(ns)))
+        nd = 2 if nq == 9 else 3
+        neigh = np.empty(n.value * nq, dtype=np.int32)
+        types = np.empty(n.value, dtype=np.int16)
+        pos = np.empty(n.value * nd, dtype=np.int32)
+        check(lib().bclbm_lattice_export(h, dp(neigh), dp(types), dp(pos)))
+        attrs = {}
+        for name in attributes:
+            a = np.empty(n.value)
+            check(lib().bclbm_lattice_attribute(h, name.encode(), dp(a)))
+            attrs[name] = a
+    finally:
+        lib().bclbm_lattice_free(h)
+    return neigh, types, pos, int(nf.value), int(ns.value), attrs
 
 
 def lattice_tables(mask, nq: int, periodic_bits: int):

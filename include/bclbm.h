@@ -215,6 +215,14 @@ int bclbm_lattice_info(const bclbm_lattice* lat, int64_t* n_nodes, int64_t* n_fl
 /* copies the arrays out (any pointer may be NULL) */
 int bclbm_lattice_export(const bclbm_lattice* lat, int32_t* neigh, int16_t* types, int32_t* pos);
 void bclbm_lattice_free(bclbm_lattice* lat);
+/* The same object from a .vtklb file as PythonScripts/vtklb.py writes it and
+ * LBvtk/Grid/Nodes read it (src/lbsolver/LBvtk.h:221-662, LBgrid.h:127-148,
+ * LBnodes.h:112-209): one rank (no PROCESSOR blocks), ASCII, 64-bit offsets (no
+ * 2 GiB limit).  Node types follow Nodes::setupNodeType from the nodetype
+ * attribute; the bulk list is the nodes of type 2 and 3. */
+int bclbm_lattice_read_vtklb(const char* path, int32_t lattice_q, bclbm_lattice** out);
+/* a SCALARS attribute of the file by name, [N] doubles (0 at the ghost node) */
+int bclbm_lattice_attribute(const bclbm_lattice* lat, const char* name, double* out);
 
 /* ---------------------------------------------------------------------------
  * Multi-instance batch (continuous batching of many solves on one GPU).  No
