@@ -663,8 +663,12 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_f64(StepArgs a) {
     const double rho = rho0 + rho1;
     double j[3] = {0.0, 0.0, 0.0}, vel[3] = {0.0, 0.0, 0.0};
     qsumc_ref<Q>(ft, j);
+    // FMA: the divisions by the same value become one reciprocal and products
+    // (an IEEE FP64 division is a dozen FP64-pipe instructions on this part);
+    // the reference-order kernel keeps every division
+    const double inv_rho = FMA ? 1.0 / rho : 0.0;
 #pragma unroll
-    for (int d = 0; d < D; ++d) vel[d] = (j[d] + 0.5 * F[d]) / rho;
+    for (int d = 0; d < D; ++d) vel[d] = FMA ? (j[d] + 0.5 * F[d]) * inv_rho : (j[d] + 0.5 * F[d]) / rho;
     const double q0 = 0.0, q1 = 0.0;  // mass sources are zero (main_TWOPHASE.cpp:132-136)
     rho0 += 0.5 * q0;
     rho1 += 0.5 * q1;
@@ -675,7 +679,7 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_f64(StepArgs a) {
     const double tau_inv = 1.0 / tau;
     const double uF = dot_ref<Q>(vel, F);
     cdotall_ref<Q>(F, cF);
-    const double tf = (1 - 0.5 / tau);
+    const double tf = FMA ? 1 - 0.5 * tau_inv : (1 - 0.5 / tau);
     double G[3] = {0.0, 0.0, 0.0};
     grad_ref<Q>(sc, G);
     const double cgn = sqrt(dot_ref<Q>(G, G));
@@ -684,10 +688,11 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_f64(StepArgs a) {
     for (int d = 0; d < D; ++d) G[d] *= gs;
     double cn[Q];
     cdotall_ref<Q>(G, cn);
-    const double af = 1.125 * cgn * a.sigma / tau;  // calcDeltaOmegaST (LBcollision2phase.h:11)
-    const double rfb = a.beta * rho0 * rho1 / rho;  // calcDeltaOmegaRC (LBcollision2phase.h:74)
-    const double c0 = (rho0 / rho);
-    const double c1 = (rho1 / rho);
+    // calcDeltaOmegaST (LBcollision2phase.h:11), calcDeltaOmegaRC (LBcollision2phase.h:74)
+    const double af = FMA ? 1.125 * cgn * a.sigma * tau_inv : 1.125 * cgn * a.sigma / tau;
+    const double rfb = FMA ? a.beta * rho0 * rho1 * inv_rho : a.beta * rho0 * rho1 / rho;
+    const double c0 = FMA ? rho0 * inv_rho : (rho0 / rho);
+    const double c1 = FMA ? rho1 * inv_rho : (rho1 / rho);
     if (MACROS) {
         a.rho_out[i] = rho0;
         a.rho_out[static_cast<size_t>(a.L.nf_pad) + i] = rho1;
@@ -705,7 +710,9 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_f64(StepArgs a) {
         const double dQ0 = tf * q0 * w * e;
         const double dQ1 = tf * q1 * w * e;
         const double dST = (q == R) ? -af * Lat<Q>::B(q) : af * (w * cn[q] * cn[q] - Lat<Q>::B(q));
-        const double dRC = (q == R) ? 0.0 : rfb * w * cn[q] / cnorm_ref(Lat<Q>::wclass(q));
+        const double dRC = (q == R)  ? 0.0
+                           : FMA     ? rfb * w * cn[q] * (Lat<Q>::wclass(q) == 1 ? 1.0 : 0.70710678118654752440)
+                                     : rfb * w * cn[q] / cnorm_ref(Lat<Q>::wclass(q));
         out[q * a.L.nf_pad + i] = c0 * (ft[q] + om + dF + dST) + dRC + dQ0;
         out[fs + q * a.L.nf_pad + i] = c1 * (ft[q] + om + dF + dST) - dRC + dQ1;
     }
