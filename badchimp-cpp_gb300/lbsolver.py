@@ -130,6 +130,28 @@ def initiate_twophase(lat: Lattice, rho0_node, rho1_node, wett_node):
     return f.reshape(-1), rho
 
 
+def write_lblbf(path, f, nfields: int, nq: int):
+    """LbField::writeToFile's binary format (src/lbsolver/LBfield.h:378-393): int32
+    nFields, nQ, nNodes, then the FP64 data [node][field][q], little endian."""
+    f = np.ascontiguousarray(f, dtype="<f8").reshape(-1)
+    n_nodes = f.size // (nfields * nq)
+    if n_nodes * nfields * nq != f.size:
+        raise ValueError("f does not hold nNodes x nFields x nQ values")
+    with open(path, "wb") as fh:
+        fh.write(np.array([nfields, nq, n_nodes], dtype="<i4").tobytes())
+        fh.write(f.tobytes())
+
+
+def read_lblbf(path):
+    """LbField::readFromFile's format: returns (f [N*nF*Q], nfields, nq, n_nodes)."""
+    raw = np.fromfile(path, dtype=np.uint8)
+    nfields, nq, n_nodes = (int(x) for x in raw[:12].view("<i4"))
+    f = raw[12:].view("<f8")
+    if f.size != nfields * nq * n_nodes:
+        raise ValueError(f"{path}: {f.size} values for {nfields} x {nq} x {n_nodes}")
+    return f.astype(np.float64), nfields, nq, n_nodes
+
+
 class Solver:
     """One device lattice instance behind the C ABI (bclbm_create ... bclbm_destroy)."""
 
@@ -161,6 +183,11 @@ class Solver:
             out = np.zeros(self.lat.n_nodes * self.nfields * self.lat.nq)
         _native.check(_native.lib().bclbm_download_f(self._h, _native.dp(out)), self._h)
         return out
+
+    def checkpoint(self, path):
+        """The populations after the last step, as the reference's LbField::writeToFile
+        writes them; a Solver created from read_lblbf(path) continues the run exactly."""
+        write_lblbf(path, self.download_f(), self.nfields, self.lat.nq)
 
     def download_macros(self):
         rho = np.zeros(self.lat.n_nodes * self.nfields)

@@ -45,6 +45,7 @@ from . import lbsolver as _lb
 from . import native as _native
 
 BUDGET = -7
+NONFINITE = -6
 
 
 @dataclass
@@ -57,6 +58,7 @@ class Request:
     tau: float
     gx: float = 1e-5
     arrival: float = 0.0  # seconds after the start of the run
+    cancel_at: float | None = None  # seconds after the start: withdrawn by then
 
 
 @dataclass
@@ -70,6 +72,7 @@ class Result:
     finished: float
     n_fluid: int
     history: list = field(default_factory=list)
+    status: str = "converged"  # converged | capped | nonfinite | cancelled | rejected
 
     @property
     def latency(self) -> float:
@@ -170,9 +173,13 @@ class Batch:
         self._check(_native.lib().bclbm_batch_step(self._b, int(nsteps)))
 
     def stats(self, ids) -> list:
+        """Sums of each instance; an instance with NaN/Inf populations (or outside the
+        fixed-point range) has nonfinite set, the others are unaffected."""
         ids = np.ascontiguousarray(ids, dtype=np.int32)
         out = (_native.Stats * max(1, len(ids)))()
-        self._check(_native.lib().bclbm_batch_stats(self._b, len(ids), _native.dp(ids), out))
+        rc = _native.lib().bclbm_batch_stats(self._b, len(ids), _native.dp(ids), out)
+        if rc != NONFINITE:
+            self._check(rc)
         return [_native.stats_dict(out[j]) for j in range(len(ids))]
 
     def download_f(self, iid: int):
@@ -267,7 +274,7 @@ class Server:
         by_id = {r.rid: r for r in reqs}
         results = []
         cnt = {"admitted": 0, "retired": 0, "promoted": 0, "refused_budget": 0, "rejected_too_large": 0,
-               "blocks": 0, "peak_active": 0, "peak_bytes": 0}
+               "cancelled": 0, "nonfinite": 0, "blocks": 0, "peak_active": 0, "peak_bytes": 0}
         # seconds of the loop in: launching steps + waiting for the statistics (the GPU's
         # share), attaching, retiring, and waiting with nothing admitted
         tm = {"step_and_stats_s": 0.0, "attach_s": 0.0, "retire_s": 0.0, "idle_s": 0.0}
@@ -324,7 +331,14 @@ class Server:
                     if max(footprint(j, rid, lat) for j in range(len(batches))) > budget:
                         ready.popleft()
                         cnt["rejected_too_large"] += 1
-                        results.append(Result(rid, float("nan"), 0, False, r.arrival, clock(), clock(), lat.n_bulk))
+                        results.append(Result(rid, float("nan"), 0, False, r.arrival, clock(), clock(), lat.n_bulk,
+                                              status="rejected"))
+                        continue
+                    if r.cancel_at is not None and clock() >= r.cancel_at:
+                        ready.popleft()
+                        cnt["cancelled"] += 1
+                        results.append(Result(rid, float("nan"), 0, False, r.arrival, clock(), clock(), lat.n_bulk,
+                                              status="cancelled"))
                         continue
                     need = footprint(0, rid, lat)
                     if committed() + need > budget or in_stage(0) >= self.max_instances:
@@ -372,9 +386,22 @@ class Server:
                     for key, sd in zip(keys, stats):
                         a = active[key]
                         r = by_id[a["rid"]]
+                        steps = a["offset"] + int(sd["steps_done"])
+                        stop = None
+                        if sd["nonfinite"]:
+                            stop, k = "nonfinite", float("nan")
+                            cnt["nonfinite"] += 1
+                        elif r.cancel_at is not None and now >= r.cancel_at:
+                            stop, k = "cancelled", float("nan")
+                            cnt["cancelled"] += 1
+                        if stop:
+                            batches[st].retire(key[1])
+                            results.append(Result(a["rid"], k, steps, False, r.arrival, a["admitted"], now, a["n"],
+                                                  a["hist"], status=stop))
+                            del active[key]
+                            continue
                         k = permeability(sd["momentum"][0], r)
                         a["hist"].append(k)
-                        steps = a["offset"] + int(sd["steps_done"])
                         if st < len(batches) - 1:
                             # an earlier format never finishes by convergence: it
                             # hands over once k settles to within promote_tol
@@ -404,7 +431,7 @@ class Server:
                             tm["retire_s"] += time.perf_counter() - t_r
                             cnt["retired"] += 1
                             results.append(Result(a["rid"], k, steps, conv, r.arrival, a["admitted"], now, a["n"],
-                                                  a["hist"]))
+                                                  a["hist"], status="converged" if conv else "capped"))
                             del active[key]
             t_end = clock()
         finally:
@@ -449,22 +476,33 @@ class Server:
             lat, f0 = prepared[r.rid] if fut is None else fut.result()
             t_adm = clock()
             hist = []
+            status = None
             with _lb.Solver(lat, f0, tau=(r.tau, r.tau), force=(r.gx, 0.0, 0.0), precision=precision,
                             fma64=self.fma64) as s:
                 s.step(1)
                 steps, k_prev = 1, None
                 while True:
+                    if r.cancel_at is not None and clock() >= r.cancel_at:
+                        status, k, conv = "cancelled", float("nan"), False
+                        break
                     s.step(self.check_every)
                     submit_arrived()
-                    st = s.reduce()
                     steps += self.check_every
+                    try:
+                        st = s.reduce()
+                    except _native.BclbmError as e:
+                        if getattr(e, "status", 0) != NONFINITE:
+                            raise
+                        status, k, conv = "nonfinite", float("nan"), False
+                        break
                     k = permeability(st["momentum"][0], r)
                     hist.append(k)
                     done, conv = self._done(k_prev, k, steps)
                     k_prev = k
                     if done:
                         break
-            results.append(Result(r.rid, k, steps, conv, r.arrival, t_adm, clock(), lat.n_bulk, hist))
+            results.append(Result(r.rid, k, steps, conv, r.arrival, t_adm, clock(), lat.n_bulk, hist,
+                                  status=status or ("converged" if conv else "capped")))
         t_end = clock()
         pool.shutdown(wait=True)
         results.sort(key=lambda x: x.rid)

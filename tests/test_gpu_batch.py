@@ -217,3 +217,64 @@ def test_attach_a_created_handle(bclbm, lattices):
         assert np.array_equal(f, fresh.download_f())
         wrong.close()
         fresh.close()
+
+
+def _small_requests(bclbm, n, seed):
+    S = bclbm.serving
+    return S.sample_requests(n, rate=0.0, seed=seed, size_range=(16, 30), radius_range=(3.0, 4.0),
+                             porosity_range=(0.45, 0.50))
+
+
+def test_server_retires_a_poisoned_request_and_keeps_the_others(bclbm):
+    """A NaN in one request's host copy of the populations: the FP64 statistics flag
+    that request, which retires with status nonfinite; the others finish exactly as
+    in a run without it."""
+    S = bclbm.serving
+    reqs = _small_requests(bclbm, 4, 21)
+    prepared = {r.rid: S.prepare(r) for r in reqs}
+    srv = S.Server(precision="f32", hbm_budget=BUDGET, check_every=100, tol=1e-5, max_steps=2000,
+                   steps_per_graph=25, prep_workers=2)
+    clean = srv.run(reqs, prepared=prepared)
+    lat, f0 = prepared[2]
+    bad = f0.copy()
+    bad[int(lat.bulk[len(lat.bulk) // 3]) * 19 + 4] = np.nan
+    poisoned = dict(prepared)
+    poisoned[2] = (lat, bad)
+    rep = srv.run(reqs, prepared=poisoned)
+    st = {r.rid: r for r in rep["results"]}
+    assert st[2].status == "nonfinite" and rep["counters"]["nonfinite"] == 1
+    for a in clean["results"]:
+        if a.rid != 2:
+            assert st[a.rid].status == a.status and st[a.rid].permeability == a.permeability
+    seq = srv.run_sequential(reqs, precision="f32", prepared=poisoned)
+    assert {r.rid: r.status for r in seq["results"]}[2] == "nonfinite"
+
+
+def test_server_cancellation(bclbm):
+    S = bclbm.serving
+    reqs = _small_requests(bclbm, 3, 22)
+    reqs[1].cancel_at = 0.0  # withdrawn before it is admitted
+    srv = S.Server(precision="f32", hbm_budget=BUDGET, check_every=100, tol=1e-5, max_steps=1500,
+                   steps_per_graph=25, prep_workers=2)
+    rep = srv.run(reqs)
+    st = {r.rid: r.status for r in rep["results"]}
+    assert st[1] == "cancelled" and st[0] in ("converged", "capped") and st[2] in ("converged", "capped")
+    assert rep["counters"]["cancelled"] == 1
+
+
+@pytest.mark.parametrize("precision", ["f64", "f16"])
+def test_checkpoint_and_resume(bclbm, lattices, tmp_path, precision):
+    """Solver.checkpoint writes LbField's .lblbf format; a solver created from it
+    continues exactly as the uninterrupted run."""
+    L = bclbm.lbsolver
+    lat, f0 = lattices[1]
+    with L.Solver(lat, f0, tau=(0.9, 0.9), force=FORCE, precision=precision) as s:
+        s.step(150)
+        s.checkpoint(tmp_path / "c.lblbf")
+        s.step(90)
+        f_cont = s.download_f()
+    f_chk, nf, nq, n = L.read_lblbf(tmp_path / "c.lblbf")
+    assert (nf, nq, n) == (1, 19, lat.n_nodes)
+    with L.Solver(lat, f_chk, tau=(0.9, 0.9), force=FORCE, precision=precision) as s:
+        s.step(90)
+        assert np.array_equal(s.download_f(), f_cont)

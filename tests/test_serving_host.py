@@ -49,3 +49,19 @@ def test_summary_percentiles(bclbm):
     rep = S.summarize(res, 0.0, 100.0)
     assert rep["solves_per_s"] == 1.0 and rep["lattice_updates"] == 100 * 50
     assert abs(rep["p50_s"] - 50.5) < 1e-9 and abs(rep["p99_s"] - 99.01) < 1e-9
+
+
+def test_lblbf_round_trip_and_header(bclbm, tmp_path):
+    L = bclbm.lbsolver
+    f = np.random.default_rng(1).random(7 * 2 * 19)
+    p = tmp_path / "x.lblbf"
+    L.write_lblbf(p, f, 2, 19)
+    raw = p.read_bytes()
+    assert np.frombuffer(raw[:12], dtype="<i4").tolist() == [2, 19, 7]
+    assert len(raw) == 12 + f.size * 8
+    g, nf, nq, n = L.read_lblbf(p)
+    assert (nf, nq, n) == (2, 19, 7) and np.array_equal(f, g)
+    (tmp_path / "bad.lblbf").write_bytes(raw[:-8])
+    import pytest
+    with pytest.raises(ValueError):
+        L.read_lblbf(tmp_path / "bad.lblbf")
