@@ -327,6 +327,17 @@ namespace {
 
 StepArgs make_args(const bclbm_handle* h) { return handle_args(h); }
 
+// FP64 populations -> the int64 fixed-point storage of the default F64 step (the
+// conversion the step itself used to make on every load); out-of-range values
+// raise the fixed-point overflow flag
+__global__ void k_encode_fx(const double* __restrict__ f, int64_t* __restrict__ out, size_t n, int* flag) {
+    const size_t k = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    unsigned emax = 0;
+    out[k] = fx::load_f64_hw(f[k], emax);
+    if (emax >= fx::kLoadEmaxLimit) atomicOr(flag, 1);
+}
+
 __global__ void k_encode(const double* __restrict__ f, void* out, int nf, int nf_pad, int Q, int nfields,
                          int precision, double rho_ref, double scale) {
     // f: FP64 [nfields][Q][nf_pad] reference populations -> storage format
@@ -385,7 +396,8 @@ int run_gather(bclbm_handle* h) {
     if (!h->d_gather) CUDA_TRY(h, cudaMalloc(&h->d_gather, n * sizeof(double)));
     StepArgs a = make_args(h);
     a.src = h->pops[h->cur];
-    CUDA_TRY(h, launch_gather(h->q, h->precision, h->nfields, !h->state_post, a, h->d_slot_bulk, h->d_gather,
+    CUDA_TRY(h, launch_gather(h->q, h->fx_storage ? kFX : h->precision, h->nfields, !h->state_post, a, h->d_slot_bulk,
+                              h->d_gather,
                               h->stream));
     return BCLBM_OK;
 }
@@ -484,6 +496,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
                (d->collision == BCLBM_RK && d->precision == BCLBM_F64 && !(d->flags & BCLBM_FLAG_FP64_FMA));
     h->trt = d->collision == BCLBM_TRT;
     h->fma64 = (d->flags & BCLBM_FLAG_FP64_FMA) != 0;
+    h->fx_storage = d->precision == BCLBM_F64 && d->collision != BCLBM_RK && !h->exact && !h->fma64;
     h->flux = d->collision == BCLBM_RK && d->flux_control != 0;
     h->mass_fix = d->collision == BCLBM_RK && d->precision != BCLBM_F64 && !(d->flags & BCLBM_FLAG_NO_MASS_FIX);
     h->n_nodes = d->n_nodes;
@@ -662,9 +675,22 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
                         soa[(static_cast<size_t>(k) * Q + q) * pad + s] = d->f_init[n * es + static_cast<size_t>(k) * Q + q];
             }
         });
-        if (h->precision == BCLBM_F64) {
+        if (h->precision == BCLBM_F64 && !h->fx_storage) {
             CREATE_TRY(cudaMemcpyAsync(h->pops[0], soa.data(), nsoa * sizeof(double), cudaMemcpyHostToDevice, h->stream));
             CREATE_TRY(cudaStreamSynchronize(h->stream));
+        } else if (h->fx_storage) {
+            double* tmp = nullptr;
+            CREATE_TRY(cudaMalloc(&tmp, nsoa * sizeof(double)));
+            cudaError_t e = cudaMemcpyAsync(tmp, soa.data(), nsoa * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+            if (e == cudaSuccess) {
+                k_encode_fx<<<static_cast<unsigned>((nsoa + kBlock - 1) / kBlock), kBlock, 0, h->stream>>>(
+                    tmp, static_cast<int64_t*>(h->pops[0]), nsoa, &h->d_params->fx_overflow);
+                launch_counter()++;
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+            cudaFree(tmp);
+            CREATE_TRY(e);
         } else {
             double* tmp = nullptr;
             CREATE_TRY(cudaMalloc(&tmp, nsoa * sizeof(double)));
@@ -869,7 +895,7 @@ int bclbm_reduce(bclbm_handle* h, bclbm_stats* out) {
     CUDA_TRY(h, cudaSetDevice(h->device));
     StepArgs a = make_args(h);
     a.src = h->pops[h->cur];
-    CUDA_TRY(h, launch_moments(h->q, h->precision, h->nfields, !h->state_post, a, h->stream));
+    CUDA_TRY(h, launch_moments(h->q, h->fx_storage ? kFX : h->precision, h->nfields, !h->state_post, a, h->stream));
     CUDA_TRY(h, launch_reduce_final(6, h->d_partials, grid_for(h->nf), h->d_red, true, h->stream));
     double red[6];
     DevParams prm;

@@ -360,7 +360,9 @@ int bclbm_batch_create(int32_t lattice_q, int32_t collision, int32_t precision, 
     cudaGetDevice(&b->device);
     const bool trt = collision == BCLBM_TRT;
     b->step_kernel = lattice_q == 9 ? pick_step<9>(precision, b->mode, trt) : pick_step<19>(precision, b->mode, trt);
-    b->mom_kernel = lattice_q == 9 ? pick_mom<9>(precision) : pick_mom<19>(precision);
+    // the fixed-point step keeps int64 storage (Store<int64_t>)
+    b->mom_kernel = b->mode == 2 ? (lattice_q == 9 ? k_batch_moments<9, int64_t> : k_batch_moments<19, int64_t>)
+                                 : (lattice_q == 9 ? pick_mom<9>(precision) : pick_mom<19>(precision));
     auto cleanup = [&](int code) {
         batch_free(b);
         delete b;

@@ -251,6 +251,22 @@ __host__ __device__ __forceinline__ double store_f64(int64_t x) {
 #endif
 }
 
+#ifdef __CUDACC__
+}  // namespace fx
+
+// Fixed-point storage of the FP64 populations (the default BCLBM_F64 step keeps its
+// state in the collision's own int64 format: no conversion per step; downloads
+// and reductions convert to FP64).
+template <>
+struct Store<int64_t> {
+    using T = int64_t;
+    static constexpr bool shifted = false;
+    __device__ static double val(int64_t v) { return fx::store_f64(v); }
+};
+
+namespace fx {
+#endif
+
 // Host-side conversion of a parameter (no overflow expected).
 inline int64_t param(double d) {
     int ovf = 0;

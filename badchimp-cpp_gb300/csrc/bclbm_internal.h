@@ -16,6 +16,7 @@ struct bclbm_handle {
     uint32_t flags = 0;
     bool exact = false, trt = false, flux = false, fma64 = false;
     bool mass_fix = false;  // two-phase shifted storage: per-step mass-drift correction
+    bool fx_storage = false;  // default F64 step: populations held as int64 fixed point
     int n_nodes = 0, nf = 0, nf_pad = 0, ns = 0;
     double tau[2] = {1.0, 1.0};
     double sigma = 0.0, beta = 0.0, mom_x = 0.0, rho_ref = 1.0, scale = 1.0;

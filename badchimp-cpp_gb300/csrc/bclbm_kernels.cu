@@ -1,5 +1,7 @@
 // Restructured FP64 kernels (FMA), FP32-arithmetic kernels for the shifted
 // storage formats, the download gather and the deterministic FP64 reductions.
+#include <type_traits>
+
 #include "bclbm_launch.h"
 
 namespace bclbm {
@@ -110,7 +112,11 @@ cudaError_t rk_shift_q(int precision, bool local, bool flux, const StepArgs& a, 
 template <int Q, class S>
 cudaError_t gather_qs(int nfields, bool local, const StepArgs& a, const int32_t* sb, double* out, cudaStream_t s) {
     const int g = grid_for(a.L.nf);
-    if (nfields == 1) {
+    if constexpr (std::is_same<S, int64_t>::value) {  // fixed-point storage is single-phase only
+        if (nfields != 1) return cudaErrorInvalidValue;
+        if (local) k_gather<Q, S, 1, true><<<g, kBlock, 0, s>>>(a, sb, out);
+        else k_gather<Q, S, 1, false><<<g, kBlock, 0, s>>>(a, sb, out);
+    } else if (nfields == 1) {
         if (local) k_gather<Q, S, 1, true><<<g, kBlock, 0, s>>>(a, sb, out);
         else k_gather<Q, S, 1, false><<<g, kBlock, 0, s>>>(a, sb, out);
     } else {
@@ -124,7 +130,11 @@ cudaError_t gather_qs(int nfields, bool local, const StepArgs& a, const int32_t*
 template <int Q, class S>
 cudaError_t moments_qs(int nfields, bool local, const StepArgs& a, cudaStream_t s) {
     const int g = grid_for(a.L.nf);
-    if (nfields == 1) {
+    if constexpr (std::is_same<S, int64_t>::value) {
+        if (nfields != 1) return cudaErrorInvalidValue;
+        if (local) k_moments<Q, S, 1, true><<<g, kBlock, 0, s>>>(a);
+        else k_moments<Q, S, 1, false><<<g, kBlock, 0, s>>>(a);
+    } else if (nfields == 1) {
         if (local) k_moments<Q, S, 1, true><<<g, kBlock, 0, s>>>(a);
         else k_moments<Q, S, 1, false><<<g, kBlock, 0, s>>>(a);
     } else {
@@ -141,6 +151,7 @@ cudaError_t moments_qs(int nfields, bool local, const StepArgs& a, cudaStream_t 
         case kF32: return FN<Q, float>(__VA_ARGS__);                     \
         case kF16: return FN<Q, __half>(__VA_ARGS__);                    \
         case kBF16: return FN<Q, __nv_bfloat16>(__VA_ARGS__);            \
+        case kFX: return FN<Q, int64_t>(__VA_ARGS__);                    \
     }                                                                    \
     return cudaErrorInvalidValue;
 

@@ -396,24 +396,14 @@ __global__ void __launch_bounds__(kBlock, single_min_blocks<S>()) k_single(StepA
 template <int Q, bool TRT, bool LOCAL>
 __device__ __forceinline__ void fixed_node(const StepArgs& a, int i) {
     constexpr int D = Lat<Q>::D;
-    double v[Q];
-    load_field<Q, double, LOCAL, true>(static_cast<const double*>(a.src), a.L, i, v);
-    int ovf = 0;
+    // the state is held in the collision's int64 format (Store<int64_t>)
     int64_t X[Q];
-#if BCLBM_FX_CONV == 2
-    unsigned emax = 0;
-#pragma unroll
-    for (int q = 0; q < Q; ++q) X[q] = fx::load_f64_hw(v[q], emax);
-    if (emax >= fx::kLoadEmaxLimit) ovf = 1;
-#else
-#pragma unroll
-    for (int q = 0; q < Q; ++q) X[q] = fx::load_f64(v[q], ovf);
-#endif
+    load_field<Q, int64_t, LOCAL, true>(static_cast<const int64_t*>(a.src), a.L, i, X);
+    int ovf = 0;
     int64_t rho, u[3];
-    double* out = static_cast<double*>(a.dst) + i;
+    int64_t* out = static_cast<int64_t*>(a.dst) + i;
     const size_t pad = static_cast<size_t>(a.L.nf_pad);
-    fx::collide_to<Q, TRT>(X, a.fxk, rho, u, ovf,
-                           [out, pad](int q, int64_t v) { out[static_cast<size_t>(q) * pad] = fx::store_f64(v); });
+    fx::collide_to<Q, TRT>(X, a.fxk, rho, u, ovf, [out, pad](int q, int64_t v) { out[static_cast<size_t>(q) * pad] = v; });
     if (a.rho_out != nullptr) {
         a.rho_out[i] = fx::store_f64(rho);
 #pragma unroll
@@ -831,7 +821,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(StepArgs a, const int32_t* __
             if constexpr (Store<S>::shifted)
                 f = Lat<Q>::w(q) * (a.rho_ref + static_cast<double>(Store<S>::val(v[q])) * a.inv_scale);
             else
-                f = v[q];
+                f = Store<S>::val(v[q]);
             out[b * Q + q] = f;
         }
     } else {
@@ -873,7 +863,7 @@ __device__ __forceinline__ void moments_node(const StepArgs& a, int i, double* v
                     bad |= !(fabsf(fq) < CUDART_INF_F);
                     mx = fmaxf(mx, fabsf(fq));
                 } else {
-                    x[q] = v[q];
+                    x[q] = Store<S>::val(v[q]);
                 }
             }
             // sums per weight class of P (mass) and signed sums of M (momentum)

@@ -12,7 +12,9 @@
 
 namespace bclbm {
 
-enum Precision { kF64 = 0, kF32 = 1, kF16 = 2, kBF16 = 3 };
+// storage formats: the public precisions, and kFX, the int64 fixed-point storage of
+// the default BCLBM_F64 step (not a public precision)
+enum Precision { kF64 = 0, kF32 = 1, kF16 = 2, kBF16 = 3, kFX = 4 };
 
 inline int grid_for(int n) { return (n + kBlock - 1) / kBlock; }
 

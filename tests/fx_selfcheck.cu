@@ -1,7 +1,8 @@
 // Test harness: runs the fixed-point collision of csrc/bclbm_fixed.cuh on the
 // CPU (host branch of its __host__ __device__ functions, 128-bit integer
-// multiplies) so that its arithmetic can be checked against the reference
-// fixtures without a GPU.  Built by tests/test_fixed_point.py with nvcc as
+// multiplies), with the state kept in int64 between steps as the device keeps
+// it, so that its arithmetic can be checked against the reference fixtures
+// without a GPU.  Built by tests/test_fixed_point.py with nvcc as
 // host-only code; never part of the library.
 #include <cmath>
 #include <cstdint>
@@ -55,49 +56,34 @@ int run(int n_nodes, const int32_t* neigh, const int16_t* types, int n_bulk, con
                 gsrc[p] = bulk[b];
                 break;
             }
-    std::vector<double> G(static_cast<size_t>(n_nodes) * Q, 0.0), G2(G.size(), 0.0);
+    // the state between steps stays in the collision's int64 format, as on the device
+    std::vector<int64_t> G(static_cast<size_t>(n_nodes) * Q, 0), G2(G.size(), 0);
     int ovf = 0;
+    auto pulled = [&](size_t x, int q) -> int64_t {
+        if (q == L::REST) return G[x * Q + q];
+        const int rq = L::rev(q);
+        const int y = neigh[x * Q + rq];
+        if (y != 0 && types[y] > 1) return G[static_cast<size_t>(y) * Q + q];
+        if (y == 0) return G[static_cast<size_t>(gsrc[rq]) * Q + rq];
+        return G[x * Q + rq];
+    };
     for (int s = 0; s < steps; ++s) {
         for (int b = 0; b < n_bulk; ++b) {
             const size_t x = static_cast<size_t>(bulk[b]);
             int64_t Fx[Q];
-            for (int q = 0; q < Q; ++q) {
-                double v;
-                if (s == 0 || q == L::REST) {
-                    v = s == 0 ? f[x * Q + q] : G[x * Q + q];
-                } else {
-                    const int rq = L::rev(q);
-                    const int y = neigh[x * Q + rq];
-                    if (y != 0 && types[y] > 1) v = G[static_cast<size_t>(y) * Q + q];
-                    else if (y == 0) v = G[static_cast<size_t>(gsrc[rq]) * Q + rq];
-                    else v = G[x * Q + rq];
-                }
-                Fx[q] = fx::from_f64(v, ovf);
-            }
+            for (int q = 0; q < Q; ++q) Fx[q] = s == 0 ? fx::from_f64(f[x * Q + q], ovf) : pulled(x, q);
             int64_t rho, u[3];
             fx::collide<Q, TRT>(Fx, K, rho, u, ovf);
             rho_out[x] = fx::to_f64(rho);
             for (int d = 0; d < L::D; ++d) vel_out[x * L::D + d] = fx::to_f64(u[d]);
-            for (int q = 0; q < Q; ++q) G2[x * Q + q] = fx::to_f64(Fx[q]);
+            for (int q = 0; q < Q; ++q) G2[x * Q + q] = Fx[q];
         }
         G.swap(G2);
     }
     // the reference's f after the last step: one pull of G
     for (int b = 0; b < n_bulk; ++b) {
         const size_t x = static_cast<size_t>(bulk[b]);
-        for (int q = 0; q < Q; ++q) {
-            double v;
-            if (q == L::REST) {
-                v = G[x * Q + q];
-            } else {
-                const int rq = L::rev(q);
-                const int y = neigh[x * Q + rq];
-                if (y != 0 && types[y] > 1) v = G[static_cast<size_t>(y) * Q + q];
-                else if (y == 0) v = G[static_cast<size_t>(gsrc[rq]) * Q + rq];
-                else v = G[x * Q + rq];
-            }
-            f[x * Q + q] = v;
-        }
+        for (int q = 0; q < Q; ++q) f[x * Q + q] = fx::to_f64(pulled(x, q));
     }
     return ovf;
 }
