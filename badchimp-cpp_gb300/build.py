@@ -9,6 +9,7 @@ Translation units are compiled in parallel:
   csrc/bclbm_batch.cu    the multi-instance batch (persistent kernel, CUDA graph)
   csrc/bclbm_geometry.cu the host-side lattice builder (voxel mask to node tables)
   csrc/bclbm_vtklb.cu    the .vtklb geometry-file reader (host)
+  csrc/bclbm_vtu.cu      the VTU/PVTU writer of the output step (host)
 Host code is compiled with -ffp-contract=off so that host-side arithmetic is
 the same on x86-64 and aarch64.
 """
@@ -36,6 +37,7 @@ UNITS = {
     "bclbm_batch.cu": [],
     "bclbm_geometry.cu": [],
     "bclbm_vtklb.cu": [],
+    "bclbm_vtu.cu": [],
 }
 
 

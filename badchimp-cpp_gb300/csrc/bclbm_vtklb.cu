@@ -5,7 +5,7 @@
 // 64-bit offsets, so files past 2 GiB read (LBvtk.h keeps positions in int).
 //
 // Sections, in file order (LBvtk.h:221-662):
-//   header line, title line, ASCII
+//   header line, title line, ASCII | BINARY (both text, as LBvtk reads them)
 //   DATASET UNSTRUCTURED_LB_GRID
 //   [NUM_DIMENSIONS nd]  GLOBAL_DIMENSIONS d0 .. d(nd-1)  [USE_ZERO_GHOST_NODE]
 //   POINTS n type          then nd integers per point
@@ -94,9 +94,12 @@ int basis_index(const int* c, int nd) {
 int parse(Cursor& c, int Q, bclbm_lattice* L, std::string& err) {
     c.rest_of_line();  // header
     c.rest_of_line();  // title
-    if (c.word() != "ASCII") {
-        err = "only ASCII .vtklb files are read";
-        return BCLBM_ERR_UNSUPPORTED;
+    // ASCII or BINARY: LBvtk reads both as text (its ascii_ flag is set and never
+    // used, LBvtk.h:277-289); anything else is an error there
+    const std::string kind = c.word();
+    if (kind != "ASCII" && kind != "BINARY") {
+        err = "files data type must be ASCII or BINARY";
+        return BCLBM_ERR_INVALID;
     }
     c.rest_of_line();
     if (c.word() != "DATASET" || c.word() != "UNSTRUCTURED_LB_GRID") {

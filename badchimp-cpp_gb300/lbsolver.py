@@ -189,10 +189,22 @@ class Solver:
         writes them; a Solver created from read_lblbf(path) continues the run exactly."""
         write_lblbf(path, self.download_f(), self.nfields, self.lat.nq)
 
-    def download_macros(self):
-        rho = np.zeros(self.lat.n_nodes * self.nfields)
-        vel = np.zeros(self.lat.n_nodes * self.lat.nd)
-        cg = np.zeros(self.lat.n_nodes) if self.nfields == 2 else None
+    def _macro_arrays(self, rho, vel, cg):
+        n = self.lat.n_nodes
+        want = ((rho, n * self.nfields), (vel, n * self.lat.nd), (cg, n if self.nfields == 2 else 0))
+        out = []
+        for a, size in want:
+            if a is None:
+                a = np.zeros(size) if size else None
+            elif a.dtype != np.float64 or not a.flags.c_contiguous or a.size != size:
+                raise ValueError(f"macro arrays are contiguous float64 of {size} values (reference layout)")
+            out.append(a)
+        return out
+
+    def download_macros(self, rho=None, vel=None, cg=None):
+        """rho / vel (/ cg) of the last step in the reference layout, written into
+        the given arrays (e.g. the fields an ``output.Output`` reads) or new ones."""
+        rho, vel, cg = self._macro_arrays(rho, vel, cg)
         _native.check(_native.lib().bclbm_download_macros(self._h, _native.dp(rho), _native.dp(vel),
                                                           _native.dp(cg)), self._h)
         return rho, vel, cg
@@ -201,11 +213,9 @@ class Solver:
         """Starts the download of the last step's rho / vel / cg (bclbm_macros_begin)."""
         _native.check(_native.lib().bclbm_macros_begin(self._h), self._h)
 
-    def macros_collect(self):
+    def macros_collect(self, rho=None, vel=None, cg=None):
         """Waits for the download started by macros_begin and returns (rho, vel, cg)."""
-        rho = np.zeros(self.lat.n_nodes * self.nfields)
-        vel = np.zeros(self.lat.n_nodes * self.lat.nd)
-        cg = np.zeros(self.lat.n_nodes) if self.nfields == 2 else None
+        rho, vel, cg = self._macro_arrays(rho, vel, cg)
         _native.check(_native.lib().bclbm_macros_collect(self._h, _native.dp(rho), _native.dp(vel),
                                                          _native.dp(cg)), self._h)
         return rho, vel, cg

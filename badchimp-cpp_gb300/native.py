@@ -70,7 +70,10 @@ EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_step_timed", "bclbm_download_f",
            "bclbm_batch_attach", "bclbm_batch_retire", "bclbm_batch_step", "bclbm_batch_stats",
            "bclbm_batch_download_f", "bclbm_batch_info", "bclbm_batch_sync", "bclbm_batch_last_error",
            "bclbm_batch_destroy", "bclbm_lattice_build", "bclbm_lattice_info", "bclbm_lattice_export",
-           "bclbm_lattice_free", "bclbm_lattice_read_vtklb", "bclbm_lattice_attribute"]
+           "bclbm_lattice_free", "bclbm_lattice_read_vtklb", "bclbm_lattice_attribute", "bclbm_output_create",
+           "bclbm_output_add_file", "bclbm_output_add_field", "bclbm_output_add_array", "bclbm_output_write",
+           "bclbm_output_write_async", "bclbm_output_wait", "bclbm_output_info", "bclbm_output_last_error",
+           "bclbm_output_destroy"]
 
 
 def lib_path() -> Path:
@@ -155,6 +158,22 @@ def lib():
     L.bclbm_lattice_read_vtklb.restype = ctypes.c_int
     L.bclbm_lattice_attribute.argtypes = [vp, ctypes.c_char_p, vp]
     L.bclbm_lattice_attribute.restype = ctypes.c_int
+    L.bclbm_output_create.argtypes = [i32, ctypes.c_int64, vp, vp, ctypes.c_char_p, i32, i32, i32, i32,
+                                      ctypes.POINTER(vp)]
+    L.bclbm_output_add_file.argtypes = [vp, ctypes.c_char_p]
+    L.bclbm_output_add_field.argtypes = [vp, ctypes.c_char_p, vp, i32, i32, i32]
+    L.bclbm_output_add_array.argtypes = [vp, ctypes.c_char_p, vp, i32, ctypes.c_int64]
+    L.bclbm_output_write.argtypes = [vp, ctypes.c_double]
+    L.bclbm_output_write_async.argtypes = [vp, ctypes.c_double]
+    L.bclbm_output_wait.argtypes = [vp]
+    L.bclbm_output_info.argtypes = [vp, i64p, i64p, ctypes.POINTER(i32)]
+    for name in ("bclbm_output_create", "bclbm_output_add_file", "bclbm_output_add_field", "bclbm_output_add_array",
+                 "bclbm_output_write", "bclbm_output_write_async", "bclbm_output_wait", "bclbm_output_info"):
+        getattr(L, name).restype = ctypes.c_int
+    L.bclbm_output_last_error.argtypes = [vp]
+    L.bclbm_output_last_error.restype = ctypes.c_char_p
+    L.bclbm_output_destroy.argtypes = [vp]
+    L.bclbm_output_destroy.restype = None
     _lib = L
     return L
 
@@ -166,11 +185,16 @@ def dp(a):
 ip = dp
 
 
-def check(rc: int, handle=None, batch=None):
+def check(rc: int, handle=None, batch=None, output=None):
     if rc != 0:
         msg = lib().bclbm_error(rc).decode()
-        if handle or batch:
-            detail = lib().bclbm_last_error(handle) if handle else lib().bclbm_batch_last_error(batch)
+        if handle or batch or output:
+            if handle:
+                detail = lib().bclbm_last_error(handle)
+            elif batch:
+                detail = lib().bclbm_batch_last_error(batch)
+            else:
+                detail = lib().bclbm_output_last_error(output)
             if detail:
                 msg += ": " + detail.decode()
         err = BclbmError(f"bclbm status {rc}: {msg}")

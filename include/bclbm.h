@@ -217,8 +217,8 @@ int bclbm_lattice_export(const bclbm_lattice* lat, int32_t* neigh, int16_t* type
 void bclbm_lattice_free(bclbm_lattice* lat);
 /* The same object from a .vtklb file as PythonScripts/vtklb.py writes it and
  * LBvtk/Grid/Nodes read it (src/lbsolver/LBvtk.h:221-662, LBgrid.h:127-148,
- * LBnodes.h:112-209): one rank (no PROCESSOR blocks), ASCII, 64-bit offsets (no
- * 2 GiB limit).  Node types follow Nodes::setupNodeType from the nodetype
+ * LBnodes.h:112-209): one rank (no PROCESSOR blocks), text (an ASCII or BINARY
+ * header, both read as text as LBvtk does), 64-bit offsets (no 2 GiB limit).  Node types follow Nodes::setupNodeType from the nodetype
  * attribute; the bulk list is the nodes of type 2 and 3. */
 int bclbm_lattice_read_vtklb(const char* path, int32_t lattice_q, bclbm_lattice** out);
 /* a SCALARS attribute of the file by name, [N] doubles (0 at the ghost node) */
@@ -274,6 +274,59 @@ int bclbm_batch_info(bclbm_batch* b, size_t* used_bytes, int32_t* n_active, int6
 int bclbm_batch_sync(bclbm_batch* b);
 const char* bclbm_batch_last_error(const bclbm_batch* b);
 void bclbm_batch_destroy(bclbm_batch* b);
+
+/* ---------------------------------------------------------------------------
+ * VTU output of the reference's write step: Output<LT, T, FMT>
+ * (src/io/Output.h:26-177) over VTK::Output (src/io/VTK.h:1421-1550).  The
+ * files are byte-identical to the reference's for the same positions,
+ * variables and write sequence (only the PVTU "Created" time differs):
+ * <dir>/<name>_<n:7>.pvtu and <dir>/vtu/<rank:4>_<name>_<n:7>.vtu, one voxel
+ * (pixel in 2-D) per cell.  Where the appended data would pass 2^31 bytes
+ * (the reference's int offsets overflow there) the VTU is written with
+ * header_type="UInt64".
+ *
+ * create: the cells are the written nodes; pos [n_cells*nd] their positions
+ *   (Grid::pos(nodes), LBgrid.h:114); nodes [n_cells] their node numbers (for
+ *   bclbm_output_add_field), or NULL for arrays only (the
+ *   Output(pos, dir, rank, nproc, ...) form).  value_type: the on-disk type T;
+ *   format: BCLBM_VTU_BINARY (the reference's default) or BCLBM_VTU_ASCII.
+ *   Creates <dir> and <dir>/vtu as the reference does (mkdir of each, 0700).
+ *   nproc > 1 is BCLBM_ERR_UNSUPPORTED (the PVTU pieces of several ranks share
+ *   one file through MPI-IO).
+ * add_file: Output::add_file (Output.h:63).
+ * add_field: Output::add_variables for one ScalarField (dim 1) or VectorField
+ *   (dim nD) of n_fields fields in the reference layout (LBfield.h:69, 219):
+ *   field_no -1 adds one variable per field (Output.h:80-88); field_no >= 0
+ *   adds that field alone (add_variable_with_names, Output.h:111-126).  As in
+ *   the reference, the name gets the field number appended (name<i>) whenever
+ *   n_fields > 1.
+ * add_array: Output::add_variables for a plain vector of `length` values of
+ *   data_type (contiguous; components per cell = length / n_cells).
+ * The data pointers are kept and read at each write (the reference keeps
+ * references to its fields).
+ * write: Output::write(time) (Output.h:58).  write_async: reads the values
+ *   now, writes the files on a background thread and returns; the next call on
+ *   the object, or bclbm_output_wait, waits for it and returns its status.
+ * ------------------------------------------------------------------------- */
+#define BCLBM_VTU_FLOAT64 0
+#define BCLBM_VTU_FLOAT32 1
+#define BCLBM_VTU_INT32 2
+#define BCLBM_VTU_BINARY 0
+#define BCLBM_VTU_ASCII 1
+typedef struct bclbm_output bclbm_output;
+
+int bclbm_output_create(int32_t nd, int64_t n_cells, const int32_t* pos, const int32_t* nodes, const char* dir,
+                        int32_t rank, int32_t nproc, int32_t value_type, int32_t format, bclbm_output** out);
+int bclbm_output_add_file(bclbm_output* o, const char* name);
+int bclbm_output_add_field(bclbm_output* o, const char* name, const double* data, int32_t n_fields, int32_t dim,
+                           int32_t field_no);
+int bclbm_output_add_array(bclbm_output* o, const char* name, const void* data, int32_t data_type, int64_t length);
+int bclbm_output_write(bclbm_output* o, double time);
+int bclbm_output_write_async(bclbm_output* o, double time);
+int bclbm_output_wait(bclbm_output* o);
+int bclbm_output_info(const bclbm_output* o, int64_t* n_points, int64_t* n_cells, int32_t* n_files);
+const char* bclbm_output_last_error(const bclbm_output* o);
+void bclbm_output_destroy(bclbm_output* o);
 
 #ifdef __cplusplus
 }

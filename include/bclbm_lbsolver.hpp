@@ -38,10 +38,12 @@
 
 #include <array>
 #include <cstdint>
+#include <functional>
 #include <cstdlib>
 #include <iostream>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "bclbm.h"
@@ -222,6 +224,112 @@ private:
     LbTables<DXQY> tab_;
     int nfields_;
     bclbm_handle* h_ = nullptr;
+};
+
+/* The output step: Output<LT, T, FMT> of src/io/Output.h:26-177 written by the
+ * library's VTU writer (bclbm_output_*, bclbm.h).  Same constructors and calls
+ * as the reference's class, the same files byte for byte; write_async returns
+ * once the values are read and writes the files on a background thread, so
+ *
+ *   step.download_macros(rho, vel);
+ *   output.write_async(i);        // the host writes while
+ *   step.run(nItrWrite);          // the GPU steps
+ *
+ * overlaps the file write with the next steps.  FMT: 0 binary (VTK::BINARY, the
+ * reference's default), 1 ASCII. */
+template <typename DXQY, typename T = double, int FMT = 0>
+class Output {
+public:
+    /* Output(grid, nodes, dir, rank, nproc) (Output.h:51-54) */
+    template <class GridT>
+    Output(const GridT& grid, const std::vector<int>& nodes, const std::string& dir, int rank, int nproc)
+        : nodes_(nodes.begin(), nodes.end()) {
+        const std::vector<int> p = grid.pos(nodes);
+        create(std::vector<int32_t>(p.begin(), p.end()), nodes_.data(), dir, rank, nproc);
+    }
+    /* Output(pos, dir, rank, nproc) (Output.h:44-47): plain vectors only */
+    Output(const std::vector<int>& pos, const std::string& dir, int rank, int nproc) {
+        create(std::vector<int32_t>(pos.begin(), pos.end()), nullptr, dir, rank, nproc);
+    }
+    /* Output(pos, dir, rank, nproc, varname, var) (Output.h:35-41) */
+    Output(const std::vector<int>& pos, const std::string& dir, int rank, int nproc, const std::string& varname,
+           const std::vector<T>& var)
+        : Output(pos, dir, rank, nproc) {
+        add_file(varname);
+        add_vector(varname, var);
+    }
+    Output(const Output&) = delete;
+    Output& operator=(const Output&) = delete;
+    ~Output() { bclbm_output_destroy(o_); }
+
+    void add_file(const std::string& name) { check(bclbm_output_add_file(o_, name.c_str()), "bclbm_output_add_file"); }
+
+    void add_scalar_variables(const std::vector<std::string>& names,
+                              const std::vector<std::reference_wrapper<const ScalarField>>& fields) {
+        add_fields(names, fields);
+    }
+    void add_vector_variables(const std::vector<std::string>& names,
+                              const std::vector<std::reference_wrapper<const VectorField<DXQY>>>& fields) {
+        add_fields(names, fields);
+    }
+    template <typename F>
+    void add_variable(const std::string& name, const F& field) {
+        add_field(name, field, -1);
+    }
+    /* one variable per field, named explicitly (Output.h:111-126) */
+    template <typename F>
+    void add_variable_with_names(const std::vector<std::string>& names, const F& field) {
+        if (static_cast<int>(names.size()) != field.num_fields())
+            adaptor_fail("bclbm: add_variable_with_names: size of names-vector does not match number of fields");
+        for (int i = 0; i < field.num_fields(); ++i) add_field(names[static_cast<size_t>(i)], field, i);
+    }
+    /* plain vectors (Output.h:137-142) */
+    void add_variables(const std::vector<std::string>& names,
+                       const std::vector<std::reference_wrapper<std::vector<T>>>& vectors) {
+        for (size_t i = 0; i < names.size() && i < vectors.size(); ++i) add_vector(names[i], vectors[i].get());
+    }
+
+    void write(double t = 0.0) { check(bclbm_output_write(o_, t), "bclbm_output_write"); }
+    void write_async(double t = 0.0) { check(bclbm_output_write_async(o_, t), "bclbm_output_write_async"); }
+    void wait() { check(bclbm_output_wait(o_), "bclbm_output_wait"); }
+
+private:
+    static constexpr int32_t type_code() {
+        return std::is_same<T, double>::value ? BCLBM_VTU_FLOAT64
+                                              : (std::is_same<T, float>::value ? BCLBM_VTU_FLOAT32 : BCLBM_VTU_INT32);
+    }
+    static_assert(std::is_same<T, double>::value || std::is_same<T, float>::value || std::is_same<T, int>::value,
+                  "the writer writes double, float or int");
+
+    void create(const std::vector<int32_t>& pos, const int32_t* nodes, const std::string& dir, int rank, int nproc) {
+        const int64_t n = static_cast<int64_t>(pos.size() / DXQY::nD);
+        const int rc = bclbm_output_create(DXQY::nD, n, pos.data(), nodes, dir.c_str(), rank, nproc, type_code(), FMT,
+                                           &o_);
+        if (rc != BCLBM_OK) adaptor_fail(std::string("bclbm: bclbm_output_create failed: ") + bclbm_error(rc));
+    }
+    void check(int rc, const char* call) const {
+        if (rc == BCLBM_OK) return;
+        std::string msg = std::string("bclbm: ") + call + " failed: " + bclbm_error(rc);
+        const std::string detail = bclbm_output_last_error(o_);
+        if (!detail.empty()) msg += " (" + detail + ")";
+        adaptor_fail(msg);
+    }
+    template <typename F>
+    void add_fields(const std::vector<std::string>& names, const std::vector<std::reference_wrapper<const F>>& fields) {
+        for (size_t i = 0; i < names.size() && i < fields.size(); ++i) add_field(names[i], fields[i].get(), -1);
+    }
+    template <typename F>
+    void add_field(const std::string& name, const F& field, int field_no) {
+        check(bclbm_output_add_field(o_, name.c_str(), &field.data()[0], field.num_fields(), field.dim(), field_no),
+              "bclbm_output_add_field");
+    }
+    void add_vector(const std::string& name, const std::vector<T>& v) {
+        check(bclbm_output_add_array(o_, name.c_str(), v.data(), type_code(), static_cast<int64_t>(v.size())),
+              "bclbm_output_add_array");
+    }
+
+    std::vector<int32_t> nodes_;
+    bclbm_output* o_ = nullptr;
 };
 
 }  // namespace bclbm

@@ -17,6 +17,12 @@
 //   twophase <vtklb> <out> k=v ...   the twophase loop (src/twophase/main_TWOPHASE.cpp:236-393);
 //                                    momx=<target> keeps the reference flux controller
 //                                    (:292-308), otherwise the body force stays constant
+//   vtu      <vtklb> <out> nfields=k     the output step (src/io/Output.h:26-177): rho [N*k] and
+//                                    vel [N*k*nD] read from <out>/fields.bin are written by
+//                                    Output<LT> (Float64, binary; two files, two writes, rho
+//                                    doubled in between), Output<LT, float>, Output<LT, double,
+//                                    VTK::ASCII> and the geo file of main_TWOPHASE.cpp:222-224,
+//                                    into <out>/f64, <out>/f32, <out>/ascii and <out>/geo
 //
 // The lattice is chosen at compile time with -DBCLBM_LT=D2Q9|D3Q19, as the
 // reference mains do with '#define LT' (src/std_case/main.cpp:14-15).
@@ -301,9 +307,59 @@ int run_twophase(LBvtk<LT>& vtklb, const std::string& out, const std::map<std::s
 
 }  // namespace
 
+// The output step of the reference mains (src/std_case/main.cpp:101-104, 151;
+// src/twophase/main_TWOPHASE.cpp:217-224), on fields read from <out>/fields.bin.
+int run_vtu(LBvtk<LT>& vtklb, const std::string& out, const std::map<std::string, double>& kv) {
+    Grid<LT> grid(vtklb);
+    Nodes<LT> nodes(vtklb, grid);
+    BndMpi<LT> mpiBoundary(vtklb, nodes, grid);
+    std::vector<int> bulkNodes = findBulkNodes(nodes);
+    const int nF = static_cast<int>(get(kv, "nfields", 1));
+    ScalarField rho(nF, grid.size());
+    VectorField<LT> vel(nF, grid.size());
+    {
+        std::ifstream ifs(out + "/fields.bin", std::ios::binary);
+        ifs.read(reinterpret_cast<char*>(&rho(0, 0)), static_cast<std::streamsize>(sizeof(double)) * nF * grid.size());
+        ifs.read(reinterpret_cast<char*>(&vel(0, 0, 0)),
+                 static_cast<std::streamsize>(sizeof(double)) * nF * LT::nD * grid.size());
+        if (!ifs) {
+            std::fprintf(stderr, "cannot read %s/fields.bin\n", out.c_str());
+            return 1;
+        }
+    }
+    Output<LT> o64(grid, bulkNodes, out + "/f64", 0, 1);
+    o64.add_file("lb_run");
+    o64.add_scalar_variables({"rho"}, {rho});
+    o64.add_vector_variables({"vel"}, {vel});
+    o64.add_file("second");
+    o64.add_scalar_variables({"rho"}, {rho});
+    o64.write(0);
+    for (int n = 0; n < grid.size(); ++n)
+        for (int i = 0; i < nF; ++i) rho(i, n) *= 2.0;
+    o64.write(1000);
+
+    Output<LT, float> o32(grid, bulkNodes, out + "/f32", 0, 1);
+    o32.add_file("lb_f32");
+    o32.add_vector_variables({"vel"}, {vel});
+    o32.add_scalar_variables({"rho"}, {rho});
+    o32.write(0.5);
+
+    Output<LT, double, VTK::ASCII> oa(grid, bulkNodes, out + "/ascii", 0, 1);
+    oa.add_file("lb_ascii");
+    oa.add_scalar_variables({"rho"}, {rho});
+    oa.add_vector_variables({"vel"}, {vel});
+    oa.write(2);
+
+    auto geo = nodes.geo(grid, vtklb);
+    Output<LT, int> geoout(grid.pos(), out + "/geo", 0, 1, "geo", geo);
+    geoout.write();
+    std::printf("vtu: N=%d Nb=%zu nF=%d\n", grid.size(), bulkNodes.size(), nF);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 4) {
-        std::fprintf(stderr, "usage: %s tables|single|twophase <file.vtklb> <outdir> [key=value ...]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s tables|single|twophase|vtu <file.vtklb> <outdir> [key=value ...]\n", argv[0]);
         return 2;
     }
     MPI_Init(NULL, NULL);
@@ -315,6 +371,7 @@ int main(int argc, char** argv) {
     if (mode == "tables") rc = run_tables(vtklb, out);
     else if (mode == "single") rc = run_single(vtklb, out, kv);
     else if (mode == "twophase") rc = run_twophase(vtklb, out, kv);
+    else if (mode == "vtu") rc = run_vtu(vtklb, out, kv);
     else std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     MPI_Finalize();
     return rc;

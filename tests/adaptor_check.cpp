@@ -4,9 +4,12 @@
 //
 //   adaptor_check <vtklb> <outdir>
 // reads the .vtklb file into the reference's LBvtk / Grid / Nodes, writes the
-// adaptor's tables (neigh.i32, types.i16, pos.i32, bulk.i32) into outdir, then
-// builds an LbStep from them and runs 3 steps; prints "status <text>" with the
+// adaptor's tables (neigh.i32, types.i16, pos.i32, bulk.i32) into outdir,
+// writes the same fields with the reference's Output<LT> and with
+// bclbm::Output<LT> into outdir/ref_out and outdir/our_out, then builds an
+// LbStep from the tables and runs 3 steps; prints "status <text>" with the
 // adaptor's error message, or "ran <sum of f>" when a GPU ran the steps.
+#include "IO.h"
 #include "LBSOLVER.h"
 
 #define BCLBM_ADAPTOR_THROW
@@ -41,6 +44,38 @@ int main(int argc, char** argv) {
     dump(out + "/types.i16", tab.types);
     dump(out + "/pos.i32", tab.pos);
     dump(out + "/bulk.i32", tab.bulk);
+    {
+        ScalarField rho(2, grid.size());
+        VectorField<LT> vel(1, grid.size());
+        for (int n = 0; n < grid.size(); ++n) {
+            rho(0, n) = 1.0 + 1e-3 * n;
+            rho(1, n) = 0.5 - 1e-4 * n;
+            for (int d = 0; d < LT::nD; ++d) vel(0, d, n) = 1e-5 * (n % 17) - 2e-5 * d;
+        }
+        auto geo = nodes.geo(grid, vtklb);
+        Output<LT> ro(grid, bulkNodes, out + "/ref_out", 0, 1);
+        ro.add_file("lb_run");
+        ro.add_scalar_variables({"rho"}, {rho});
+        ro.add_vector_variables({"vel"}, {vel});
+        ro.add_file("named");
+        ro.add_variable_with_names({"red", "blue"}, rho);
+        Output<LT, int> rg(grid.pos(), out + "/ref_out", 0, 1, "geo", geo);
+        bclbm::Output<LT> bo(grid, bulkNodes, out + "/our_out", 0, 1);
+        bo.add_file("lb_run");
+        bo.add_scalar_variables({"rho"}, {rho});
+        bo.add_vector_variables({"vel"}, {vel});
+        bo.add_file("named");
+        bo.add_variable_with_names({"red", "blue"}, rho);
+        bclbm::Output<LT, int> bg(grid.pos(), out + "/our_out", 0, 1, "geo", geo);
+        ro.write(0);
+        rg.write();
+        bo.write(0);
+        bg.write();
+        for (int n = 0; n < grid.size(); ++n) rho(0, n) *= 3.0;
+        ro.write(500);
+        bo.write_async(500);
+        bo.wait();
+    }
     LbField<LT> f(1, grid.size());
     for (auto n : bulkNodes)
         for (int q = 0; q < LT::nQ; ++q) f(0, q, n) = LT::w[q] * 1.0;

@@ -19,6 +19,10 @@ in ``<case>.npz``.  Config 1 (the 256x64 channel) is additionally run through
 the UNMODIFIED ``src/std_case/main.cpp`` and its VTU output is compared with
 the driver's dump, which pins the driver itself.
 
+``vtu_<case>.npz`` holds the reference's own output step (``src/io/Output.h``
+through ``ref_driver vtu``) on seeded fields: the fields and the bytes of every
+VTU/PVTU file it wrote.
+
 The fixtures are inputs to the tests; nothing at test time reads the
 reference tree.
 """
@@ -245,11 +249,66 @@ def pin_std_case(ref: Path, vtk: Path, work: Path):
     print(f"std_case pin: {last.name} rho/vel bit-exact against the driver ({nf} nodes)")
 
 
+# The VTU fixtures: (case, fields per node, seed)
+VTU_CASES = [("disc_40x32", 2, 11), ("box_12x10x8", 1, 12)]
+
+
+def vtu_fields(n_nodes, nfields, nd, seed):
+    """Seeded rho [N, nF] and vel [N, nF, nD], with zeros, a negative zero and
+    values below the ASCII writer's 1e-20 cut."""
+    rng = np.random.default_rng(seed)
+    rho = rng.uniform(0.5, 1.5, (n_nodes, nfields))
+    vel = rng.normal(0.0, 0.01, (n_nodes, nfields, nd))
+    rho[3, 0] = 0.0
+    rho[5, 0] = 1e-25
+    vel[4, 0, 0] = -0.0
+    vel[6, 0, nd - 1] = -3e-22
+    vel[7, 0, 0] = 123456.789
+    return rho, vel
+
+
+def reference_vtu(ref: Path, work: Path, vtk: Path, lattice: str, nfields: int, rho, vel):
+    """Runs the reference's output step on the fields; returns {relative path: bytes}."""
+    out = work / "vtu_ref"
+    out.mkdir(parents=True, exist_ok=True)
+    with open(out / "fields.bin", "wb") as fh:
+        fh.write(np.ascontiguousarray(rho, dtype=np.float64).tobytes())
+        fh.write(np.ascontiguousarray(vel, dtype=np.float64).tobytes())
+    exe = REPO / "oracle" / "_ref" / f"ref_driver_{lattice.lower()}"
+    run([str(exe), "vtu", str(vtk), str(out), f"nfields={nfields}"])
+    files = {}
+    for sub in ("f64", "f32", "ascii", "geo"):
+        for p in sorted((out / sub).rglob("*")):
+            if p.is_file():
+                files[str(p.relative_to(out))] = p.read_bytes()
+    return files
+
+
+def make_vtu(ref: Path, name: str, nfields: int, seed: int):
+    z = np.load(HERE / f"{name}.npz")
+    meta = json.loads(bytes(z["meta"]).decode())
+    work = Path(tempfile.mkdtemp(prefix="bclbm_vtu_"))
+    try:
+        mask = z["mask"]
+        vtk = write_vtklb(ref, work, mask, meta["lattice"], meta["periodic"], {"init_rho": np.ones(mask.shape)})
+        rho, vel = vtu_fields(meta["n_nodes"], nfields, meta["nd"], seed)
+        files = reference_vtu(ref, work, vtk, meta["lattice"], nfields, rho, vel)
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    arrays = {"rho": rho, "vel": vel, "nfields": np.array(nfields),
+              "names": np.frombuffer("\n".join(files).encode(), dtype=np.uint8)}
+    for i, (k, v) in enumerate(files.items()):
+        arrays[f"file{i}"] = np.frombuffer(v, dtype=np.uint8)
+    np.savez_compressed(HERE / f"vtu_{name}.npz", **arrays)
+    print(f"vtu_{name}.npz: {len(files)} files, {sum(len(v) for v in files.values())} bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("BCLBM_REFERENCE", "/root/reference"))
     ap.add_argument("--only", default=None)
     ap.add_argument("--pin-only", action="store_true", help="only rerun the std_case pin of config 1")
+    ap.add_argument("--vtu-only", action="store_true", help="only rewrite the VTU fixtures")
     args = ap.parse_args()
     ref = Path(args.reference)
     if args.pin_only:
@@ -261,10 +320,17 @@ def main():
         finally:
             shutil.rmtree(work, ignore_errors=True)
         return
+    if args.vtu_only:
+        for name, nf, seed in VTU_CASES:
+            make_vtu(ref, name, nf, seed)
+        return
     for case in cases():
         if args.only and case["name"] != args.only:
             continue
         make_case(ref, case)
+    for name, nf, seed in VTU_CASES:
+        if not args.only or args.only == name:
+            make_vtu(ref, name, nf, seed)
 
 
 if __name__ == "__main__":

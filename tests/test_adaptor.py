@@ -47,6 +47,16 @@ def test_adaptor_tables_equal_the_reference(bclbm, checker, tmp_path):
     assert np.array_equal(types, lat["types"])
     assert np.array_equal(pos, lat["pos"])
     assert np.array_equal(bulk, np.nonzero(lat["types"] > 1)[0])
+    # bclbm::Output writes the reference Output's files byte for byte
+    import re
+    created = re.compile(rb"<!-- Created [^>]* -->")
+    ref_files = sorted(p.relative_to(tmp_path / "ref_out") for p in (tmp_path / "ref_out").rglob("*") if p.is_file())
+    our_files = sorted(p.relative_to(tmp_path / "our_out") for p in (tmp_path / "our_out").rglob("*") if p.is_file())
+    assert ref_files == our_files and len(ref_files) == 10
+    for rel in ref_files:
+        a = created.sub(b"", (tmp_path / "ref_out" / rel).read_bytes())
+        b = created.sub(b"", (tmp_path / "our_out" / rel).read_bytes())
+        assert a == b, rel
     import torch
     if not torch.cuda.is_available():
         assert res.stdout.startswith("status bclbm: bclbm_create failed: "), res.stdout

@@ -58,9 +58,15 @@ def test_reader_errors(bclbm, tmp_path):
         N.read_vtklb(cut, 9)
     binary = tmp_path / "bin.vtklb"
     binary.write_text(text.replace("ASCII", "BINARY", 1))
+    # LBvtk reads a BINARY header's file as text too (its flag is unused)
+    got = N.read_vtklb(binary, 9)
+    want = N.read_vtklb(vtk, 9)
+    assert all(np.array_equal(a, b) for a, b in zip(got[:3], want[:3]))
+    other = tmp_path / "other.vtklb"
+    other.write_text(text.replace("ASCII", "XML", 1))
     with pytest.raises(N.BclbmError) as e:
-        N.read_vtklb(binary, 9)
-    assert e.value.status == -5
+        N.read_vtklb(other, 9)
+    assert e.value.status == -1
     with pytest.raises(N.BclbmError):
         N.read_vtklb(tmp_path / "missing.vtklb", 9)
     # the intact file reads
