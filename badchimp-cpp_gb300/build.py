@@ -10,6 +10,7 @@ Translation units are compiled in parallel:
   csrc/bclbm_geometry.cu the host-side lattice builder (voxel mask to node tables)
   csrc/bclbm_vtklb.cu    the .vtklb geometry-file reader (host)
   csrc/bclbm_vtu.cu      the VTU/PVTU writer of the output step (host)
+  csrc/bclbm_links.cu    the std_one_phase step: tag resolution, FMA kernel instances
 Host code is compiled with -ffp-contract=off so that host-side arithmetic is
 the same on x86-64 and aarch64.
 """
@@ -38,6 +39,7 @@ UNITS = {
     "bclbm_geometry.cu": [],
     "bclbm_vtklb.cu": [],
     "bclbm_vtu.cu": [],
+    "bclbm_links.cu": [],
 }
 
 

@@ -20,6 +20,7 @@
 #include "bclbm_internal.h"
 #include "bclbm_host.h"
 #include "bclbm_launch.h"
+#include "bclbm_links.h"
 
 using namespace bclbm;
 using bclbm::host::FirstBad;
@@ -76,7 +77,15 @@ int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full)
         err = "n_nodes, neigh, types, n_bulk and bulk are required";
         return BCLBM_ERR_INVALID;
     }
-    if (d->collision < BCLBM_BGK || d->collision > BCLBM_RK) { err = "unknown collision"; return BCLBM_ERR_INVALID; }
+    if (d->collision < BCLBM_BGK || d->collision > BCLBM_LINKS) { err = "unknown collision"; return BCLBM_ERR_INVALID; }
+    if (d->collision == BCLBM_LINKS && (Q != 19 || d->precision != BCLBM_F64)) {
+        err = "BCLBM_LINKS (the std_one_phase step) is D3Q19 with BCLBM_F64";
+        return BCLBM_ERR_UNSUPPORTED;
+    }
+    if (d->collision == BCLBM_LINKS && (!d->tags || !d->labels)) {
+        err = "BCLBM_LINKS needs the tags and labels attributes";
+        return BCLBM_ERR_INVALID;
+    }
     if (d->precision < BCLBM_F64 || d->precision > BCLBM_BF16) { err = "unknown precision"; return BCLBM_ERR_INVALID; }
     if ((d->flags & BCLBM_FLAG_EXACT) && d->precision != BCLBM_F64) {
         err = "BCLBM_FLAG_EXACT needs BCLBM_F64";
@@ -242,6 +251,7 @@ size_t footprint_bytes(const bclbm_desc* d, const Plan& p) {
     if (d->collision == BCLBM_RK)                                                           // colour field
         b += (static_cast<size_t>(p.nf) + p.ns + 1) * (d->precision == BCLBM_F64 ? 8 : 12);
     b += (static_cast<size_t>(grid_for(p.nf)) * 6 + 64) * 8;                               // reduction partials
+    if (d->collision == BCLBM_LINKS) b += pad * 12 + pad * 8;  // info, u_store index, force; labelled-node lists
     return b;
 }
 
@@ -327,6 +337,30 @@ namespace {
 
 StepArgs make_args(const bclbm_handle* h) { return handle_args(h); }
 
+LinksArgs links_args(const bclbm_handle* h, const StepArgs& a) {
+    LinksArgs A;
+    std::memset(&A, 0, sizeof(A));
+    A.s = a;
+    A.info = h->d_info;
+    A.pidx = h->d_pidx;
+    A.force_on = h->d_force_on;
+    A.ustore = h->d_ustore;
+    A.npress = h->npress;
+    A.rho_w = h->rho_w;
+    A.lab_slot = h->d_lab_slot;
+    A.lab_start = h->d_lab_start;
+    A.lab_val = h->d_lab_val;
+    A.lab_g = h->d_lab_g;
+    A.lab_q = h->d_lab_q;
+    A.nlab = h->nlab;
+    A.nlabeled = h->nlabeled;
+    A.flux_slot = h->d_flux_slot;
+    A.flux_phase = h->d_flux_phase;
+    A.nflux = h->nflux;
+    A.flux_out = h->d_flux_out;
+    return A;
+}
+
 // FP64 populations -> the int64 fixed-point storage of the default F64 step (the
 // conversion the step itself used to make on every load); out-of-range values
 // raise the fixed-point overflow flag
@@ -385,6 +419,18 @@ void free_all(bclbm_handle* h) {
     cudaFree(h->d_partials);
     cudaFree(h->d_red);
     cudaFree(h->d_gather);
+    cudaFree(h->d_info);
+    cudaFree(h->d_pidx);
+    cudaFree(h->d_force_on);
+    cudaFree(h->d_ustore);
+    cudaFree(h->d_lab_slot);
+    cudaFree(h->d_lab_start);
+    cudaFree(h->d_lab_val);
+    cudaFree(h->d_lab_g);
+    cudaFree(h->d_lab_q);
+    cudaFree(h->d_flux_slot);
+    cudaFree(h->d_flux_phase);
+    cudaFree(h->d_flux_out);
     if (h->stage) cudaFreeHost(h->stage);
     if (h->stage_cgf) cudaFreeHost(h->stage_cgf);
     if (h->stage_event) cudaEventDestroy(h->stage_event);
@@ -396,6 +442,11 @@ int run_gather(bclbm_handle* h) {
     if (!h->d_gather) CUDA_TRY(h, cudaMalloc(&h->d_gather, n * sizeof(double)));
     StepArgs a = make_args(h);
     a.src = h->pops[h->cur];
+    if (h->collision == BCLBM_LINKS) {
+        CUDA_TRY(h, launch_links_gather(h->exact, !h->state_post, links_args(h, a), h->d_slot_bulk, h->d_gather,
+                                        h->stream));
+        return BCLBM_OK;
+    }
     CUDA_TRY(h, launch_gather(h->q, h->fx_storage ? kFX : h->precision, h->nfields, !h->state_post, a, h->d_slot_bulk,
                               h->d_gather,
                               h->stream));
@@ -432,7 +483,7 @@ int bclbm_footprint(const bclbm_desc* desc, size_t* bytes) {
     if (!bytes || !desc) return BCLBM_ERR_INVALID;
     const int Q = desc->lattice_q;
     if ((Q != 9 && Q != 19) || desc->n_nodes < 2 || desc->n_bulk < 1 || desc->n_bulk >= desc->n_nodes ||
-        desc->collision < BCLBM_BGK || desc->collision > BCLBM_RK || desc->precision < BCLBM_F64 ||
+        desc->collision < BCLBM_BGK || desc->collision > BCLBM_LINKS || desc->precision < BCLBM_F64 ||
         desc->precision > BCLBM_BF16)
         return BCLBM_ERR_INVALID;
     Plan p;
@@ -496,7 +547,9 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
                (d->collision == BCLBM_RK && d->precision == BCLBM_F64 && !(d->flags & BCLBM_FLAG_FP64_FMA));
     h->trt = d->collision == BCLBM_TRT;
     h->fma64 = (d->flags & BCLBM_FLAG_FP64_FMA) != 0;
-    h->fx_storage = d->precision == BCLBM_F64 && d->collision != BCLBM_RK && !h->exact && !h->fma64;
+    h->fx_storage = d->precision == BCLBM_F64 && d->collision != BCLBM_RK && d->collision != BCLBM_LINKS &&
+                    !h->exact && !h->fma64;
+    h->rho_w = d->rho_w != 0.0 ? d->rho_w : 1.0;
     h->flux = d->collision == BCLBM_RK && d->flux_control != 0;
     h->mass_fix = d->collision == BCLBM_RK && d->precision != BCLBM_F64 && !(d->flags & BCLBM_FLAG_NO_MASS_FIX);
     h->n_nodes = d->n_nodes;
@@ -562,7 +615,28 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             if (last[pdir].load() >= 0) h->ghost_src[pdir] = slot_of_bulk[last[pdir].load()];
     }
     std::vector<int32_t> tab;
-    if (h->collision == BCLBM_RK) {
+    LinksPlan lp;
+    if (h->collision == BCLBM_LINKS) {
+        std::string lerr;
+        if (static_cast<size_t>(Q) * pad > static_cast<size_t>(INT32_MAX)) {
+            std::fprintf(stderr, "bclbm_create: %d fluid nodes exceed the int32 pull table\n", h->nf);
+            free_all(h);
+            delete h;
+            return BCLBM_ERR_UNSUPPORTED;
+        }
+        const int lrc = links_plan(d, h->slot_node, h->ghost_src, pad, lp, tab, lerr);
+        if (lrc != BCLBM_OK) {
+            std::fprintf(stderr, "bclbm_create: %s\n", lerr.c_str());
+            free_all(h);
+            delete h;
+            return lrc;
+        }
+        h->npress = lp.npress;
+        h->nlab = lp.nlab;
+        h->nlabeled = static_cast<int>(lp.lab_slot.size());
+        h->nflux = static_cast<int>(lp.flux_slot.size());
+        h->force_on_sum = lp.force_on_sum;
+    } else if (h->collision == BCLBM_RK) {
         // extended neighbour table in device numbering (pull + colour gradient)
         tab.assign(static_cast<size_t>(R) * pad, static_cast<int32_t>(h->nf + h->ns));
         parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
@@ -638,6 +712,30 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         }
     }
     CREATE_TRY(cudaMemcpyAsync(h->d_params, &prm, sizeof(prm), cudaMemcpyHostToDevice, h->stream));
+    if (h->collision == BCLBM_LINKS) {
+        auto up = [&](auto** dst, const auto& v, size_t n_min) -> cudaError_t {
+            using E = typename std::remove_reference<decltype(v)>::type::value_type;
+            const size_t n = std::max(v.size(), n_min);
+            cudaError_t e = cudaMalloc(reinterpret_cast<void**>(dst), n * sizeof(E));
+            if (e == cudaSuccess && !v.empty())
+                e = cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice, h->stream);
+            return e;
+        };
+        CREATE_TRY(up(&h->d_info, lp.info, 1));
+        CREATE_TRY(up(&h->d_pidx, lp.pidx, 1));
+        CREATE_TRY(up(&h->d_force_on, lp.force_on, 1));
+        CREATE_TRY(up(&h->d_lab_slot, lp.lab_slot, 1));
+        CREATE_TRY(up(&h->d_lab_start, lp.lab_start, 2));
+        CREATE_TRY(up(&h->d_lab_g, lp.lab_g, 1));
+        CREATE_TRY(up(&h->d_flux_slot, lp.flux_slot, 1));
+        CREATE_TRY(up(&h->d_flux_phase, lp.flux_phase, 1));
+        CREATE_TRY(cudaMalloc(&h->d_ustore, std::max<size_t>(3 * static_cast<size_t>(h->npress), 1) * sizeof(double)));
+        CREATE_TRY(cudaMalloc(&h->d_lab_val, std::max<size_t>(lp.lab_slot.size(), 1) * sizeof(double)));
+        CREATE_TRY(cudaMalloc(&h->d_lab_q, (static_cast<size_t>(h->nlab) + 1) * sizeof(double)));
+        CREATE_TRY(cudaMemsetAsync(h->d_lab_q, 0, (static_cast<size_t>(h->nlab) + 1) * sizeof(double), h->stream));
+        CREATE_TRY(cudaMalloc(&h->d_flux_out, 2 * sizeof(double)));
+        CREATE_TRY(cudaStreamSynchronize(h->stream));  // the host vectors go out of scope
+    }
 
     // colour field: fluid slots (written every step), stored solids (fixed), ghost (0)
     if (h->collision == BCLBM_RK) {
@@ -731,7 +829,11 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
         a.dst = h->pops[1 - h->cur];
         a.rho_out = macros ? h->d_rho : nullptr;
         a.vel_out = macros ? h->d_vel : nullptr;
-        if (h->collision != BCLBM_RK) {
+        if (h->collision == BCLBM_LINKS) {
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
+            CUDA_TRY(h, launch_links_step(h->exact, local, links_args(h, a), h->stream));
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
+        } else if (h->collision != BCLBM_RK) {
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
             if (h->exact) CUDA_TRY(h, launch_single_exact(h->q, h->trt, local, a, h->stream));
             else if (h->precision == BCLBM_F64 && !h->fma64)
@@ -895,7 +997,10 @@ int bclbm_reduce(bclbm_handle* h, bclbm_stats* out) {
     CUDA_TRY(h, cudaSetDevice(h->device));
     StepArgs a = make_args(h);
     a.src = h->pops[h->cur];
-    CUDA_TRY(h, launch_moments(h->q, h->fx_storage ? kFX : h->precision, h->nfields, !h->state_post, a, h->stream));
+    if (h->collision == BCLBM_LINKS)
+        CUDA_TRY(h, launch_links_moments(h->exact, !h->state_post, links_args(h, a), h->stream));
+    else
+        CUDA_TRY(h, launch_moments(h->q, h->fx_storage ? kFX : h->precision, h->nfields, !h->state_post, a, h->stream));
     CUDA_TRY(h, launch_reduce_final(6, h->d_partials, grid_for(h->nf), h->d_red, true, h->stream));
     double red[6];
     DevParams prm;
@@ -907,7 +1012,8 @@ int bclbm_reduce(bclbm_handle* h, bclbm_stats* out) {
     out->mass[1] = red[1];
     for (int k = 0; k < 3; ++k) {
         out->flux_fc[k] = red[2 + k];
-        out->momentum[k] = red[2 + k] + 0.5 * prm.force[k] * static_cast<double>(h->nf);
+        out->momentum[k] = red[2 + k] + 0.5 * prm.force[k] *
+                                            (h->collision == BCLBM_LINKS ? h->force_on_sum : static_cast<double>(h->nf));
     }
     out->saturation = h->collision == BCLBM_RK ? red[0] / (red[0] + red[1]) : 0.0;
     out->max_abs_f = red[5];
@@ -931,6 +1037,20 @@ int bclbm_set_force(bclbm_handle* h, const double force[3]) {
     }
     CUDA_TRY(h, cudaMemcpyAsync(h->d_params, &prm, offsetof(DevParams, fx_overflow), cudaMemcpyHostToDevice,
                                 h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return BCLBM_OK;
+}
+
+int bclbm_pressure_flux(bclbm_handle* h, double q[2]) {
+    if (!h || !q) return BCLBM_ERR_INVALID;
+    if (h->collision != BCLBM_LINKS) return fail(h, BCLBM_ERR_INVALID, "the mass flux is a BCLBM_LINKS output");
+    if (!h->macros_valid) return fail(h, BCLBM_ERR_INVALID, "no step has run yet");
+    CUDA_TRY(h, cudaSetDevice(h->device));
+    StepArgs a = make_args(h);
+    a.rho_out = h->d_rho;
+    a.vel_out = h->d_vel;
+    CUDA_TRY(h, launch_links_flux(links_args(h, a), h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(q, h->d_flux_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return BCLBM_OK;
 }

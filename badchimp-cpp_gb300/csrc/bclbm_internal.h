@@ -53,6 +53,23 @@ struct bclbm_handle {
     cudaEvent_t stage_event = nullptr;
     bool stage_pending = false;
     bool stage_cg = false;
+    // the std_one_phase step (BCLBM_LINKS): per-slot info / u_store index / force
+    // attribute, the velocity store of the pressure-boundary nodes, the interior
+    // domains' node lists, sums and sources, and the mass-flux node list
+    uint32_t* d_info = nullptr;
+    int32_t* d_pidx = nullptr;
+    int32_t* d_force_on = nullptr;
+    double* d_ustore = nullptr;
+    int32_t* d_lab_slot = nullptr;
+    int32_t* d_lab_start = nullptr;
+    double* d_lab_val = nullptr;
+    double* d_lab_g = nullptr;
+    double* d_lab_q = nullptr;
+    int32_t* d_flux_slot = nullptr;
+    int32_t* d_flux_phase = nullptr;
+    double* d_flux_out = nullptr;
+    int npress = 0, nlab = 0, nlabeled = 0, nflux = 0;
+    double rho_w = 1.0, force_on_sum = 0.0;
     std::string last_error;
 };
 

@@ -1,0 +1,46 @@
+// The std_one_phase step (BCLBM_LINKS): host plan and launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "bclbm.h"
+#include "bclbm_links.cuh"
+
+namespace bclbm {
+
+// what bclbm_create derives from the node attributes of a BCLBM_LINKS descriptor
+struct LinksPlan {
+    std::vector<uint32_t> info;        // [nf] label | kLinkAdd | kLinkPress
+    std::vector<int32_t> pidx;         // [nf] u_store index or -1
+    std::vector<int32_t> force_on;     // [nf]
+    std::vector<int32_t> lab_slot;     // labelled bulk nodes by label, bulk order
+    std::vector<int32_t> lab_start;    // [nlab + 2]
+    std::vector<double> lab_g;         // [nlab + 1] 0.9 * 2 / (source nodes of the label)
+    std::vector<int32_t> flux_slot;    // bulk pressure-boundary nodes, node order
+    std::vector<int32_t> flux_phase;
+    int npress = 0, nlab = 0;
+    double force_on_sum = 0.0;         // sum of the force attribute over the bulk nodes
+};
+
+// resolves the tags into the pull table tab [18][pad] (see bclbm_links.cu)
+int links_plan(const bclbm_desc* d, const std::vector<int32_t>& slot_node, const int32_t* ghost_src, size_t pad,
+               LinksPlan& P, std::vector<int32_t>& tab, std::string& err);
+
+// bclbm_exact.cu (-fmad=false): the reference's rounding
+cudaError_t launch_links_step_exact(bool local, const LinksArgs& A, cudaStream_t s);
+cudaError_t launch_links_gather_exact(bool local, const LinksArgs& A, const int32_t* slot_bulk, double* out,
+                                      cudaStream_t s);
+cudaError_t launch_links_moments_exact(bool local, const LinksArgs& A, cudaStream_t s);
+// the write step's mass flux from the last step's moments (always exact)
+cudaError_t launch_links_flux(const LinksArgs& A, cudaStream_t s);
+
+// bclbm_links.cu: exact or contracting instances
+cudaError_t launch_links_step(bool exact, bool local, const LinksArgs& A, cudaStream_t s);
+cudaError_t launch_links_gather(bool exact, bool local, const LinksArgs& A, const int32_t* slot_bulk, double* out,
+                                cudaStream_t s);
+cudaError_t launch_links_moments(bool exact, bool local, const LinksArgs& A, cudaStream_t s);
+
+}  // namespace bclbm

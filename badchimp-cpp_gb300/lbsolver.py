@@ -25,7 +25,7 @@ import numpy as np
 from . import geometry as _geometry
 from . import native as _native
 
-BGK, TRT, RK = 0, 1, 2
+BGK, TRT, RK, LINKS = 0, 1, 2, 3
 F64, F32, F16, BF16 = 0, 1, 2, 3
 PRECISION = {"f64": F64, "f32": F32, "f16": F16, "bf16": BF16}
 FLAG_EXACT = 1
@@ -157,9 +157,23 @@ class Solver:
 
     def __init__(self, lat: Lattice, f_init, collision=BGK, precision=F64, tau=(1.0, 1.0), force=(0.0, 0.0, 0.0),
                  sigma=0.0, beta=0.0, flux_control=False, mom_x=0.0, rho_init=None, exact=False, sfc=False,
-                 rho_ref=1.0, store_scale=0.0, fma64=False, mass_fix=True):
+                 rho_ref=1.0, store_scale=0.0, fma64=False, mass_fix=True, tags=None, labels=None, force_on=None,
+                 rho_w=1.0):
+        """collision LINKS is the std_one_phase step (src/std_one_phase/main.cpp):
+        tags, labels (interior domains) and force_on are its node attributes [N]
+        (Nodes tags, interior_domains, force), rho_w the pressure-boundary density."""
         if isinstance(precision, str):
             precision = PRECISION[precision]
+        links = None
+        if collision == LINKS:
+            if tags is None or labels is None:
+                raise ValueError("the std_one_phase step needs tags and labels")
+            self._links = tuple(None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+                                for a in (tags, labels, force_on))
+            for a in self._links:
+                if a is not None and a.size != lat.n_nodes:
+                    raise ValueError("tags, labels and force_on have one value per node")
+            links = self._links + (float(rho_w),)
         self.lat = lat
         self.nfields = 2 if collision == RK else 1
         flags = (FLAG_EXACT if exact else 0) | (FLAG_SFC_ORDER if sfc else 0) | (FLAG_FP64_FMA if fma64 else 0) | \
@@ -169,7 +183,8 @@ class Solver:
         self._h = _native.create(lat, np.ascontiguousarray(f_init, dtype=np.float64), collision, precision, flags,
                                  tuple(float(t) for t in tau) + ((1.0,) if len(tau) == 1 else ()), F, sigma, beta,
                                  int(bool(flux_control)), mom_x, rho_ref, store_scale,
-                                 None if rho_init is None else np.ascontiguousarray(rho_init, dtype=np.float64))
+                                 None if rho_init is None else np.ascontiguousarray(rho_init, dtype=np.float64),
+                                 links)
 
     def step(self, nsteps: int = 1):
         _native.check(_native.lib().bclbm_step(self._h, int(nsteps)), self._h)
@@ -222,6 +237,13 @@ class Solver:
 
     def reduce(self) -> dict:
         return _native.reduce(self._h)
+
+    def pressure_flux(self) -> np.ndarray:
+        """std_one_phase: the write step's (q1, q2), 0.5 * sum of rho u_z over the
+        pressure-boundary nodes of each phase after the last step."""
+        q = np.zeros(2)
+        _native.check(_native.lib().bclbm_pressure_flux(self._h, _native.dp(q)), self._h)
+        return q
 
     def set_force(self, force):
         F = np.zeros(3)

@@ -42,6 +42,10 @@ class Desc(ctypes.Structure):
         ("store_scale", ctypes.c_double),
         ("f_init", ctypes.c_void_p),
         ("rho_init", ctypes.c_void_p),
+        ("tags", ctypes.c_void_p),
+        ("labels", ctypes.c_void_p),
+        ("force_on", ctypes.c_void_p),
+        ("rho_w", ctypes.c_double),
     ]
 
 
@@ -64,7 +68,7 @@ class Timing(ctypes.Structure):
 
 
 EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_step_timed", "bclbm_download_f", "bclbm_download_macros",
-           "bclbm_macros_begin", "bclbm_macros_collect", "bclbm_reduce", "bclbm_set_force", "bclbm_node_perm",
+           "bclbm_macros_begin", "bclbm_macros_collect", "bclbm_reduce", "bclbm_set_force", "bclbm_pressure_flux", "bclbm_node_perm",
            "bclbm_footprint", "bclbm_sync", "bclbm_destroy", "bclbm_error", "bclbm_last_error", "bclbm_launch_count",
            "bclbm_moments_static", "bclbm_batch_create", "bclbm_batch_admit", "bclbm_batch_admit_steps",
            "bclbm_batch_attach", "bclbm_batch_retire", "bclbm_batch_step", "bclbm_batch_stats",
@@ -107,6 +111,8 @@ def lib():
     L.bclbm_reduce.argtypes = [vp, ctypes.POINTER(Stats)]
     L.bclbm_reduce.restype = ctypes.c_int
     L.bclbm_set_force.argtypes = [vp, vp]
+    L.bclbm_pressure_flux.argtypes = [vp, vp]
+    L.bclbm_pressure_flux.restype = ctypes.c_int
     L.bclbm_set_force.restype = ctypes.c_int
     L.bclbm_node_perm.argtypes = [vp, vp]
     L.bclbm_node_perm.restype = ctypes.c_int
@@ -203,7 +209,7 @@ def check(rc: int, handle=None, batch=None, output=None):
 
 
 def make_desc(lat, f_init, collision, precision, flags, tau, force, sigma, beta, flux_control, mom_x, rho_ref,
-              store_scale, rho_init):
+              store_scale, rho_init, links=None):
     d = Desc()
     d.lattice_q = lat.nq
     d.n_nodes = lat.n_nodes
@@ -226,13 +232,19 @@ def make_desc(lat, f_init, collision, precision, flags, tau, force, sigma, beta,
     d.store_scale = float(store_scale)
     d.f_init = f_init.ctypes.data if f_init is not None else None
     d.rho_init = rho_init.ctypes.data if rho_init is not None else None
+    if links is not None:  # (tags, labels, force_on or None, rho_w): int32 [N] arrays the caller keeps alive
+        tags, labels, force_on, rho_w = links
+        d.tags = tags.ctypes.data
+        d.labels = labels.ctypes.data
+        d.force_on = force_on.ctypes.data if force_on is not None else None
+        d.rho_w = float(rho_w)
     return d
 
 
 def create(lat, f_init, collision, precision, flags, tau, force, sigma, beta, flux_control, mom_x, rho_ref,
-           store_scale, rho_init):
+           store_scale, rho_init, links=None):
     d = make_desc(lat, f_init, collision, precision, flags, tau, force, sigma, beta, flux_control, mom_x, rho_ref,
-                  store_scale, rho_init)
+                  store_scale, rho_init, links)
     h = ctypes.c_void_p()
     rc = lib().bclbm_create(ctypes.byref(d), ctypes.byref(h))
     check(rc)

@@ -57,6 +57,11 @@ extern "C" {
 #define BCLBM_BGK 0 /* calcOmegaBGK + calcDeltaOmegaF          (src/lbsolver/LBcollision.h:27-46, 194-213) */
 #define BCLBM_TRT 1 /* calcOmegaBGKTRT + calcDeltaOmegaFTRT(phi=1) (LBcollision.h:50-75, 215-236) */
 #define BCLBM_RK 2  /* Rothman-Keller two-phase step of src/twophase/main_TWOPHASE.cpp:238-392 */
+#define BCLBM_LINKS 3 /* the std_one_phase step (src/std_one_phase/main.cpp:470-575, D3Q19, BCLBM_F64):
+                         BGK + Guo force times the per-node force attribute, interior-domain mass
+                         sources (calcDeltaOmegaQ) and the solid-fluid, pressure (anti-bounce-back)
+                         and fluid-fluid link boundaries of the node tags; FLAG_EXACT gives the
+                         reference's rounding, else FP64 with FMA */
 
 /* population storage on the device */
 #define BCLBM_F64 0  /* plain FP64 populations; arithmetic: 64-bit fixed point with 2^-60
@@ -107,6 +112,13 @@ typedef struct {
     const double* f_init;     /* [N*nF*Q] initial populations, nF = 2 for RK else 1 */
     const double* rho_init;   /* RK: [N*2] densities; only the solid boundary entries (type 1)
                                  are read (the wettability densities); else NULL */
+    /* BCLBM_LINKS: the nodetags, interior_domains and force attributes, [N] each (entry 0
+       unused: node 0's tag is -1, as Nodes initialises it; force_on NULL = 1 everywhere),
+       and the pressure-boundary density (0: 1.0, the value main.cpp:537 passes) */
+    const int32_t* tags;
+    const int32_t* labels;
+    const int32_t* force_on;
+    double rho_w;
 } bclbm_desc;
 
 typedef struct {
@@ -154,6 +166,10 @@ int bclbm_macros_collect(bclbm_handle* h, double* rho, double* vel, double* cg);
 /* FP64 reductions over the current populations (deterministic order). */
 int bclbm_reduce(bclbm_handle* h, bclbm_stats* out);
 int bclbm_set_force(bclbm_handle* h, const double force[3]);
+/* BCLBM_LINKS: the write step's mass flux of the last step, q[phase] = 0.5 * sum of
+ * rho u_z over the pressure-boundary nodes (tag bit 16) of fluid phase 1 and 2, in
+ * node order (src/std_one_phase/main.cpp:548-562); synchronises */
+int bclbm_pressure_flux(bclbm_handle* h, double q[2]);
 /* internal node order: out[i] = reference node number of device slot i, [n_bulk] */
 int bclbm_node_perm(bclbm_handle* h, int32_t* out);
 /* device bytes held by a handle created from desc (admission by HBM footprint) */

@@ -522,3 +522,166 @@ int oracle_twophase_run(const oracle_grid* g, int nsteps, double tau0, double ta
     free(solid);
     return cur == f ? 0 : 1;
 }
+
+
+/* ---- std_one_phase (src/std_one_phase/main.cpp:24-203, 318-575) ---- */
+typedef struct {
+    const lattice_t* L;
+    const oracle_grid* g;
+    double tau;
+    const double* bf;
+    const int32_t* labels;
+    const int32_t* force_on;
+    const double* scale;
+    const double* mchange;
+    const double* add;
+    const double* f;
+    double* ftmp;
+    double* rho;
+    double* vel;
+} links_ctx;
+
+static void links_slice(void* p, int begin, int end) {
+    links_ctx* c = (links_ctx*)p;
+    const lattice_t* L = c->L;
+    double fn[19], cu[19], cF[19], vel[3], j[3], F[3];
+    for (int b = begin; b < end; ++b) {
+        const size_t node = (size_t)c->g->bulk[b];
+        memcpy(fn, c->f + node * 19, sizeof(double) * 19);
+        double rho = qsum(L, fn);
+        const int label = c->labels[node];
+        /* main.cpp:504-507 */
+        const double qm = 0.9 * 2 * c->scale[label] * c->mchange[label] * c->add[node];
+        rho += 0.5 * qm;
+        for (int d = 0; d < 3; ++d) F[d] = c->bf[d] * (double)c->force_on[node];
+        qsumc(L, fn, j);
+        for (int d = 0; d < 3; ++d) vel[d] = (j[d] + 0.5 * F[d]) / rho;
+        c->rho[node] = rho;
+        for (int d = 0; d < 3; ++d) c->vel[node * 3 + d] = vel[d];
+        const double u2 = dotv(L, vel, vel);
+        cdotall(L, vel, cu);
+        const double uF = dotv(L, vel, F);
+        cdotall(L, F, cF);
+        const double tau_inv = 1.0 / c->tau;
+        const double tf = (1 - 0.5 / c->tau);
+        const int32_t* nb = c->g->neigh + node * 19;
+        for (int q = 0; q < 19; ++q) {
+            /* calcOmegaBGK, calcDeltaOmegaF, calcDeltaOmegaQ (LBcollision.h:38-45, 80-98, 205-212) */
+            const double om = -tau_inv * (fn[q] - rho * L->w[q] * (1.0 + C2INV * cu[q] + C4INV0_5 * (cu[q] * cu[q] - C2 * u2)));
+            const double dF = L->w[q] * tf * (C2INV * cF[q] + C4INV * (cF[q] * cu[q] - C2 * uF));
+            const double dQ = tf * qm * L->w[q] * (1.0 + C2INV * cu[q] + C4INV0_5 * (cu[q] * cu[q] - C2 * u2));
+            c->ftmp[(size_t)nb[q] * 19 + q] = fn[q] + om + dF + dQ;
+        }
+    }
+}
+
+int oracle_links_run(const oracle_grid* g, int nsteps, double tau, const double* force, const int32_t* tags,
+                     const int32_t* labels, const int32_t* force_on, double rho_w, double* f, double* ftmp,
+                     double* rho, double* vel, double* flux, int nthreads) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (g->nq != 19 || !tags || !labels || !force_on) return -1;
+    lattice_t L;
+    lattice_init(&L, 19);
+    const int N = g->n_nodes;
+#define TAG(n) ((n) == 0 ? -1 : tags[(n)])
+    /* link lists (findSolidFluidLinks, findPressureFluidLinks, findFluidFluidLinks):
+     * {node, qUnknown, neighbour, qKnown} */
+    int nsf = 0, npf = 0, nff = 0, cap = 0;
+    for (int n = 1; n < N; ++n) cap += 18;
+    int32_t* sf = (int32_t*)malloc(sizeof(int32_t) * 4 * (size_t)cap);
+    int32_t* pf = (int32_t*)malloc(sizeof(int32_t) * 4 * (size_t)cap);
+    int32_t* ff = (int32_t*)malloc(sizeof(int32_t) * 4 * (size_t)cap);
+    int lmax = 0;
+    for (int n = 1; n < N; ++n)
+        if (labels[n] > lmax) lmax = labels[n];
+    double* scale = (double*)calloc((size_t)lmax + 1, sizeof(double));
+    double* mchange = (double*)calloc((size_t)lmax + 1, sizeof(double));
+    double* add = (double*)calloc((size_t)N, sizeof(double));
+    if (!sf || !pf || !ff || !scale || !mchange || !add) return -10;
+    for (int n = 1; n < N; ++n) {
+        const int t = TAG(n);
+        for (int q = 0; q < 18; ++q) {
+            const int nn = g->neigh[(size_t)n * 19 + q];
+            const int tn = TAG(nn);
+            int32_t* rec = NULL;
+            if (((t >> 3) & 1) && (tn & 3) == 0) rec = sf + 4 * nsf++;
+            if (rec) { rec[0] = n; rec[1] = L.rev[q]; rec[2] = nn; rec[3] = q; }
+            rec = NULL;
+            if (((t >> 4) & 1) && (tn & 3) == 3) rec = pf + 4 * npf++;
+            if (rec) { rec[0] = n; rec[1] = L.rev[q]; rec[2] = nn; rec[3] = q; }
+            rec = NULL;
+            if (((t >> 2) & 1) && (t & 3) == 1 && (tn & 3) == 2) rec = ff + 4 * nff++;
+            if (rec) { rec[0] = n; rec[1] = L.rev[q]; rec[2] = nn; rec[3] = q; }
+        }
+    }
+    /* interior-domain sources (main.cpp:331-358) */
+    for (int n = 1; n < N; ++n)
+        if (labels[n] > 0 && TAG(n) < 3) {
+            scale[labels[n]] += 1;
+            add[n] = 1.0;
+        }
+    for (int i = 1; i <= lmax; ++i) {
+        if (scale[i] == 0.0) return -20;
+        scale[i] = 1.0 / scale[i];
+    }
+    links_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.L = &L;
+    c.g = g;
+    c.tau = tau;
+    c.bf = force;
+    c.labels = labels;
+    c.force_on = force_on;
+    c.scale = scale;
+    c.mchange = mchange;
+    c.add = add;
+    c.rho = rho;
+    c.vel = vel;
+    double* cur = f;
+    double* nxt = ftmp;
+    for (int it = 0; it < nsteps; ++it) {
+        /* main.cpp:486-495 */
+        for (int l = 0; l <= lmax; ++l) mchange[l] = 0.0;
+        for (int b = 0; b < g->n_bulk; ++b) {
+            const int n = g->bulk[b];
+            mchange[labels[n]] += 1.0 - qsum(&L, cur + (size_t)n * 19);
+        }
+        c.f = cur;
+        c.ftmp = nxt;
+        parallel_for(g->n_bulk, nthreads, links_slice, &c);
+        double* t = cur; cur = nxt; nxt = t;
+        for (int k = 0; k < nsf; ++k) {  /* applySolidFluidBoundary */
+            const int32_t* r = sf + 4 * k;
+            cur[(size_t)r[0] * 19 + r[1]] = cur[(size_t)r[2] * 19 + r[3]];
+        }
+        for (int k = 0; k < npf; ++k) {  /* applyPressureFluidBoundary (anti-bounce-back) */
+            const int32_t* r = pf + 4 * k;
+            const double* u = vel + (size_t)r[0] * 3;
+            const double u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+            const double cu = L.c[r[3]][0] * u[0] + L.c[r[3]][1] * u[1] + L.c[r[3]][2] * u[2];
+            const double w = L.w[r[3]];
+            cur[(size_t)r[0] * 19 + r[1]] = -cur[(size_t)r[2] * 19 + r[3]] + 2 * w * rho_w * (1 + 0.5 * (C4INV * cu * cu - C2INV * u2));
+        }
+        for (int k = 0; k < nff; ++k) {  /* applyFluidFluidBoundary (its correction is 0) */
+            const int32_t* r = ff + 4 * k;
+            const double f1 = cur[(size_t)r[0] * 19 + r[1]];
+            cur[(size_t)r[0] * 19 + r[1]] = cur[(size_t)r[2] * 19 + r[3]];
+            cur[(size_t)r[2] * 19 + r[3]] = f1;
+        }
+    }
+    if (flux) {  /* main.cpp:550-562 */
+        double s[2] = {0.0, 0.0};
+        for (int n = 1; n < N; ++n)
+            if ((TAG(n) >> 4) & 1) {
+                const int ph = (TAG(n) & 3) - 1;
+                if (ph != 0 && ph != 1) return -21;
+                s[ph] += vel[(size_t)n * 3 + 2] * rho[n];
+            }
+        flux[0] = 0.5 * s[0];
+        flux[1] = 0.5 * s[1];
+    }
+#undef TAG
+    free(sf); free(pf); free(ff); free(scale); free(mchange); free(add);
+    return cur == f ? 0 : 1;
+}

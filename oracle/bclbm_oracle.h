@@ -58,6 +58,20 @@ int oracle_twophase_run(const oracle_grid* g, int nsteps, double tau0, double ta
                         double* f, double* ftmp, double* rho, double* vel, double* cg,
                         double* force_log, int nthreads);
 
+/* std_one_phase step (src/std_one_phase/main.cpp:470-575), D3Q19: BGK with the
+ * body force times the per-node force attribute, the interior-domain mass
+ * sources (calcDeltaOmegaQ) and the solid-fluid, pressure-fluid and
+ * fluid-fluid link boundaries of the node tags (main.cpp:24-203).
+ * tags, labels, force_on: the nodetags, interior_domains and force attributes,
+ * [n_nodes], entry 0 unused (node 0's tag is -1, as Nodes initialises it).
+ * rho_w: the pressure-boundary density (the reference passes 1.0).
+ * f, ftmp, the return value, rho and vel as for oracle_single_run; flux (may
+ * be NULL): the write step's q1, q2 (main.cpp:548-562) after the last step.
+ * Returns -20 if an interior domain has no source node (the reference exits). */
+int oracle_links_run(const oracle_grid* g, int nsteps, double tau, const double* force, const int32_t* tags,
+                     const int32_t* labels, const int32_t* force_on, double rho_w, double* f, double* ftmp,
+                     double* rho, double* vel, double* flux, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

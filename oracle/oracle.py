@@ -44,6 +44,9 @@ def lib():
         _lib.oracle_twophase_run.argtypes = [ctypes.POINTER(_Grid), ctypes.c_int, ctypes.c_double,
                                              ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                              ctypes.c_double, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int]
+        vp = ctypes.c_void_p
+        _lib.oracle_links_run.argtypes = [ctypes.POINTER(_Grid), ctypes.c_int, ctypes.c_double, dp, vp, vp, vp,
+                                          ctypes.c_double, dp, dp, dp, dp, dp, ctypes.c_int]
     return _lib
 
 
@@ -127,3 +130,26 @@ def twophase_run(g: OracleGrid, f, rho, nsteps, tau0, tau1, sigma, beta, force, 
     if rc < 0:
         raise RuntimeError(f"oracle_twophase_run failed with {rc}")
     return bufs[rc], rho, vel, cg, log[:int(nsteps)]
+
+
+def links_run(g: OracleGrid, f, nsteps, tau, force, tags, labels, force_on, rho_w=1.0, nthreads=1):
+    """std_one_phase loop (D3Q19) from the LbField(1,N) data f [N*19]; tags,
+    labels, force_on are the node attributes [N].  Returns (f, rho [N],
+    vel [N*3], flux [2]) with the last step's moments (rho starts at 1, vel at 0
+    at every node, as the reference initialises them)."""
+    bufs = [np.ascontiguousarray(f, dtype=np.float64).reshape(-1).copy(), None]
+    bufs[1] = np.zeros_like(bufs[0])
+    rho = np.ones(g.n_nodes)
+    vel = np.zeros(g.n_nodes * 3)
+    flux = np.zeros(2)
+    F = np.zeros(3)
+    F[:len(force)] = force
+    t = np.ascontiguousarray(tags, dtype=np.int32)
+    lab = np.ascontiguousarray(labels, dtype=np.int32)
+    fo = np.ascontiguousarray(force_on, dtype=np.int32)
+    rc = lib().oracle_links_run(ctypes.byref(g._s), int(nsteps), float(tau), _dp(F), t.ctypes.data, lab.ctypes.data,
+                                fo.ctypes.data, float(rho_w), _dp(bufs[0]), _dp(bufs[1]), _dp(rho), _dp(vel),
+                                _dp(flux), int(nthreads))
+    if rc < 0:
+        raise RuntimeError(f"oracle_links_run failed with {rc}")
+    return bufs[rc], rho, vel, flux

@@ -303,12 +303,124 @@ def make_vtu(ref: Path, name: str, nfields: int, seed: int):
     print(f"vtu_{name}.npz: {len(files)} files, {sum(len(v) for v in files.values())} bytes")
 
 
+# ---------------------------------------------------------------------------
+# std_one_phase: relative-permeability geometry with node tags (0 solid, 1 / 2
+# fluid phase, 3 pressure ghost, +4 fluid-fluid, +8 fluid-solid, +16 pressure
+# boundary), interior domains with mass sources, a force indicator and normals.
+# ---------------------------------------------------------------------------
+ONEPHASE_DIRS = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0], [1, -1, 0], [1, 0, 1], [1, 0, -1], [0, 1, 1],
+                          [0, 1, -1], [-1, 0, 0], [0, -1, 0], [0, 0, -1], [-1, -1, 0], [-1, 1, 0], [-1, 0, -1],
+                          [-1, 0, 1], [0, -1, -1], [0, -1, 1]])
+
+
+def onephase_geometry(shape, seed, ghost_layers=True):
+    """Mask (1 fluid) and voxel attributes of a periodic-in-x,y box whose z faces
+    are pressure boundaries: with ghost_layers the faces z = 0 and z = nz-1 are
+    ghost nodes (tag 3, solid); without, the fluid reaches the faces and their
+    neighbour beyond is node 0 (tag -1 in Nodes, which counts as a ghost)."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = shape
+    x, y, z = np.indices(shape)
+    mask = np.ones(shape, dtype=np.int8)
+    z0, z1 = (1, nz - 2) if ghost_layers else (0, nz - 1)
+    # phase 2: two blobs away from the pressure faces (interior domains 1 and 2),
+    # kept free of solid so that each has interior (untagged) nodes
+    blobs = [((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2 <= 3.0 ** 2)
+             for c in ((3.0, 3.0, nz / 2 - 1), (nx - 3.5, ny - 4.0, nz / 2 + 1))]
+    for _ in range(3):
+        c = rng.uniform([0, 0, z0 + 3], [nx, ny, z1 - 2])
+        d2 = sum(np.minimum(np.abs(a - ci), n - np.abs(a - ci)) ** 2 for a, ci, n in ((x, c[0], nx), (y, c[1], ny))) \
+            + (z - c[2]) ** 2
+        mask[(d2 <= 2.2 ** 2) & ~blobs[0] & ~blobs[1]] = 0
+    if ghost_layers:
+        mask[:, :, 0] = 0
+        mask[:, :, -1] = 0
+    ghost = np.zeros(shape, dtype=bool)
+    if ghost_layers:
+        ghost[:, :, 0] = ghost[:, :, -1] = True
+    phase = np.where(mask == 1, 1, 0)
+    labels = np.zeros(shape, dtype=np.int64)
+    for lab, b in enumerate(blobs, start=1):
+        blob = b & (mask == 1)
+        phase[blob] = 2
+        labels[blob] = lab
+    tags = np.where(ghost, 3, np.where(mask == 1, phase, 0)).astype(np.int64)
+    base = tags.copy()
+    for c in ONEPHASE_DIRS:
+        nb = np.roll(base, shift=(-c[0], -c[1]), axis=(0, 1))
+        # z neighbours: shifted, outside the box is node 0 (tag -1, & 3 == 3)
+        if c[2] != 0:
+            nb = np.roll(nb, shift=-c[2], axis=2)
+            if c[2] > 0:
+                nb[:, :, -1] = -1
+            else:
+                nb[:, :, 0] = -1
+        fl = mask == 1
+        other = np.where(phase == 1, 2, 1)
+        tags[fl & ((nb & 3) == other) & ((nb & 3) != 0)] |= 4
+        tags[fl & ((nb & 3) == 0) & (nb >= 0)] |= 8
+        tags[fl & ((nb & 3) == 3)] |= 16
+    force = np.where(mask == 1, 1, 0).astype(np.int64)
+    force[:, :, z0] = 0  # no body force on the first fluid layer
+    nrm = rng.normal(size=(3,) + shape)
+    nrm /= np.linalg.norm(nrm, axis=0)
+    attrs = {"nodetags": tags, "force": force, "interior_domains": labels,
+             "normal_x": nrm[0], "normal_y": nrm[1], "normal_z": nrm[2]}
+    return mask, attrs
+
+
+ONEPHASE_CASES = [
+    dict(name="onephase_ghost", shape=(10, 9, 14), seed=21, ghost_layers=True, steps=300, tau=0.9,
+         fx=2e-6, fy=0.0, fz=1e-5),
+    dict(name="onephase_open", shape=(9, 10, 12), seed=22, ghost_layers=False, steps=200, tau=0.8,
+         fx=0.0, fy=1e-6, fz=2e-5),
+]
+
+
+def make_onephase(ref: Path, case: dict):
+    drv = REPO / "oracle" / "_ref" / "ref_onephase"
+    tdrv = REPO / "oracle" / "_ref" / "ref_driver_d3q19"
+    if not drv.exists():
+        raise SystemExit(f"{drv} missing: run 'make -C oracle ref' first")
+    mask, attrs = onephase_geometry(case["shape"], case["seed"], case["ghost_layers"])
+    work = Path(tempfile.mkdtemp(prefix="bclbm_onephase_"))
+    try:
+        vtk = write_vtklb(ref, work, mask, "D3Q19", "xy", attrs)
+        tdir = work / "tables"
+        tdir.mkdir()
+        run([str(tdrv), "tables", str(vtk), str(tdir)])
+        rdir = work / "run"
+        rdir.mkdir()
+        kv = [f"{k}={case[k]!r}" for k in ("steps", "tau", "fx", "fy", "fz")]
+        msg = run([str(drv), str(vtk), str(rdir)] + kv)
+        arrays = {"mask": mask.astype(np.uint8),
+                  "neigh": np.fromfile(tdir / "neigh.i32", dtype=np.int32),
+                  "types": np.fromfile(tdir / "types.i16", dtype=np.int16),
+                  "pos": np.fromfile(tdir / "pos.i32", dtype=np.int32),
+                  "bulk": np.fromfile(tdir / "bulk.i32", dtype=np.int32)}
+        nf = arrays["bulk"].size
+        for k, v in attrs.items():
+            arrays["attr_" + k] = np.asarray(v)
+        arrays["f"] = read_lbfield(rdir / "f.lblbf")[1:nf + 1].copy()
+        arrays["rho"] = read_scalar(rdir / "rho.lbsca")[1:nf + 1].copy()
+        arrays["vel"] = read_vector(rdir / "vel.lbvec")[1:nf + 1].copy()
+        arrays["flux"] = np.array([float(v) for v in (rdir / "flux.txt").read_text().split()])
+        meta = {k: case[k] for k in ("name", "shape", "seed", "ghost_layers", "steps", "tau", "fx", "fy", "fz")}
+        meta.update(nq=19, nd=3, nf=int(nf), n_nodes=int(arrays["types"].size), periodic="xy", driver=msg.strip())
+        arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+        np.savez_compressed(HERE / f"{case['name']}.npz", **arrays)
+        print(f"{case['name']}: N={meta['n_nodes']} Nf={nf}; {msg.strip()}")
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("BCLBM_REFERENCE", "/root/reference"))
     ap.add_argument("--only", default=None)
     ap.add_argument("--pin-only", action="store_true", help="only rerun the std_case pin of config 1")
     ap.add_argument("--vtu-only", action="store_true", help="only rewrite the VTU fixtures")
+    ap.add_argument("--onephase-only", action="store_true", help="only rewrite the std_one_phase fixtures")
     args = ap.parse_args()
     ref = Path(args.reference)
     if args.pin_only:
@@ -319,6 +431,10 @@ def main():
             pin_std_case(ref, vtk, work)
         finally:
             shutil.rmtree(work, ignore_errors=True)
+        return
+    if args.onephase_only:
+        for case in ONEPHASE_CASES:
+            make_onephase(ref, case)
         return
     if args.vtu_only:
         for name, nf, seed in VTU_CASES:
@@ -331,6 +447,9 @@ def main():
     for name, nf, seed in VTU_CASES:
         if not args.only or args.only == name:
             make_vtu(ref, name, nf, seed)
+    for case in ONEPHASE_CASES:
+        if not args.only or args.only == case["name"]:
+            make_onephase(ref, case)
 
 
 if __name__ == "__main__":

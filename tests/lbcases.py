@@ -55,3 +55,42 @@ def all_runs():
         for r in meta["runs"]:
             out.append((name, r["tag"]))
     return out
+
+
+ONEPHASE_CASES = ["onephase_ghost", "onephase_open"]
+
+
+class OnephaseCase:
+    """A std_one_phase fixture: tables, node attributes (reference numbering),
+    the reference's f / rho / vel / mass flux after meta['steps'] steps."""
+
+    def __init__(self, name, bclbm):
+        self.name = name
+        self.z = np.load(GOLDEN / f"{name}.npz")
+        self.meta = json.loads(bytes(self.z["meta"]).decode())
+        self.n_nodes, self.nf = self.meta["n_nodes"], self.meta["nf"]
+        L = bclbm.lbsolver
+        self.L = L
+        self.lat = L.Lattice(19, self.z["neigh"], self.z["types"], self.z["pos"], self.z["bulk"],
+                             shape=self.z["mask"].shape, periodic="xy")
+        self.tags = self.node_attr("nodetags")
+        self.labels = self.node_attr("interior_domains")
+        self.force_on = self.node_attr("force")
+        self.force = [self.meta["fx"], self.meta["fy"], self.meta["fz"]]
+
+    def node_attr(self, name):
+        """A voxel attribute at the nodes (0 at node 0), as Nodes/LBvtk read it."""
+        v = self.z["attr_" + name]
+        out = np.zeros(self.n_nodes, dtype=np.int32 if v.dtype.kind == "i" else np.float64)
+        p = self.lat.pos.reshape(-1, 3)[1:]
+        sh = v.shape
+        out[1:] = v[p[:, 0] % sh[0], p[:, 1] % sh[1], p[:, 2] % sh[2]]
+        return out
+
+    def f_init(self):
+        """calcfeq at rho = 1, u = 0: w_q at the bulk nodes (main.cpp:457-464)."""
+        return self.L.initiate_single(self.lat, np.ones(self.n_nodes))
+
+    def solver(self, **kw):
+        return self.L.Solver(self.lat, self.f_init(), collision=self.L.LINKS, tau=(self.meta["tau"],) * 2,
+                             force=self.force, tags=self.tags, labels=self.labels, force_on=self.force_on, **kw)

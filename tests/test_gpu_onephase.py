@@ -1,0 +1,101 @@
+"""The std_one_phase step (BCLBM_LINKS) on the GPU against the reference's own
+run of src/std_one_phase/main.cpp (tests/golden/onephase_*.npz):
+
+* exact FP64 (BCLBM_FLAG_EXACT): populations, rho, u and the write step's mass
+  flux bit-identical, in reference and in Morton node order;
+* FP64 with FMA: relative L2 error <= 1e-12 in f and rho, u within 1e-12 of
+  max |u|, mass flux within 1e-10;
+* the set-up errors: a link without a boundary rule, an interior domain
+  without source nodes, combinations that are not built."""
+
+import numpy as np
+import pytest
+
+import lbcases
+
+pytestmark = pytest.mark.gpu
+
+
+def relerr(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
+def run(c, steps, pieces=1, **kw):
+    with c.solver(**kw) as s:
+        left = steps
+        for k in range(pieces):
+            n = left // (pieces - k)
+            s.step(n)
+            left -= n
+        f = s.download_f()
+        rho, vel, _ = s.download_macros()
+        flux = s.pressure_flux()
+        st = s.reduce()
+        perm = s.node_perm()
+    b = c.lat.bulk
+    return {"f": f.reshape(-1, 19)[b], "rho": rho[b], "vel": vel.reshape(-1, 3)[b], "flux": flux, "stats": st,
+            "perm": perm}
+
+
+@pytest.mark.parametrize("sfc", [False, True], ids=["refOrder", "morton"])
+@pytest.mark.parametrize("name", lbcases.ONEPHASE_CASES)
+def test_exact_matches_reference(bclbm, gpu, name, sfc):
+    c = lbcases.OnephaseCase(name, bclbm)
+    got = run(c, c.meta["steps"], exact=True, sfc=sfc)
+    assert np.array_equal(got["f"], c.z["f"][:, 0, :])
+    assert np.array_equal(got["rho"], c.z["rho"][:, 0])
+    assert np.array_equal(got["vel"], c.z["vel"][:, 0, :])
+    assert np.array_equal(got["flux"], c.z["flux"])
+    assert np.array_equal(np.sort(got["perm"]), c.lat.bulk)
+
+
+@pytest.mark.parametrize("name", lbcases.ONEPHASE_CASES)
+def test_exact_in_pieces_and_stats(bclbm, gpu, name):
+    """Steps taken in several calls (the velocity store and the moments carry
+    over) give the same state; the sums of bclbm_reduce are those of f."""
+    c = lbcases.OnephaseCase(name, bclbm)
+    got = run(c, c.meta["steps"], pieces=3, exact=True)
+    assert np.array_equal(got["f"], c.z["f"][:, 0, :])
+    assert np.array_equal(got["flux"], c.z["flux"])
+    st = got["stats"]
+    fe = c.z["f"][:, 0, :]
+    assert abs(st["mass"][0] - fe.sum()) <= 1e-13 * fe.sum()
+    cx = np.array([1, 0, 0, 1, 1, 1, 1, 0, 0, -1, 0, 0, -1, -1, -1, -1, 0, 0, 0])
+    jx = (fe * cx).sum()
+    assert abs(st["flux_fc"][0] - jx) <= 1e-12 * np.abs(fe * cx).sum()
+
+
+@pytest.mark.parametrize("name", lbcases.ONEPHASE_CASES)
+def test_fma_within_1e12(bclbm, gpu, name):
+    c = lbcases.OnephaseCase(name, bclbm)
+    got = run(c, c.meta["steps"])
+    assert relerr(got["f"], c.z["f"][:, 0, :]) <= 1e-12
+    assert relerr(got["rho"], c.z["rho"][:, 0]) <= 1e-12
+    ve = c.z["vel"][:, 0, :]
+    assert np.abs(got["vel"] - ve).max() <= 1e-12 * np.abs(ve).max()
+    assert np.abs(got["flux"] - c.z["flux"]).max() <= 1e-10 * np.abs(c.z["flux"]).max()
+
+
+def test_setup_errors(bclbm, gpu):
+    N = bclbm.native
+    c = lbcases.OnephaseCase("onephase_ghost", bclbm)
+    # a fluid node next to a solid without the fluid-solid bit: no rule for that link
+    nb = c.z["neigh"].reshape(-1, 19)
+    t = c.tags.copy()
+    n = next(int(n) for n in c.lat.bulk if (t[n] >> 3) & 1)
+    t[n] &= ~8
+    with pytest.raises(N.BclbmError) as e:
+        c.L.Solver(c.lat, c.f_init(), collision=c.L.LINKS, tags=t, labels=c.labels, force_on=c.force_on)
+    assert e.value.status == -2
+    # an interior domain whose nodes all carry interface bits: no source node
+    lab = c.labels.copy()
+    iface = [int(n) for n in c.lat.bulk if t[n] >= 3 and lab[n] == 0]
+    lab[iface[0]] = 3
+    with pytest.raises(N.BclbmError) as e:
+        c.L.Solver(c.lat, c.f_init(), collision=c.L.LINKS, tags=c.tags, labels=lab, force_on=c.force_on)
+    assert e.value.status == -1
+    # shifted storage is not built for this step
+    with pytest.raises(N.BclbmError) as e:
+        c.solver(precision="f32")
+    assert e.value.status == -5
+    assert nb.shape[1] == 19
