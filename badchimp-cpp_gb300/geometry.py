@@ -53,6 +53,75 @@ def lattice_name(q: int) -> str:
     raise ValueError(f"unsupported lattice with {q} directions")
 
 
+def tagged_pack(shape, radius: float, porosity: float, seed: int, blob_radius: float = 5.0,
+                blob_spacing: int = 24, ghost_layers: bool = True):
+    """A synthetic input of the std_one_phase step (src/std_one_phase/main.cpp):
+    a box periodic in x and y whose z faces are pressure boundaries, with the
+    node attributes that step reads, as voxel arrays.  The reference's own
+    inputs are level-set phase distributions in rock images, which are not
+    available; this stands in for them.
+
+    * mask: a periodic sphere pack (``sphere_pack``); with ghost_layers the
+      faces z = 0 and z = nz-1 are pressure ghost nodes (solid, tag 3);
+    * phase 2: balls of ``blob_radius`` on a regular grid of spacing
+      ``blob_spacing`` inside the box, each an interior domain (label 1, 2, ...)
+      when it has at least one node without interface bits; phase 1 elsewhere;
+    * nodetags: 0 solid, 1 / 2 fluid phase, 3 pressure ghost, +4 next to the
+      other phase, +8 next to a solid, +16 next to a pressure ghost (D3Q19
+      neighbours; beyond the z faces the neighbour is node 0, tag -1);
+    * force: 1 on fluid, 0 on solid; interior_domains: the labels.
+
+    Returns (mask, attrs) with int32 arrays ``nodetags``, ``interior_domains``
+    and ``force`` of the mask's shape."""
+    shape = tuple(int(n) for n in shape)
+    nx, ny, nz = shape
+    mask = sphere_pack(shape, radius, porosity, seed)[0].copy()
+    ghost = np.zeros(shape, dtype=bool)
+    if ghost_layers:
+        mask[:, :, 0] = 0
+        mask[:, :, -1] = 0
+        ghost[:, :, 0] = ghost[:, :, -1] = True
+    fluid = mask == 1
+    phase = np.where(fluid, 1, 0).astype(np.int64)
+    labels = np.zeros(shape, dtype=np.int64)
+    x, y, z = (np.arange(n) for n in shape)
+    h = blob_spacing
+    cz = np.arange(h // 2 + 2, nz - h // 2 - 1, h)
+    blobs = [(a, b, c) for a in range(h // 2, nx, h) for b in range(h // 2, ny, h) for c in cz]
+    r2 = float(blob_radius) ** 2
+    ri = int(np.ceil(blob_radius))
+    for k, (a, b, c) in enumerate(blobs, start=1):
+        sx, sy, sz = (slice(max(v - ri, 0), min(v + ri + 1, n)) for v, n in ((a, nx), (b, ny), (c, nz)))
+        d2 = (x[sx, None, None] - a) ** 2 + (y[None, sy, None] - b) ** 2 + (z[None, None, sz] - c) ** 2
+        sel = (d2 <= r2) & fluid[sx, sy, sz]
+        phase[sx, sy, sz][sel] = 2
+        labels[sx, sy, sz][sel] = k
+    tags = np.where(ghost, 3, phase).astype(np.int64)
+    base = tags.copy()
+    other = np.where(phase == 1, 2, 1)
+    for c in D3Q19_C[:18]:
+        nb = np.roll(base, shift=(-c[0], -c[1]), axis=(0, 1))
+        if c[2] != 0:
+            nb = np.roll(nb, shift=-c[2], axis=2)
+            if c[2] > 0:
+                nb[:, :, -1] = -1
+            else:
+                nb[:, :, 0] = -1
+        tags[fluid & ((nb & 3) == other) & ((nb & 3) != 0)] |= 4
+        tags[fluid & ((nb & 3) == 0) & (nb >= 0)] |= 8
+        tags[fluid & ((nb & 3) == 3)] |= 16
+    # drop the labels of blobs that have no interior (untagged) node
+    present = np.unique(labels[labels > 0])
+    keep = np.unique(labels[(labels > 0) & (tags < 3)])
+    remap = np.zeros(int(labels.max()) + 1, dtype=np.int64)
+    remap[keep] = np.arange(1, keep.size + 1)
+    labels = remap[labels]
+    del present
+    attrs = {"nodetags": tags.astype(np.int32), "interior_domains": labels.astype(np.int32),
+             "force": fluid.astype(np.int32)}
+    return mask, attrs
+
+
 def channel_2d(nx: int = 256, ny: int = 64) -> np.ndarray:
     """2D channel: solid rows y=0 and y=ny-1, fluid in between (x periodic by the caller)."""
     geo = np.ones((nx, ny), dtype=np.int8)

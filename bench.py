@@ -25,6 +25,10 @@ serving       (rank 0) a sample of the serving workload: --requests permeability
 
   python bench.py --workload serving [--requests R --rates 0,2,5]
   prints the serving measurement as the bench line (solves/s).
+
+  python bench.py --workload links [--size 192]
+  the std_one_phase step (link boundaries from node tags, interior-domain mass
+  sources) on a tagged sphere pack: FP64 FMA and exact kernels, oracle on the host.
 """
 
 from __future__ import annotations
@@ -577,6 +581,101 @@ def run_twophase(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def links_bytes(lat, tags, labels):
+    """Algorithmic bytes of one std_one_phase step: every fluid node reads its 19
+    pulled populations, 18 table entries, its info word and force attribute and
+    writes 19 populations; the labelled nodes are read once more by the mass pass
+    (plus their list entry and the 1 - rho written); the pressure-boundary nodes
+    read and write their velocity (and read its index)."""
+    b = lat.bulk
+    nlab = int(np.count_nonzero(labels[b] > 0))
+    npress = int(np.count_nonzero((tags[b] >> 4) & 1))
+    per = 2 * 19 * 8 + 18 * 4 + 4 + 4
+    return lat.n_bulk * per + nlab * (19 * 8 + 18 * 4 + 4 + 4 + 8) + npress * (4 + 48), nlab, npress
+
+
+def run_links(args, world, rank):
+    """--workload links: the std_one_phase step (interior-domain mass sources and
+    the solid / pressure / fluid-fluid link boundaries of the node tags) on a
+    tagged sphere pack: FP64 with FMA (the line's value) and the reference-order
+    exact FP64 kernel, against the oracle on the host cores."""
+    import __graft_entry__ as ge
+    bclbm = ge.load()
+    L = bclbm.lbsolver
+    if rank != 0:
+        return
+    t = time.time()
+    mask, attrs = bclbm.geometry.tagged_pack((args.size,) * 3, args.radius, args.porosity, args.seed)
+    lat = L.Lattice.from_geometry(mask, "D3Q19", "xy")
+    tags, labels, fon = (lat.attribute(attrs[k]).astype(np.int32) for k in ("nodetags", "interior_domains", "force"))
+    phi = float(mask[:, :, 1:-1].mean())
+    log(f"tagged pack {args.size}^3: porosity {phi:.4f}, fluid {lat.n_bulk}, nodes {lat.n_nodes}, "
+        f"{labels.max()} interior domains ({time.time() - t:.1f}s)")
+    f0 = L.initiate_single(lat, np.ones(lat.n_nodes))
+    force = (args.gx, 0.0, args.gx)
+    peak, peak_kind = peaks()
+    nbytes, nlab, npress = links_bytes(lat, tags, labels)
+    res, fs = {}, {}
+    l0 = bclbm.native.launch_count()
+    with ClockSampler(0) as clk:
+        for name, exact in (("f64-fma", False), ("f64-exact", True)):
+            with L.Solver(lat, f0, collision=L.LINKS, tau=(args.tau, args.tau), force=force, tags=tags,
+                          labels=labels, force_on=fon, exact=exact) as s:
+                tm = time_solver(s, args.steps, args.warmup)
+                fs[name] = s.download_f()
+                q = s.pressure_flux()
+            mlups = lat.n_bulk * args.steps / (tm["total_ms"] * 1e-3) / 1e6
+            ach = nbytes / (tm["step_kernel_ms"] / args.steps * 1e-3) / 1e9
+            res[name] = {"mlups": mlups, "ms_per_step": tm["total_ms"] / args.steps, "achieved_gbs": ach,
+                         "frac": ach / peak, "mass_flux": [float(v) for v in q]}
+            log(f"{name}: {mlups:.0f} MLUPS, {ach:.0f} GB/s ({ach / peak:.3f}), flux {q}")
+    launches = bclbm.native.launch_count() - l0
+    a, b = fs["f64-fma"].reshape(-1, 19)[lat.bulk], fs["f64-exact"].reshape(-1, 19)[lat.bulk]
+    rel = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    cpu = None
+    if not args.no_cpu:
+        sys.path.insert(0, str(REPO / "oracle"))
+        import oracle
+        n = max(24, args.size // 4)
+        m2, a2 = bclbm.geometry.tagged_pack((n,) * 3, args.radius / 4 + 1, args.porosity, args.seed)
+        l2 = L.Lattice.from_geometry(m2, "D3Q19", "xy")
+        t2, lb2, fo2 = (l2.attribute(a2[k]).astype(np.int32) for k in ("nodetags", "interior_domains", "force"))
+        g = oracle.OracleGrid(19, l2.neigh, l2.types, l2.bulk)
+        nth = oracle.default_threads()
+        steps2 = 2
+        t0 = time.time()
+        oracle.links_run(g, L.initiate_single(l2, np.ones(l2.n_nodes)), steps2, args.tau, force, t2, lb2, fo2,
+                         nthreads=nth)
+        dt = time.time() - t0
+        steps2 = max(2, int(steps2 * min(args.cpu_seconds / max(dt, 1e-3), 200)))
+        t0 = time.time()
+        oracle.links_run(g, L.initiate_single(l2, np.ones(l2.n_nodes)), steps2, args.tau, force, t2, lb2, fo2,
+                         nthreads=nth)
+        dt = time.time() - t0
+        cpu = {"value": l2.n_bulk * steps2 / dt / 1e6, "unit": "MLUPS", "cores": nth, "kind": "port",
+               "sample": f"oracle (C restatement of src/std_one_phase/main.cpp:470-575) on a {n}^3 tagged pack, "
+                         f"{l2.n_bulk} fluid nodes, {steps2} steps, {dt:.1f} s"}
+    head = res["f64-fma"]
+    line = {
+        "metric": METRIC, "value": head["mlups"], "unit": "MLUPS", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded sphere pack with phase-2 blobs and node tags (numpy default_rng), no dataset",
+        "config": {"workload": f"D3Q19 std_one_phase step, {args.size}^3 sphere pack radius {args.radius:g} periodic "
+                               f"in x, y with pressure-ghost z faces, porosity {phi:.4f}, tau {args.tau:g}, "
+                               f"force ({args.gx:g}, 0, {args.gx:g})",
+                   "fluid_nodes": lat.n_bulk, "labelled_nodes": nlab, "pressure_nodes": npress,
+                   "interior_domains": int(labels.max()), "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "achieved": head["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": head["frac"], "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "k_links_mass + k_links_label_sum + k_links_collide (one step)",
+                     "bytes_per_step": nbytes, "units_per_launch": lat.n_bulk},
+        "variants": res, "fma_vs_exact_rel_l2_f": rel, "cpu_baseline": cpu, "clocks": clk.summary(),
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -600,7 +699,7 @@ def main():
                     help="steps of the FP64 / FP32 / FP16 / BF16 permeability comparison (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sample of the pack workload line")
-    ap.add_argument("--workload", default="pack", choices=["pack", "serving", "twophase"],
+    ap.add_argument("--workload", default="pack", choices=["pack", "serving", "twophase", "links"],
                     help="pack: the 256^3 sphere-pack time step; serving: the request loop; twophase: the "
                          "Rothman-Keller step (use --size 192 --radius 8 for the 192^3 case)")
     ap.add_argument("--tp-steps", type=int, default=20000, help="twophase: total steps of the accuracy run")
@@ -634,6 +733,8 @@ def main():
             run_serving(args, world, rank)
         elif args.workload == "twophase":
             run_twophase(args, world, rank)
+        elif args.workload == "links":
+            run_links(args, world, rank)
         else:
             run_mine(args, world, rank)
     if world > 1:

@@ -74,6 +74,15 @@ struct TwoPhase {
     double store_scale = 0.0;
 };
 
+/* std_one_phase: relaxation time, body force and the pressure-boundary density
+ * (main.cpp:537 passes 1.0); flags BCLBM_FLAG_EXACT for the reference's rounding. */
+struct OnePhaseLinks {
+    double tau;
+    std::array<double, 3> force;
+    double rho_w = 1.0;
+    uint32_t flags = 0;
+};
+
 [[noreturn]] inline void adaptor_fail(const std::string& what) {
 #ifdef BCLBM_ADAPTOR_THROW
     throw std::runtime_error(what);
@@ -160,6 +169,44 @@ public:
         d.f_init = &f(0, 0, 0);
         d.rho_init = &rho(0, 0);
         create(d);
+    }
+
+    /* std_one_phase (src/std_one_phase/main.cpp:239-575): the node tags are read
+     * through Nodes::getTag, the interior-domain labels and the force indicator
+     * as main.cpp:284-305 stores them */
+    template <class GridT, class NodesT>
+    LbStep(const GridT& grid, const NodesT& nodes, const std::vector<int>& bulkNodes, const LbField<DXQY>& f,
+           const std::vector<int>& interiorDomainsLabel, const ScalarField& forceOn, const OnePhaseLinks& p)
+        : tab_(grid, nodes, bulkNodes), nfields_(1) {
+        const int N = grid.size();
+        if (f.num_fields() != 1 || static_cast<int>(interiorDomainsLabel.size()) != N)
+            adaptor_fail("bclbm: std_one_phase takes one LbField field and a label per node");
+        std::vector<int32_t> tags(static_cast<size_t>(N), -1), labels(interiorDomainsLabel.begin(),
+                                                                      interiorDomainsLabel.end()),
+            force(static_cast<size_t>(N), 0);
+        for (int n = 1; n < N; ++n) {
+            tags[static_cast<size_t>(n)] = nodes.getTag(n);
+            force[static_cast<size_t>(n)] = static_cast<int32_t>(forceOn(0, n));
+        }
+        bclbm_desc d = base_desc(N);
+        d.collision = BCLBM_LINKS;
+        d.precision = BCLBM_F64;
+        d.flags = p.flags;
+        d.tau[0] = d.tau[1] = p.tau;
+        for (int k = 0; k < 3; ++k) d.force[k] = p.force[k];
+        d.f_init = &f(0, 0, 0);
+        d.tags = tags.data();
+        d.labels = labels.data();
+        d.force_on = force.data();
+        d.rho_w = p.rho_w;
+        create(d);
+    }
+
+    /* std_one_phase: the write step's q1, q2 (main.cpp:548-562) of the last step */
+    std::array<double, 2> pressure_flux() const {
+        std::array<double, 2> q{};
+        adaptor_check(bclbm_pressure_flux(h_, q.data()), h_, "bclbm_pressure_flux");
+        return q;
     }
 
     LbStep(const LbStep&) = delete;

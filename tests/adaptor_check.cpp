@@ -93,6 +93,18 @@ int main(int argc, char** argv) {
     } catch (const std::runtime_error& e) {
         std::printf("status %s\n", e.what());
     }
+    // the std_one_phase constructor (node tags from Nodes::getTag; none are set here,
+    // so every tag is the -1 Nodes starts with)
+    try {
+        ScalarField forceOn(1, grid.size());
+        std::vector<int> labels(grid.size(), 0);
+        bclbm::LbStep<LT> links(grid, nodes, bulkNodes, f, labels, forceOn, bclbm::OnePhaseLinks{0.8, {0.0, 0.0, 1e-5}});
+        links.run(2);
+        const auto q = links.pressure_flux();
+        std::printf("links ran %.17g\n", q[0]);
+    } catch (const std::runtime_error& e) {
+        std::printf("links status %s\n", e.what());
+    }
     MPI_Finalize();
     return 0;
 }
