@@ -78,8 +78,8 @@ int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full)
         return BCLBM_ERR_INVALID;
     }
     if (d->collision < BCLBM_BGK || d->collision > BCLBM_LINKS) { err = "unknown collision"; return BCLBM_ERR_INVALID; }
-    if (d->collision == BCLBM_LINKS && (Q != 19 || d->precision != BCLBM_F64)) {
-        err = "BCLBM_LINKS (the std_one_phase step) is D3Q19 with BCLBM_F64";
+    if (d->collision == BCLBM_LINKS && Q != 19) {
+        err = "BCLBM_LINKS (the std_one_phase step) is D3Q19";
         return BCLBM_ERR_UNSUPPORTED;
     }
     if (d->collision == BCLBM_LINKS && (!d->tags || !d->labels)) {
@@ -358,6 +358,8 @@ LinksArgs links_args(const bclbm_handle* h, const StepArgs& a) {
     A.flux_phase = h->d_flux_phase;
     A.nflux = h->nflux;
     A.flux_out = h->d_flux_out;
+    A.f_rho_w = static_cast<float>(h->rho_w);
+    A.f_dw = static_cast<float>(2.0 * (h->rho_w - h->rho_ref));
     return A;
 }
 
@@ -443,8 +445,8 @@ int run_gather(bclbm_handle* h) {
     StepArgs a = make_args(h);
     a.src = h->pops[h->cur];
     if (h->collision == BCLBM_LINKS) {
-        CUDA_TRY(h, launch_links_gather(h->exact, !h->state_post, links_args(h, a), h->d_slot_bulk, h->d_gather,
-                                        h->stream));
+        CUDA_TRY(h, launch_links_gather(h->precision, h->exact, !h->state_post, links_args(h, a), h->d_slot_bulk,
+                                        h->d_gather, h->stream));
         return BCLBM_OK;
     }
     CUDA_TRY(h, launch_gather(h->q, h->fx_storage ? kFX : h->precision, h->nfields, !h->state_post, a, h->d_slot_bulk,
@@ -831,7 +833,7 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
         a.vel_out = macros ? h->d_vel : nullptr;
         if (h->collision == BCLBM_LINKS) {
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
-            CUDA_TRY(h, launch_links_step(h->exact, local, links_args(h, a), h->stream));
+            CUDA_TRY(h, launch_links_step(h->precision, h->exact, local, links_args(h, a), h->stream));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
         } else if (h->collision != BCLBM_RK) {
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
@@ -998,7 +1000,7 @@ int bclbm_reduce(bclbm_handle* h, bclbm_stats* out) {
     StepArgs a = make_args(h);
     a.src = h->pops[h->cur];
     if (h->collision == BCLBM_LINKS)
-        CUDA_TRY(h, launch_links_moments(h->exact, !h->state_post, links_args(h, a), h->stream));
+        CUDA_TRY(h, launch_links_moments(h->precision, h->exact, !h->state_post, links_args(h, a), h->stream));
     else
         CUDA_TRY(h, launch_moments(h->q, h->fx_storage ? kFX : h->precision, h->nfields, !h->state_post, a, h->stream));
     CUDA_TRY(h, launch_reduce_final(6, h->d_partials, grid_for(h->nf), h->d_red, true, h->stream));

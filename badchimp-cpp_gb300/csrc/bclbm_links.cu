@@ -183,15 +183,56 @@ cudaError_t step_fma(const LinksArgs& A, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <class S, bool LOCAL>
+cudaError_t step_shift(const LinksArgs& A, cudaStream_t s) {
+    if (A.nlabeled > 0) {
+        k_links_mass_shift<S, LOCAL><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
+        k_links_label_sum<false><<<(A.nlab * 32 + kBlock - 1) / kBlock, kBlock, 0, s>>>(A);
+        launch_counter() += 2;
+    }
+    k_links_collide_shift<S, LOCAL><<<grid_for(A.s.L.nf), kBlock, 0, s>>>(A);
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t shift_s(int what, bool local, const LinksArgs& A, const int32_t* slot_bulk, double* out, cudaStream_t s) {
+    const int g = grid_for(A.s.L.nf);
+    switch (what) {
+        case 0: return local ? step_shift<S, true>(A, s) : step_shift<S, false>(A, s);
+        case 1:
+            if (local) k_links_gather_shift<S, true><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
+            else k_links_gather_shift<S, false><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
+            break;
+        default:
+            if (local) k_links_moments_shift<S, true><<<g, kBlock, 0, s>>>(A);
+            else k_links_moments_shift<S, false><<<g, kBlock, 0, s>>>(A);
+    }
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+cudaError_t shift(int precision, int what, bool local, const LinksArgs& A, const int32_t* slot_bulk, double* out,
+                  cudaStream_t s) {
+    switch (precision) {
+        case kF32: return shift_s<float>(what, local, A, slot_bulk, out, s);
+        case kF16: return shift_s<__half>(what, local, A, slot_bulk, out, s);
+        case kBF16: return shift_s<__nv_bfloat16>(what, local, A, slot_bulk, out, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
 }  // namespace
 
-cudaError_t launch_links_step(bool exact, bool local, const LinksArgs& A, cudaStream_t s) {
+cudaError_t launch_links_step(int precision, bool exact, bool local, const LinksArgs& A, cudaStream_t s) {
+    if (precision != kF64) return shift(precision, 0, local, A, nullptr, nullptr, s);
     if (exact) return launch_links_step_exact(local, A, s);
     return local ? step_fma<true>(A, s) : step_fma<false>(A, s);
 }
 
-cudaError_t launch_links_gather(bool exact, bool local, const LinksArgs& A, const int32_t* slot_bulk, double* out,
-                                cudaStream_t s) {
+cudaError_t launch_links_gather(int precision, bool exact, bool local, const LinksArgs& A, const int32_t* slot_bulk,
+                                double* out, cudaStream_t s) {
+    if (precision != kF64) return shift(precision, 1, local, A, slot_bulk, out, s);
     if (exact) return launch_links_gather_exact(local, A, slot_bulk, out, s);
     const int g = grid_for(A.s.L.nf);
     if (local) k_links_gather<false, true><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
@@ -200,7 +241,8 @@ cudaError_t launch_links_gather(bool exact, bool local, const LinksArgs& A, cons
     return cudaGetLastError();
 }
 
-cudaError_t launch_links_moments(bool exact, bool local, const LinksArgs& A, cudaStream_t s) {
+cudaError_t launch_links_moments(int precision, bool exact, bool local, const LinksArgs& A, cudaStream_t s) {
+    if (precision != kF64) return shift(precision, 2, local, A, nullptr, nullptr, s);
     if (exact) return launch_links_moments_exact(local, A, s);
     const int g = grid_for(A.s.L.nf);
     if (local) k_links_moments<false, true><<<g, kBlock, 0, s>>>(A);

@@ -44,6 +44,8 @@ struct LinksArgs {
     const int32_t* flux_phase;  // [nflux] their fluid phase (0 or 1)
     int nflux;
     double* flux_out;           // [2]
+    float f_rho_w;              // shifted storage: rho_w and 2 (rho_w - rho_ref) in FP32
+    float f_dw;
 };
 
 // the populations that stream into slot i: plain pulls, bounce-back, and the
@@ -230,6 +232,180 @@ __global__ void __launch_bounds__(kBlock) k_links_moments(LinksArgs A) {
         vals[2] = j[0];
         vals[3] = j[1];
         vals[4] = j[2];
+        vals[5] = mx;
+    }
+    block_reduce_store<6>(vals, A.s.partials, true);
+}
+
+// ---------------------------------------------------------------------------
+// Shifted storage (F32 / F16 / BF16) with FP32 arithmetic on the deviations
+// d_q = f_q - w_q rho_ref; the stored value is d_q * scale / w_q.
+// ---------------------------------------------------------------------------
+template <class S, bool LOCAL>
+__device__ __forceinline__ void load_links_shift(const S* __restrict__ g, const LinksArgs& A, int i, const float* u,
+                                                 float* fd) {
+    constexpr int Q = 19, R = Lat<Q>::REST;
+    const LatticeView& L = A.s.L;
+    const size_t pad = static_cast<size_t>(L.nf_pad);
+    const float is = A.s.f_inv_scale;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const float wq = static_cast<float>(Lat<Q>::w(q));
+        if (LOCAL || q == R) {
+            fd[q] = Store<S>::val(g[static_cast<size_t>(q) * pad + i]) * (wq * is);
+            continue;
+        }
+        const int e = __ldg(L.pull + static_cast<size_t>(q) * pad + i);
+        if (e >= 0) {
+            fd[q] = Store<S>::val(g[e]) * (wq * is);  // reversed directions have the same weight
+        } else {
+            // f = -f_k + 2 w rho_w (1 + (9 cu^2 - 3 u^2)/2)  ->  d = -d_k + w (2 (rho_w - rho_ref) + rho_w (9 cu^2 - 3 u^2))
+            const int k = Lat<Q>::rev(q);
+            const float dk = Store<S>::val(g[~e]) * (wq * is);
+            const float u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+            const float cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];
+            fd[q] = -dk + wq * (A.f_dw + A.f_rho_w * (9.0f * cu * cu - 3.0f * u2));
+        }
+    }
+}
+
+template <bool LOCAL>
+__device__ __forceinline__ void links_velocity_f(const LinksArgs& A, int i, uint32_t inf, float* u) {
+    u[0] = u[1] = u[2] = 0.0f;
+    if (!LOCAL && (inf & kLinkPress)) {
+        const int p = __ldg(A.pidx + i);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) u[d] = static_cast<float>(A.ustore[static_cast<size_t>(d) * A.npress + p]);
+    }
+}
+
+// the collision of collide_links on deviations: feq - w rho_ref = w (drho + rho (3 cu + 4.5 cu^2 - 1.5 u^2))
+__device__ __forceinline__ void collide_links_shift(float* fd, const LinksArgs& A, int i, uint32_t inf, float& drho_o,
+                                                    float* vel_o) {
+    constexpr int Q = 19;
+    const StepArgs& a = A.s;
+    float dr = 0.0f;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) dr += fd[q];
+    const float qs = (inf & kLinkAdd) ? static_cast<float>(A.lab_q[inf & kLinkLabelMask]) : 0.0f;
+    dr += 0.5f * qs;
+    const float rho = a.f_rho_ref + dr;
+    const float fo = static_cast<float>(__ldg(A.force_on + i));
+    float F[3], j[3] = {0.0f, 0.0f, 0.0f}, vel[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) F[d] = a.params->forcef[d] * fo;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        j[0] += Lat<Q>::cx(q) * fd[q];
+        j[1] += Lat<Q>::cy(q) * fd[q];
+        j[2] += Lat<Q>::cz(q) * fd[q];
+    }
+    const float irho = 1.0f / rho;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) vel[d] = (j[d] + 0.5f * F[d]) * irho;
+    drho_o = dr;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) vel_o[d] = vel[d];
+    const float u2 = vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2];
+    const float uF = vel[0] * F[0] + vel[1] * F[1] + vel[2] * F[2];
+    const float oms = a.f_tau_inv, tf = a.f_tf;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const float w = static_cast<float>(Lat<Q>::w(q));
+        const float cu = Lat<Q>::cx(q) * vel[0] + Lat<Q>::cy(q) * vel[1] + Lat<Q>::cz(q) * vel[2];
+        const float cF = Lat<Q>::cx(q) * F[0] + Lat<Q>::cy(q) * F[1] + Lat<Q>::cz(q) * F[2];
+        const float sh = 3.0f * cu + 4.5f * cu * cu - 1.5f * u2;
+        const float eq = w * (dr + rho * sh);
+        const float dF = w * tf * (3.0f * cF + 9.0f * cF * cu - 3.0f * uF);
+        const float dQ = tf * qs * w * (1.0f + sh);
+        fd[q] = fd[q] - oms * (fd[q] - eq) + dF + dQ;
+    }
+}
+
+template <class S, bool LOCAL>
+__global__ void __launch_bounds__(kBlock) k_links_mass_shift(LinksArgs A) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.nlabeled) return;
+    const int i = __ldg(A.lab_slot + k);
+    const uint32_t inf = __ldg(A.info + i);
+    float u[3], fd[19];
+    links_velocity_f<LOCAL>(A, i, inf, u);
+    load_links_shift<S, LOCAL>(static_cast<const S*>(A.s.src), A, i, u, fd);
+    float dr = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) dr += fd[q];
+    A.lab_val[k] = (1.0 - A.s.rho_ref) - static_cast<double>(dr);
+}
+
+// resident blocks per SM asked of the register allocator for the shifted step (192^3
+// tagged pack, F32 / F16 MLUPS: 3 blocks 15.7k / 17.1k, 4: 17.6k / 18.7k, 5: 18.3k / 20.4k,
+// 6: 17.4k / 18.7k)
+#ifndef BCLBM_LINKS_MINB
+#define BCLBM_LINKS_MINB 5
+#endif
+
+template <class S, bool LOCAL>
+__global__ void __launch_bounds__(kBlock, BCLBM_LINKS_MINB) k_links_collide_shift(LinksArgs A) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.s.L.nf) return;
+    const uint32_t inf = __ldg(A.info + i);
+    float u[3], fd[19], dr, vel[3];
+    links_velocity_f<LOCAL>(A, i, inf, u);
+    load_links_shift<S, LOCAL>(static_cast<const S*>(A.s.src), A, i, u, fd);
+    collide_links_shift(fd, A, i, inf, dr, vel);
+    const size_t pad = static_cast<size_t>(A.s.L.nf_pad);
+    S* out = static_cast<S*>(A.s.dst);
+    const float sc = A.s.f_scale;
+#pragma unroll
+    for (int q = 0; q < 19; ++q)
+        Store<S>::store(out + static_cast<size_t>(q) * pad + i, fd[q] * (sc / static_cast<float>(Lat<19>::w(q))));
+    if (inf & kLinkPress) {
+        const int p = __ldg(A.pidx + i);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) A.ustore[static_cast<size_t>(d) * A.npress + p] = vel[d];
+    }
+    if (A.s.rho_out) {
+        A.s.rho_out[i] = A.s.rho_ref + static_cast<double>(dr);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) A.s.vel_out[static_cast<size_t>(d) * pad + i] = vel[d];
+    }
+}
+
+template <class S, bool LOCAL>
+__global__ void __launch_bounds__(kBlock) k_links_gather_shift(LinksArgs A, const int32_t* __restrict__ slot_bulk,
+                                                               double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.s.L.nf) return;
+    const uint32_t inf = __ldg(A.info + i);
+    float u[3], fd[19];
+    links_velocity_f<LOCAL>(A, i, inf, u);
+    load_links_shift<S, LOCAL>(static_cast<const S*>(A.s.src), A, i, u, fd);
+    const size_t b = static_cast<size_t>(slot_bulk[i]);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) out[b * 19 + q] = Lat<19>::w(q) * A.s.rho_ref + static_cast<double>(fd[q]);
+}
+
+template <class S, bool LOCAL>
+__global__ void __launch_bounds__(kBlock) k_links_moments_shift(LinksArgs A) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double vals[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (i < A.s.L.nf) {
+        const uint32_t inf = __ldg(A.info + i);
+        float u[3], fd[19];
+        links_velocity_f<LOCAL>(A, i, inf, u);
+        load_links_shift<S, LOCAL>(static_cast<const S*>(A.s.src), A, i, u, fd);
+        double mx = 0.0, dr = 0.0;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const double d = static_cast<double>(fd[q]);
+            dr += d;
+            vals[2] += Lat<19>::cx(q) * d;
+            vals[3] += Lat<19>::cy(q) * d;
+            vals[4] += Lat<19>::cz(q) * d;
+            const double af = fabs(Lat<19>::w(q) * A.s.rho_ref + d);
+            mx = (af != af || isinf(af)) ? CUDART_INF : fmax(mx, af);
+        }
+        vals[0] = A.s.rho_ref + dr;
         vals[5] = mx;
     }
     block_reduce_store<6>(vals, A.s.partials, true);

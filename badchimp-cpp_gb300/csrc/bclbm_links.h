@@ -37,10 +37,11 @@ cudaError_t launch_links_moments_exact(bool local, const LinksArgs& A, cudaStrea
 // the write step's mass flux from the last step's moments (always exact)
 cudaError_t launch_links_flux(const LinksArgs& A, cudaStream_t s);
 
-// bclbm_links.cu: exact or contracting instances
-cudaError_t launch_links_step(bool exact, bool local, const LinksArgs& A, cudaStream_t s);
-cudaError_t launch_links_gather(bool exact, bool local, const LinksArgs& A, const int32_t* slot_bulk, double* out,
-                                cudaStream_t s);
-cudaError_t launch_links_moments(bool exact, bool local, const LinksArgs& A, cudaStream_t s);
+// bclbm_links.cu: F64 exact or contracting instances, or the shifted storage formats
+// (precision BCLBM_F32 / F16 / BF16, FP32 arithmetic)
+cudaError_t launch_links_step(int precision, bool exact, bool local, const LinksArgs& A, cudaStream_t s);
+cudaError_t launch_links_gather(int precision, bool exact, bool local, const LinksArgs& A, const int32_t* slot_bulk,
+                                double* out, cudaStream_t s);
+cudaError_t launch_links_moments(int precision, bool exact, bool local, const LinksArgs& A, cudaStream_t s);
 
 }  // namespace bclbm

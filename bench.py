@@ -26,6 +26,9 @@ serving       (rank 0) a sample of the serving workload: --requests permeability
   python bench.py --workload serving [--requests R --rates 0,2,5]
   prints the serving measurement as the bench line (solves/s).
 
+  python bench.py --workload output [--size 256 --write-every 1000 --writes 4]
+  the std_case loop with VTU output steps, synchronous against asynchronous writes.
+
   python bench.py --workload links [--size 192]
   the std_one_phase step (link boundaries from node tags, interior-domain mass
   sources) on a tagged sphere pack: FP64 FMA and exact kernels, oracle on the host.
@@ -581,7 +584,7 @@ def run_twophase(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def links_bytes(lat, tags, labels):
+def links_bytes(lat, tags, labels, sf=8):
     """Algorithmic bytes of one std_one_phase step: every fluid node reads its 19
     pulled populations, 18 table entries, its info word and force attribute and
     writes 19 populations; the labelled nodes are read once more by the mass pass
@@ -590,8 +593,8 @@ def links_bytes(lat, tags, labels):
     b = lat.bulk
     nlab = int(np.count_nonzero(labels[b] > 0))
     npress = int(np.count_nonzero((tags[b] >> 4) & 1))
-    per = 2 * 19 * 8 + 18 * 4 + 4 + 4
-    return lat.n_bulk * per + nlab * (19 * 8 + 18 * 4 + 4 + 4 + 8) + npress * (4 + 48), nlab, npress
+    per = 2 * 19 * sf + 18 * 4 + 4 + 4
+    return lat.n_bulk * per + nlab * (19 * sf + 18 * 4 + 4 + 4 + 8) + npress * (4 + 48), nlab, npress
 
 
 def run_links(args, world, rank):
@@ -618,20 +621,26 @@ def run_links(args, world, rank):
     res, fs = {}, {}
     l0 = bclbm.native.launch_count()
     with ClockSampler(0) as clk:
-        for name, exact in (("f64-fma", False), ("f64-exact", True)):
-            with L.Solver(lat, f0, collision=L.LINKS, tau=(args.tau, args.tau), force=force, tags=tags,
-                          labels=labels, force_on=fon, exact=exact) as s:
+        for name, exact, prec in (("f64-fma", False, "f64"), ("f64-exact", True, "f64"), ("f32", False, "f32"),
+                                  ("f16", False, "f16")):
+            with L.Solver(lat, f0, collision=L.LINKS, precision=prec, tau=(args.tau, args.tau), force=force,
+                          tags=tags, labels=labels, force_on=fon, exact=exact) as s:
                 tm = time_solver(s, args.steps, args.warmup)
                 fs[name] = s.download_f()
                 q = s.pressure_flux()
             mlups = lat.n_bulk * args.steps / (tm["total_ms"] * 1e-3) / 1e6
-            ach = nbytes / (tm["step_kernel_ms"] / args.steps * 1e-3) / 1e9
+            nb_prec = links_bytes(lat, tags, labels, {"f64": 8, "f32": 4, "f16": 2}[prec])[0]
+            ach = nb_prec / (tm["step_kernel_ms"] / args.steps * 1e-3) / 1e9
             res[name] = {"mlups": mlups, "ms_per_step": tm["total_ms"] / args.steps, "achieved_gbs": ach,
-                         "frac": ach / peak, "mass_flux": [float(v) for v in q]}
+                         "frac": ach / peak, "bytes_per_step": nb_prec, "mass_flux": [float(v) for v in q]}
             log(f"{name}: {mlups:.0f} MLUPS, {ach:.0f} GB/s ({ach / peak:.3f}), flux {q}")
     launches = bclbm.native.launch_count() - l0
-    a, b = fs["f64-fma"].reshape(-1, 19)[lat.bulk], fs["f64-exact"].reshape(-1, 19)[lat.bulk]
-    rel = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    ex = fs["f64-exact"].reshape(-1, 19)[lat.bulk]
+    rel = {k: float(np.linalg.norm(v.reshape(-1, 19)[lat.bulk] - ex) / np.linalg.norm(ex)) for k, v in fs.items()
+           if k != "f64-exact"}
+    qex = res["f64-exact"]["mass_flux"][0]
+    for k in res:
+        res[k]["mass_flux_rel_err"] = abs(res[k]["mass_flux"][0] - qex) / abs(qex) if qex else None
     cpu = None
     if not args.no_cpu:
         sys.path.insert(0, str(REPO / "oracle"))
@@ -647,7 +656,7 @@ def run_links(args, world, rank):
         oracle.links_run(g, L.initiate_single(l2, np.ones(l2.n_nodes)), steps2, args.tau, force, t2, lb2, fo2,
                          nthreads=nth)
         dt = time.time() - t0
-        steps2 = max(2, int(steps2 * min(args.cpu_seconds / max(dt, 1e-3), 200)))
+        steps2 = max(2, int(steps2 * min(args.cpu_seconds / max(dt, 1e-3), 5000)))
         t0 = time.time()
         oracle.links_run(g, L.initiate_single(l2, np.ones(l2.n_nodes)), steps2, args.tau, force, t2, lb2, fo2,
                          nthreads=nth)
@@ -670,8 +679,78 @@ def run_links(args, world, rank):
                      "frac": head["frac"], "traffic": None, "peak_kind": peak_kind,
                      "kernel": "k_links_mass + k_links_label_sum + k_links_collide (one step)",
                      "bytes_per_step": nbytes, "units_per_launch": lat.n_bulk},
-        "variants": res, "fma_vs_exact_rel_l2_f": rel, "cpu_baseline": cpu, "clocks": clk.summary(),
+        "variants": res, "rel_l2_f_vs_exact": rel, "cpu_baseline": cpu, "clocks": clk.summary(),
         "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_output(args, world, rank):
+    """--workload output: the std_case loop with an output step every --write-every
+    steps (download of the device moments into the fields the VTU writer reads,
+    then the write), synchronous against asynchronous writes; the line's value
+    is the MLUPS of the asynchronous loop including the writes."""
+    import shutil
+    import tempfile
+    bclbm, lat, phi = build_workload(args.size, args.radius, args.porosity, args.seed)
+    if rank != 0:
+        return
+    L = bclbm.lbsolver
+    f0 = L.initiate_single(lat, np.ones(lat.n_nodes))
+    rho = np.zeros((lat.n_nodes, 1))
+    vel = np.zeros((lat.n_nodes, 1, 3))
+    W, nw = args.write_every, args.writes
+    root = Path(tempfile.mkdtemp(prefix="bclbm_vtu_"))
+    res = {}
+    l0 = bclbm.native.launch_count()
+    try:
+        with ClockSampler(0) as clk, L.Solver(lat, f0, tau=(args.tau, args.tau), force=(args.gx, 0, 0)) as s:
+            s.step(args.warmup)
+            s.sync()
+            for mode in ("steps_only", "sync", "async", "writes_only"):
+                d = root / mode
+                d.mkdir()
+                with bclbm.output.Output(lat, lat.bulk, d) as o:
+                    o.add_file("lb_run")
+                    o.add_scalar_variables(["rho"], [rho])
+                    o.add_vector_variables(["vel"], [vel])
+                    t0 = time.perf_counter()
+                    for k in range(nw):
+                        if mode != "writes_only":
+                            s.step(W)
+                        if mode == "steps_only":
+                            s.sync()
+                            continue
+                        s.download_macros(rho.reshape(-1), vel.reshape(-1))
+                        if mode == "async":
+                            o.write_async(k)
+                        else:
+                            o.write(k)
+                    if mode == "async":
+                        o.wait()
+                    s.sync()
+                    res[mode] = time.perf_counter() - t0
+                nbytes = sum(p.stat().st_size for p in d.rglob("*") if p.is_file())
+                res[mode + "_bytes"] = nbytes
+                shutil.rmtree(d, ignore_errors=True)
+                log(f"{mode}: {res[mode]:.3f} s ({nbytes / 1e6:.0f} MB written)")
+    finally:
+        shutil.rmtree(root, ignore_errors=True)
+    launches = bclbm.native.launch_count() - l0
+    steps = W * nw
+    mlups = {m: lat.n_bulk * steps / res[m] / 1e6 for m in ("steps_only", "sync", "async")}
+    hidden = (res["sync"] - res["async"]) / max(res["writes_only"], 1e-9)
+    line = {
+        "metric": METRIC, "value": mlups["async"], "unit": "MLUPS", "n_gpus": 1, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": res["async"] / steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded periodic sphere pack (numpy default_rng), no dataset",
+        "config": {"workload": f"D3Q19 BGK periodic {args.size}^3 sphere pack, FP64 step, an output step (rho, vel "
+                               f"VTU, Float64, binary) every {W} steps, {nw} writes",
+                   "fluid_nodes": lat.n_bulk, "l2": "inputs larger than L2"},
+        "seconds": {k: v for k, v in res.items() if not k.endswith("_bytes")},
+        "vtu_bytes_per_write": res["sync_bytes"] // max(nw, 1), "mlups_by_mode": mlups,
+        "write_time_hidden": hidden, "clocks": clk.summary(), "gpu_launches": launches,
     }
     print(json.dumps(line), flush=True)
 
@@ -699,10 +778,12 @@ def main():
                     help="steps of the FP64 / FP32 / FP16 / BF16 permeability comparison (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sample of the pack workload line")
-    ap.add_argument("--workload", default="pack", choices=["pack", "serving", "twophase", "links"],
+    ap.add_argument("--workload", default="pack", choices=["pack", "serving", "twophase", "links", "output"],
                     help="pack: the 256^3 sphere-pack time step; serving: the request loop; twophase: the "
                          "Rothman-Keller step (use --size 192 --radius 8 for the 192^3 case)")
     ap.add_argument("--tp-steps", type=int, default=20000, help="twophase: total steps of the accuracy run")
+    ap.add_argument("--write-every", type=int, default=1000, help="output: steps between output steps")
+    ap.add_argument("--writes", type=int, default=4, help="output: output steps")
     ap.add_argument("--tp-precisions", default="f64,f16")
     ap.add_argument("--saturation", type=float, default=0.5)
     ap.add_argument("--sigma", type=float, default=0.01)
@@ -735,6 +816,8 @@ def main():
             run_twophase(args, world, rank)
         elif args.workload == "links":
             run_links(args, world, rank)
+        elif args.workload == "output":
+            run_output(args, world, rank)
         else:
             run_mine(args, world, rank)
     if world > 1:

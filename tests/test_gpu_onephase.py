@@ -5,6 +5,8 @@ run of src/std_one_phase/main.cpp (tests/golden/onephase_*.npz):
   flux bit-identical, in reference and in Morton node order;
 * FP64 with FMA: relative L2 error <= 1e-12 in f and rho, u within 1e-12 of
   max |u|, mass flux within 1e-10;
+* shifted F32 / F16 / BF16 storage with FP32 arithmetic within the tolerances
+  of test_shifted_storage;
 * the set-up errors: a link without a boundary rule, an interior domain
   without source nodes, combinations that are not built."""
 
@@ -76,6 +78,21 @@ def test_fma_within_1e12(bclbm, gpu, name):
     assert np.abs(got["flux"] - c.z["flux"]).max() <= 1e-10 * np.abs(c.z["flux"]).max()
 
 
+@pytest.mark.parametrize("prec,tol_f,tol_u,tol_q", [("f32", 1e-6, 1e-5, 1e-5), ("f16", 1e-4, 1e-3, 1e-3),
+                                                   ("bf16", 1e-3, 1e-2, 1e-2)])
+@pytest.mark.parametrize("name", lbcases.ONEPHASE_CASES)
+def test_shifted_storage(bclbm, gpu, name, prec, tol_f, tol_u, tol_q):
+    """Shifted storage with FP32 arithmetic on the deviations f - w rho_ref:
+    errors against the reference after the fixture's steps within the stated
+    tolerances (f: relative L2; u: of max |u|; mass flux: relative)."""
+    c = lbcases.OnephaseCase(name, bclbm)
+    got = run(c, c.meta["steps"], precision=prec)
+    assert relerr(got["f"], c.z["f"][:, 0, :]) <= tol_f
+    ve = c.z["vel"][:, 0, :]
+    assert np.abs(got["vel"] - ve).max() <= tol_u * np.abs(ve).max()
+    assert np.abs(got["flux"] - c.z["flux"]).max() <= tol_q * np.abs(c.z["flux"]).max()
+
+
 def test_setup_errors(bclbm, gpu):
     N = bclbm.native
     c = lbcases.OnephaseCase("onephase_ghost", bclbm)
@@ -94,8 +111,8 @@ def test_setup_errors(bclbm, gpu):
     with pytest.raises(N.BclbmError) as e:
         c.L.Solver(c.lat, c.f_init(), collision=c.L.LINKS, tags=c.tags, labels=lab, force_on=c.force_on)
     assert e.value.status == -1
-    # shifted storage is not built for this step
+    # the exact kernel is FP64 only
     with pytest.raises(N.BclbmError) as e:
-        c.solver(precision="f32")
-    assert e.value.status == -5
+        c.solver(precision="f32", exact=True)
+    assert e.value.status == -1
     assert nb.shape[1] == 19
