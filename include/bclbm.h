@@ -57,11 +57,12 @@ extern "C" {
 #define BCLBM_BGK 0 /* calcOmegaBGK + calcDeltaOmegaF          (src/lbsolver/LBcollision.h:27-46, 194-213) */
 #define BCLBM_TRT 1 /* calcOmegaBGKTRT + calcDeltaOmegaFTRT(phi=1) (LBcollision.h:50-75, 215-236) */
 #define BCLBM_RK 2  /* Rothman-Keller two-phase step of src/twophase/main_TWOPHASE.cpp:238-392 */
-#define BCLBM_LINKS 3 /* the std_one_phase step (src/std_one_phase/main.cpp:470-575, D3Q19, BCLBM_F64):
+#define BCLBM_LINKS 3 /* the std_one_phase step (src/std_one_phase/main.cpp:470-575, D3Q19):
                          BGK + Guo force times the per-node force attribute, interior-domain mass
                          sources (calcDeltaOmegaQ) and the solid-fluid, pressure (anti-bounce-back)
-                         and fluid-fluid link boundaries of the node tags; FLAG_EXACT gives the
-                         reference's rounding, else FP64 with FMA */
+                         and fluid-fluid link boundaries of the node tags.  BCLBM_F64: FP64 with FMA,
+                         or the reference's rounding with FLAG_EXACT; BCLBM_F32 / F16 / BF16: shifted
+                         storage with FP32 arithmetic on the deviations */
 
 /* population storage on the device */
 #define BCLBM_F64 0  /* plain FP64 populations; arithmetic: 64-bit fixed point with 2^-60
