@@ -54,22 +54,27 @@ cudaError_t rk_f64_q(bool local, bool flux, const StepArgs& a, cudaStream_t s, b
     return cudaGetLastError();
 }
 
-template <bool LOCAL>
-cudaError_t links_step_exact(const LinksArgs& A, cudaStream_t s) {
-    if (A.nlabeled > 0) {
-        k_links_mass<true, LOCAL><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
-        k_links_label_sum<true><<<(A.nlab + kBlock - 1) / kBlock, kBlock, 0, s>>>(A);
-        launch_counter() += 2;
-    }
-    k_links_collide<true, LOCAL><<<grid_for(A.s.L.nf), kBlock, 0, s>>>(A);
+}  // namespace
+
+cudaError_t launch_links_mass_exact(bool local, const LinksArgs& A, cudaStream_t s) {
+    if (local) k_links_mass<true, true><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
+    else k_links_mass<true, false><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
     launch_counter()++;
     return cudaGetLastError();
 }
 
-}  // namespace
+cudaError_t launch_links_label_sum_exact(const LinksArgs& A, cudaStream_t s) {
+    k_links_label_sum<true><<<(A.nlab + kBlock - 1) / kBlock, kBlock, 0, s>>>(A);
+    launch_counter()++;
+    return cudaGetLastError();
+}
 
-cudaError_t launch_links_step_exact(bool local, const LinksArgs& A, cudaStream_t s) {
-    return local ? links_step_exact<true>(A, s) : links_step_exact<false>(A, s);
+cudaError_t launch_links_collide_exact(bool local, const LinksArgs& A, cudaStream_t s) {
+    const int n = A.s.L.nf;
+    if (local) k_links_collide<true, true><<<grid_for(n), kBlock, 0, s>>>(A);
+    else k_links_collide<true, false><<<grid_for(n), kBlock, 0, s>>>(A);
+    launch_counter()++;
+    return cudaGetLastError();
 }
 
 cudaError_t launch_links_gather_exact(bool local, const LinksArgs& A, const int32_t* slot_bulk, double* out,

@@ -171,26 +171,47 @@ int links_plan(const bclbm_desc* d, const std::vector<int32_t>& slot_node, const
 
 namespace {
 
-template <bool LOCAL>
-cudaError_t step_fma(const LinksArgs& A, cudaStream_t s) {
-    if (A.nlabeled > 0) {
-        k_links_mass<false, LOCAL><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
-        k_links_label_sum<false><<<(A.nlab * 32 + kBlock - 1) / kBlock, kBlock, 0, s>>>(A);
-        launch_counter() += 2;
-    }
-    k_links_collide<false, LOCAL><<<grid_for(A.s.L.nf), kBlock, 0, s>>>(A);
+// the three parts of a step for one arithmetic (exact FP64, FMA FP64, shifted S)
+struct StepParts {
+    cudaError_t (*mass)(bool, const LinksArgs&, cudaStream_t);
+    cudaError_t (*sum)(const LinksArgs&, cudaStream_t);
+    cudaError_t (*collide)(bool, const LinksArgs&, cudaStream_t);
+};
+
+cudaError_t sum_fast(const LinksArgs& A, cudaStream_t s) {
+    k_links_label_sum<false><<<(A.nlab * 32 + kBlock - 1) / kBlock, kBlock, 0, s>>>(A);
     launch_counter()++;
     return cudaGetLastError();
 }
 
-template <class S, bool LOCAL>
-cudaError_t step_shift(const LinksArgs& A, cudaStream_t s) {
-    if (A.nlabeled > 0) {
-        k_links_mass_shift<S, LOCAL><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
-        k_links_label_sum<false><<<(A.nlab * 32 + kBlock - 1) / kBlock, kBlock, 0, s>>>(A);
-        launch_counter() += 2;
-    }
-    k_links_collide_shift<S, LOCAL><<<grid_for(A.s.L.nf), kBlock, 0, s>>>(A);
+cudaError_t mass_fma(bool local, const LinksArgs& A, cudaStream_t s) {
+    if (local) k_links_mass<false, true><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
+    else k_links_mass<false, false><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+cudaError_t collide_fma(bool local, const LinksArgs& A, cudaStream_t s) {
+    const int n = A.s.L.nf;
+    if (local) k_links_collide<false, true><<<grid_for(n), kBlock, 0, s>>>(A);
+    else k_links_collide<false, false><<<grid_for(n), kBlock, 0, s>>>(A);
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t mass_shift(bool local, const LinksArgs& A, cudaStream_t s) {
+    if (local) k_links_mass_shift<S, true><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
+    else k_links_mass_shift<S, false><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t collide_shift(bool local, const LinksArgs& A, cudaStream_t s) {
+    const int n = A.s.L.nf;
+    if (local) k_links_collide_shift<S, true><<<grid_for(n), kBlock, 0, s>>>(A);
+    else k_links_collide_shift<S, false><<<grid_for(n), kBlock, 0, s>>>(A);
     launch_counter()++;
     return cudaGetLastError();
 }
@@ -198,15 +219,12 @@ cudaError_t step_shift(const LinksArgs& A, cudaStream_t s) {
 template <class S>
 cudaError_t shift_s(int what, bool local, const LinksArgs& A, const int32_t* slot_bulk, double* out, cudaStream_t s) {
     const int g = grid_for(A.s.L.nf);
-    switch (what) {
-        case 0: return local ? step_shift<S, true>(A, s) : step_shift<S, false>(A, s);
-        case 1:
-            if (local) k_links_gather_shift<S, true><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
-            else k_links_gather_shift<S, false><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
-            break;
-        default:
-            if (local) k_links_moments_shift<S, true><<<g, kBlock, 0, s>>>(A);
-            else k_links_moments_shift<S, false><<<g, kBlock, 0, s>>>(A);
+    if (what == 1) {
+        if (local) k_links_gather_shift<S, true><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
+        else k_links_gather_shift<S, false><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
+    } else {
+        if (local) k_links_moments_shift<S, true><<<g, kBlock, 0, s>>>(A);
+        else k_links_moments_shift<S, false><<<g, kBlock, 0, s>>>(A);
     }
     launch_counter()++;
     return cudaGetLastError();
@@ -222,12 +240,32 @@ cudaError_t shift(int precision, int what, bool local, const LinksArgs& A, const
     return cudaErrorInvalidValue;
 }
 
+bool parts_for(int precision, bool exact, StepParts& P) {
+    switch (precision) {
+        case kF64:
+            P = exact ? StepParts{launch_links_mass_exact, launch_links_label_sum_exact, launch_links_collide_exact}
+                      : StepParts{mass_fma, sum_fast, collide_fma};
+            return true;
+        case kF32: P = StepParts{mass_shift<float>, sum_fast, collide_shift<float>}; return true;
+        case kF16: P = StepParts{mass_shift<__half>, sum_fast, collide_shift<__half>}; return true;
+        case kBF16:
+            P = StepParts{mass_shift<__nv_bfloat16>, sum_fast, collide_shift<__nv_bfloat16>};
+            return true;
+    }
+    return false;
+}
+
 }  // namespace
 
 cudaError_t launch_links_step(int precision, bool exact, bool local, const LinksArgs& A, cudaStream_t s) {
-    if (precision != kF64) return shift(precision, 0, local, A, nullptr, nullptr, s);
-    if (exact) return launch_links_step_exact(local, A, s);
-    return local ? step_fma<true>(A, s) : step_fma<false>(A, s);
+    StepParts P;
+    if (!parts_for(precision, exact, P)) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if (A.nlabeled > 0) {
+        if ((e = P.mass(local, A, s)) != cudaSuccess) return e;
+        if ((e = P.sum(A, s)) != cudaSuccess) return e;
+    }
+    return P.collide(local, A, s);
 }
 
 cudaError_t launch_links_gather(int precision, bool exact, bool local, const LinksArgs& A, const int32_t* slot_bulk,

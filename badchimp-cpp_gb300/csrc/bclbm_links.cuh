@@ -60,21 +60,21 @@ __device__ __forceinline__ void load_links(const double* __restrict__ g, const L
         for (int q = 0; q < Q; ++q) f[q] = g[static_cast<size_t>(q) * pad + i];
         return;
     }
-    double u2 = 0.0;
+    // table entries, then the gathers (an anti-bounce-back entry ~e reads element e), then the
+    // anti-bounce-back terms, so that the loads are in flight together
+    int e[Q - 1];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        if (q == R) {
-            f[q] = g[static_cast<size_t>(R) * pad + i];
-            continue;
-        }
-        const int e = __ldg(L.pull + static_cast<size_t>(q) * pad + i);
-        if (e >= 0) {
-            f[q] = g[e];
-        } else {
+    for (int q = 0; q < Q - 1; ++q) e[q] = __ldg(L.pull + static_cast<size_t>(q) * pad + i);
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) f[q] = g[e[q] >= 0 ? e[q] : ~e[q]];
+    f[R] = g[static_cast<size_t>(R) * pad + i];
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) {
+        if (e[q] < 0) {
             // applyPressureFluidBoundary, qUnknown = q, qKnown = rev(q)
             const int k = Lat<Q>::rev(q);
-            const double fk = g[~e];
-            u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];  // DXQY::dot
+            const double fk = f[q];
+            const double u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];  // DXQY::dot
             const double cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];  // cDotRef
             const double w = Lat<Q>::w(k);
             f[q] = -fk + 2 * w * rho_w * (1 + 0.5 * (9.0 * cu * cu - 3.0 * u2));
@@ -164,6 +164,7 @@ __global__ void k_links_label_sum(LinksArgs A) {
         const int lane = threadIdx.x & 31;
         if (l > A.nlab) return;
         double s = 0.0;
+#pragma unroll 8
         for (int k = A.lab_start[l] + lane; k < A.lab_start[l + 1]; k += 32) s += A.lab_val[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -248,24 +249,33 @@ __device__ __forceinline__ void load_links_shift(const S* __restrict__ g, const 
     const LatticeView& L = A.s.L;
     const size_t pad = static_cast<size_t>(L.nf_pad);
     const float is = A.s.f_inv_scale;
+    if constexpr (LOCAL) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            fd[q] = Store<S>::val(g[static_cast<size_t>(q) * pad + i]) * (static_cast<float>(Lat<Q>::w(q)) * is);
+        return;
+    }
+    // all table entries, then all gathers (an anti-bounce-back entry ~e reads element e), then the
+    // anti-bounce-back terms: no branch between the loads, so they are all in flight together
+    int e[Q - 1];
+    typename Store<S>::T raw[Q];
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) e[q] = __ldg(L.pull + static_cast<size_t>(q) * pad + i);
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) raw[q] = g[e[q] >= 0 ? e[q] : ~e[q]];
+    raw[R] = g[static_cast<size_t>(R) * pad + i];
+    const float u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const float wq = static_cast<float>(Lat<Q>::w(q));
-        if (LOCAL || q == R) {
-            fd[q] = Store<S>::val(g[static_cast<size_t>(q) * pad + i]) * (wq * is);
-            continue;
-        }
-        const int e = __ldg(L.pull + static_cast<size_t>(q) * pad + i);
-        if (e >= 0) {
-            fd[q] = Store<S>::val(g[e]) * (wq * is);  // reversed directions have the same weight
-        } else {
+        const float wq = static_cast<float>(Lat<Q>::w(q));  // reversed directions have the same weight
+        float v = Store<S>::val(raw[q]) * (wq * is);
+        if (q != R && e[q < R ? q : 0] < 0) {
             // f = -f_k + 2 w rho_w (1 + (9 cu^2 - 3 u^2)/2)  ->  d = -d_k + w (2 (rho_w - rho_ref) + rho_w (9 cu^2 - 3 u^2))
             const int k = Lat<Q>::rev(q);
-            const float dk = Store<S>::val(g[~e]) * (wq * is);
-            const float u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
             const float cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];
-            fd[q] = -dk + wq * (A.f_dw + A.f_rho_w * (9.0f * cu * cu - 3.0f * u2));
+            v = -v + wq * (A.f_dw + A.f_rho_w * (9.0f * cu * cu - 3.0f * u2));
         }
+        fd[q] = v;
     }
 }
 
@@ -279,47 +289,67 @@ __device__ __forceinline__ void links_velocity_f(const LinksArgs& A, int i, uint
     }
 }
 
-// the collision of collide_links on deviations: feq - w rho_ref = w (drho + rho (3 cu + 4.5 cu^2 - 1.5 u^2))
+// the collision of collide_links on deviations, regrouped by direction pairs
+// (k, k + 9): with drho' = sum d + q/2, rho = rho_ref + drho', G = oms rho + tsf q,
+//   X = w (G (4.5 cu^2 - 1.5 u^2) + oms drho' + tsf q + tsf (9 cF cu - 3 uF))
+//   Y = 3 w (G cu + tsf cF)
+//   d*_k = (1 - oms) d_k + X + Y,   d*_{k+9} = (1 - oms) d_{k+9} + X - Y
+// which is calcOmegaBGK + calcDeltaOmegaF + calcDeltaOmegaQ of the node loop.
 __device__ __forceinline__ void collide_links_shift(float* fd, const LinksArgs& A, int i, uint32_t inf, float& drho_o,
                                                     float* vel_o) {
-    constexpr int Q = 19;
+    constexpr int Q = 19, NP = Lat<Q>::NP, R = Lat<Q>::REST;
     const StepArgs& a = A.s;
-    float dr = 0.0f;
+    float p[NP], m[NP];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) dr += fd[q];
+    for (int k = 0; k < NP; ++k) {
+        p[k] = fd[k] + fd[k + NP];
+        m[k] = fd[k] - fd[k + NP];
+    }
+    float dr = fd[R];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) dr += p[k];
+    float j[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        if (Lat<Q>::cx(k) > 0) j[0] += m[k];
+        if (Lat<Q>::cx(k) < 0) j[0] -= m[k];
+        if (Lat<Q>::cy(k) > 0) j[1] += m[k];
+        if (Lat<Q>::cy(k) < 0) j[1] -= m[k];
+        if (Lat<Q>::cz(k) > 0) j[2] += m[k];
+        if (Lat<Q>::cz(k) < 0) j[2] -= m[k];
+    }
     const float qs = (inf & kLinkAdd) ? static_cast<float>(A.lab_q[inf & kLinkLabelMask]) : 0.0f;
     dr += 0.5f * qs;
     const float rho = a.f_rho_ref + dr;
     const float fo = static_cast<float>(__ldg(A.force_on + i));
-    float F[3], j[3] = {0.0f, 0.0f, 0.0f}, vel[3];
+    float F[3], u[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) F[d] = a.params->forcef[d] * fo;
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        j[0] += Lat<Q>::cx(q) * fd[q];
-        j[1] += Lat<Q>::cy(q) * fd[q];
-        j[2] += Lat<Q>::cz(q) * fd[q];
-    }
     const float irho = 1.0f / rho;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) vel[d] = (j[d] + 0.5f * F[d]) * irho;
+    for (int d = 0; d < 3; ++d) u[d] = (j[d] + 0.5f * F[d]) * irho;
     drho_o = dr;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) vel_o[d] = vel[d];
-    const float u2 = vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2];
-    const float uF = vel[0] * F[0] + vel[1] * F[1] + vel[2] * F[2];
-    const float oms = a.f_tau_inv, tf = a.f_tf;
+    for (int d = 0; d < 3; ++d) vel_o[d] = u[d];
+    const float u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    const float uF = u[0] * F[0] + u[1] * F[1] + u[2] * F[2];
+    const float oms = a.f_tau_inv, tsf = a.f_tf;
+    const float G = oms * rho + tsf * qs;
+    const float base = -1.5f * u2;
+    const float K0 = oms * dr + tsf * qs - 3.0f * tsf * uF;
+    const float keep = 1.0f - oms;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        const float w = static_cast<float>(Lat<Q>::w(q));
-        const float cu = Lat<Q>::cx(q) * vel[0] + Lat<Q>::cy(q) * vel[1] + Lat<Q>::cz(q) * vel[2];
-        const float cF = Lat<Q>::cx(q) * F[0] + Lat<Q>::cy(q) * F[1] + Lat<Q>::cz(q) * F[2];
-        const float sh = 3.0f * cu + 4.5f * cu * cu - 1.5f * u2;
-        const float eq = w * (dr + rho * sh);
-        const float dF = w * tf * (3.0f * cF + 9.0f * cF * cu - 3.0f * uF);
-        const float dQ = tf * qs * w * (1.0f + sh);
-        fd[q] = fd[q] - oms * (fd[q] - eq) + dF + dQ;
+    for (int k = 0; k < NP; ++k) {
+        const float w = static_cast<float>(Lat<Q>::w(k));
+        const float cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];
+        const float cF = Lat<Q>::cx(k) * F[0] + Lat<Q>::cy(k) * F[1] + Lat<Q>::cz(k) * F[2];
+        const float X = w * (G * (4.5f * cu * cu + base) + (9.0f * tsf * cF) * cu + K0);
+        const float Y = 3.0f * w * (G * cu + tsf * cF);
+        const float fq = fd[k], fr = fd[k + NP];
+        fd[k] = keep * fq + (X + Y);
+        fd[k + NP] = keep * fr + (X - Y);
     }
+    fd[R] = keep * fd[R] + static_cast<float>(Lat<Q>::w(R)) * (G * base + K0);
 }
 
 template <class S, bool LOCAL>
