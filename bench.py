@@ -584,6 +584,17 @@ def run_twophase(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def links_traffic(n_fluid):
+    """DRAM bytes of one k_links_collide launch (FP64 FMA) from the committed ncu
+    capture, scaled by the fluid nodes, or None."""
+    f = REPO / "profiles" / "traffic.json"
+    try:
+        bpn = json.loads(f.read_text())["k_links_collide_d3q19_f64_fma"]["bytes_per_node"]
+        return int(bpn * n_fluid)
+    except Exception:
+        return None
+
+
 def links_bytes(lat, tags, labels, sf=8):
     """Algorithmic bytes of one std_one_phase step: every fluid node reads its 19
     pulled populations, 18 table entries, its info word and force attribute and
@@ -676,7 +687,7 @@ def run_links(args, world, rank):
                    "fluid_nodes": lat.n_bulk, "labelled_nodes": nlab, "pressure_nodes": npress,
                    "interior_domains": int(labels.max()), "l2": "inputs larger than L2"},
         "roofline": {"bound": "hbm", "achieved": head["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                     "frac": head["frac"], "traffic": None, "peak_kind": peak_kind,
+                     "frac": head["frac"], "traffic": links_traffic(lat.n_bulk), "peak_kind": peak_kind,
                      "kernel": "k_links_mass + k_links_label_sum + k_links_collide (one step)",
                      "bytes_per_step": nbytes, "units_per_launch": lat.n_bulk},
         "variants": res, "rel_l2_f_vs_exact": rel, "cpu_baseline": cpu, "clocks": clk.summary(),
