@@ -556,8 +556,18 @@ __device__ __forceinline__ void load_rk(const S* __restrict__ g, const LatticeVi
 // per-block sums of qSumC(f0 + f1)[0] for the flux controller (:292-298) and,
 // for shifted storage, of the node totals sum_q (f0 + f1) - rho_ref and
 // sum_q (f0 - f1) for the mass-drift correction.
+// resident blocks per SM asked of the register allocator by the shifted two-phase passes
+// (192^3 pack, F16 / F32 MLUPS: no hint 7,935 / 7,026 (4 and 3 blocks); 4 + 4: 8,532 / 7,810;
+// 5 + 4: 8,170 / 7,503; 6 + 4: 7,754 / 7,055; 5 + 3: 8,225 / 6,882)
+#ifndef BCLBM_RK_DENS_MINB
+#define BCLBM_RK_DENS_MINB 4
+#endif
+#ifndef BCLBM_RK_COLL_MINB
+#define BCLBM_RK_COLL_MINB 4
+#endif
+
 template <int Q, class S, bool LOCAL, bool SUMS>
-__global__ void __launch_bounds__(kBlock) k_rk_density(StepArgs a) {
+__global__ void __launch_bounds__(kBlock, (Store<S>::shifted ? BCLBM_RK_DENS_MINB : 1)) k_rk_density(StepArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double fx = 0.0;
     float fxf = 0.f, mt = 0.f, mc = 0.f;
@@ -714,7 +724,7 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_f64(StepArgs a) {
 // c0 X + RC and c1 X - RC become  ft'_post = X - w rho_ref  and
 // dc_post = (c0 - c1) X + 2 RC.
 template <int Q, class S, bool LOCAL>
-__global__ void __launch_bounds__(kBlock) k_rk_collide_shift(StepArgs a) {
+__global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_collide_shift(StepArgs a) {
     const bool MACROS = a.rho_out != nullptr;
     constexpr int D = Lat<Q>::D, R = Lat<Q>::REST;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
