@@ -408,6 +408,68 @@ __global__ void k_encode(const double* __restrict__ f, void* out, int nf, int nf
     }
 }
 
+// The initial populations straight from the reference's AoS rows of the bulk nodes
+// (aos [n_bulk][nfields][Q], uploaded as they are) into the storage format, slot
+// by slot: the transpose runs on the device instead of the host.
+__global__ void k_upload_aos(const double* __restrict__ aos, const int32_t* __restrict__ slot_bulk, void* out,
+                             int nf, int nf_pad, int Q, int nfields, int mode, int precision, double rho_ref,
+                             double scale, int* flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf) return;
+    const size_t es = static_cast<size_t>(nfields) * Q;
+    const double* row = aos + static_cast<size_t>(slot_bulk[i]) * es;
+    const size_t fs = static_cast<size_t>(Q) * nf_pad;
+    unsigned emax = 0;
+    for (int q = 0; q < Q; ++q) {
+        const size_t k = static_cast<size_t>(q) * nf_pad + i;
+        if (mode == 0) {  // FP64 storage
+            for (int f = 0; f < nfields; ++f) static_cast<double*>(out)[f * fs + k] = row[f * Q + q];
+            continue;
+        }
+        if (mode == 1) {  // int64 fixed point (single field)
+            static_cast<int64_t*>(out)[k] = fx::load_f64_hw(row[q], emax);
+            continue;
+        }
+        const double w = Q == 9 ? (q == 8 ? 16.0 / 36.0 : (q % 2 == 0 ? 4.0 / 36.0 : 1.0 / 36.0))
+                                : (q == 18 ? 12.0 / 36.0 : ((q % 9) < 3 ? 2.0 / 36.0 : 1.0 / 36.0));
+        double v0, v1 = 0.0;
+        if (nfields == 1) {
+            v0 = (row[q] - w * rho_ref) / w * scale;
+        } else {
+            v0 = (row[q] + row[Q + q] - w * rho_ref) / w * scale;
+            v1 = (row[q] - row[Q + q]) / w * scale;
+        }
+        switch (precision) {
+            case BCLBM_F32:
+                static_cast<float*>(out)[k] = static_cast<float>(v0);
+                if (nfields == 2) static_cast<float*>(out)[fs + k] = static_cast<float>(v1);
+                break;
+            case BCLBM_F16:
+                static_cast<__half*>(out)[k] = __double2half(v0);
+                if (nfields == 2) static_cast<__half*>(out)[fs + k] = __double2half(v1);
+                break;
+            case BCLBM_BF16:
+                static_cast<__nv_bfloat16*>(out)[k] = __double2bfloat16(v0);
+                if (nfields == 2) static_cast<__nv_bfloat16*>(out)[fs + k] = __double2bfloat16(v1);
+                break;
+        }
+    }
+    if (mode == 1 && emax >= fx::kLoadEmaxLimit) atomicOr(flag, 1);
+}
+
+// rho [nfields][pad] and vel [nd][pad] of the last step (slot order) -> the reference's
+// node-major rows of the bulk nodes: rho [n_bulk][nfields] then vel [n_bulk][nd]
+__global__ void k_macros_aos(const double* __restrict__ rho, const double* __restrict__ vel,
+                             const int32_t* __restrict__ slot_bulk, double* __restrict__ out, int nf, int nf_pad,
+                             int nfields, int nd) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nf) return;
+    const size_t b = static_cast<size_t>(slot_bulk[s]);
+    for (int k = 0; k < nfields; ++k) out[b * nfields + k] = rho[static_cast<size_t>(k) * nf_pad + s];
+    double* ov = out + static_cast<size_t>(nf) * nfields;
+    for (int d = 0; d < nd; ++d) ov[b * nd + d] = vel[static_cast<size_t>(d) * nf_pad + s];
+}
+
 void free_all(bclbm_handle* h) {
     cudaFree(h->pops[0]);
     cudaFree(h->pops[1]);
@@ -762,8 +824,31 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         CREATE_TRY(cudaStreamSynchronize(h->stream));
     }
 
-    // initial populations: reference AoS -> FP64 SoA -> storage format
-    {
+    // initial populations: reference AoS -> storage format.  The bulk nodes' rows are
+    // one contiguous block in the common case (vtklb.py numbers the fluid nodes first):
+    // upload it as it is and transpose on the device; otherwise transpose on the host.
+    if (h->bulk_contiguous) {
+        const int es = h->nfields * Q;
+        const size_t naos = static_cast<size_t>(h->nf) * es;
+        const int mode = h->fx_storage ? 1 : (h->precision == BCLBM_F64 ? 0 : 2);
+        double* tmp = nullptr;
+        CREATE_TRY(cudaMalloc(&tmp, naos * sizeof(double)));
+        cudaError_t e = cudaMemsetAsync(h->pops[0], 0, static_cast<size_t>(h->nfields) * Q * pad * store_bytes(h->precision),
+                                        h->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(tmp, d->f_init + static_cast<size_t>(h->bulk.front()) * es, naos * sizeof(double),
+                                cudaMemcpyHostToDevice, h->stream);
+        if (e == cudaSuccess) {
+            k_upload_aos<<<grid_for(h->nf), kBlock, 0, h->stream>>>(tmp, h->d_slot_bulk, h->pops[0], h->nf, h->nf_pad, Q,
+                                                                    h->nfields, mode, h->precision, h->rho_ref,
+                                                                    h->scale, &h->d_params->fx_overflow);
+            launch_counter()++;
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        cudaFree(tmp);
+        CREATE_TRY(e);
+    } else {
         const size_t nsoa = static_cast<size_t>(h->nfields) * Q * pad;
         std::vector<double> soa(nsoa, 0.0);
         const int es = h->nfields * Q;
@@ -990,6 +1075,24 @@ int bclbm_macros_collect(bclbm_handle* h, double* rho, double* vel, double* cg) 
 }
 
 int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg) {
+    if (h && h->collision != BCLBM_RK && h->bulk_contiguous && h->macros_valid && !h->stage_pending && rho && vel) {
+        // synchronous download: reorder on the device and copy the two blocks of bulk rows
+        // straight into the caller's arrays (no pinned staging, no host scatter)
+        CUDA_TRY(h, cudaSetDevice(h->device));
+        const size_t n = static_cast<size_t>(h->nf) * h->nfields * h->q;
+        if (!h->d_gather) CUDA_TRY(h, cudaMalloc(&h->d_gather, n * sizeof(double)));
+        k_macros_aos<<<grid_for(h->nf), kBlock, 0, h->stream>>>(h->d_rho, h->d_vel, h->d_slot_bulk, h->d_gather, h->nf,
+                                                                h->nf_pad, h->nfields, h->nd);
+        launch_counter()++;
+        CUDA_TRY(h, cudaGetLastError());
+        const size_t b0 = static_cast<size_t>(h->bulk.front()), nr = static_cast<size_t>(h->nf) * h->nfields;
+        CUDA_TRY(h, cudaMemcpyAsync(rho + b0 * h->nfields, h->d_gather, nr * sizeof(double), cudaMemcpyDeviceToHost,
+                                    h->stream));
+        CUDA_TRY(h, cudaMemcpyAsync(vel + b0 * h->nd, h->d_gather + nr, static_cast<size_t>(h->nf) * h->nd * sizeof(double),
+                                    cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        return BCLBM_OK;
+    }
     const int rc = bclbm_macros_begin(h);
     return rc ? rc : bclbm_macros_collect(h, rho, vel, cg);
 }
