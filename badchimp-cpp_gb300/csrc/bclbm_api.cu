@@ -217,11 +217,11 @@ int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full)
                 bad_rest.set(static_cast<int64_t>(b));
                 return;
             }
+            // y = neighbor(rev q, n) fluid must have neighbor(q, y) = n; over all q this
+            // also covers the downstream side (t = neighbor(q, n) with neighbor(rev q, t) = n)
             for (int q = 0; q < R; ++q) {
                 const int y = nbr[n * Q + rev_dir(Q, q)];
-                const int t = nbr[n * Q + q];
-                if ((y != 0 && ty[y] > 1 && nbr[static_cast<size_t>(y) * Q + q] != static_cast<int32_t>(n)) ||
-                    (t != 0 && ty[t] > 1 && nbr[static_cast<size_t>(t) * Q + rev_dir(Q, q)] != static_cast<int32_t>(n))) {
+                if (y != 0 && ty[y] > 1 && nbr[static_cast<size_t>(y) * Q + q] != static_cast<int32_t>(n)) {
                     bad_sym.set(static_cast<int64_t>(b) * 32 + q);
                     return;
                 }
