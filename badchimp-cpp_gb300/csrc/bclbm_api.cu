@@ -21,6 +21,7 @@
 #include "bclbm_host.h"
 #include "bclbm_launch.h"
 #include "bclbm_links.h"
+#include "bclbm_trace.h"
 
 using namespace bclbm;
 using bclbm::host::FirstBad;
@@ -586,6 +587,7 @@ int bclbm_footprint(const bclbm_desc* desc, size_t* bytes) {
 }
 
 int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
+    BCLBM_TRACE("bclbm_create");
     if (!out) return BCLBM_ERR_INVALID;
     *out = nullptr;
     Plan p;
@@ -905,6 +907,7 @@ namespace {
 // The step loop.  ev (optional) receives, per step, the events around the
 // density pass (RK) and around the main step kernel: ev[4 s + 0..3].
 int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
+    BCLBM_TRACE("bclbm_step");
     if (!h || nsteps < 0) return BCLBM_ERR_INVALID;
     if (nsteps == 0) return BCLBM_OK;
     CUDA_TRY(h, cudaSetDevice(h->device));
@@ -997,6 +1000,7 @@ int bclbm_sync(bclbm_handle* h) {
 }
 
 int bclbm_download_f(bclbm_handle* h, double* f) {
+    BCLBM_TRACE("bclbm_download_f");
     if (!h || !f) return BCLBM_ERR_INVALID;
     CUDA_TRY(h, cudaSetDevice(h->device));
     int rc = run_gather(h);
@@ -1075,6 +1079,7 @@ int bclbm_macros_collect(bclbm_handle* h, double* rho, double* vel, double* cg) 
 }
 
 int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg) {
+    BCLBM_TRACE("bclbm_download_macros");
     if (h && h->collision != BCLBM_RK && h->bulk_contiguous && h->macros_valid && !h->stage_pending && rho && vel) {
         // synchronous download: reorder on the device and copy the two blocks of bulk rows
         // straight into the caller's arrays (no pinned staging, no host scatter)
@@ -1098,6 +1103,7 @@ int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg)
 }
 
 int bclbm_reduce(bclbm_handle* h, bclbm_stats* out) {
+    BCLBM_TRACE("bclbm_reduce");
     if (!h || !out) return BCLBM_ERR_INVALID;
     CUDA_TRY(h, cudaSetDevice(h->device));
     StepArgs a = make_args(h);
@@ -1147,6 +1153,7 @@ int bclbm_set_force(bclbm_handle* h, const double force[3]) {
 }
 
 int bclbm_pressure_flux(bclbm_handle* h, double q[2]) {
+    BCLBM_TRACE("bclbm_pressure_flux");
     if (!h || !q) return BCLBM_ERR_INVALID;
     if (h->collision != BCLBM_LINKS) return fail(h, BCLBM_ERR_INVALID, "the mass flux is a BCLBM_LINKS output");
     if (!h->macros_valid) return fail(h, BCLBM_ERR_INVALID, "no step has run yet");

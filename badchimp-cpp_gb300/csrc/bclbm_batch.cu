@@ -38,6 +38,7 @@
 
 #include "bclbm.h"
 #include "bclbm_internal.h"
+#include "bclbm_trace.h"
 #include "bclbm_launch.h"
 
 using namespace bclbm;
@@ -439,6 +440,7 @@ int bclbm_batch_attach(bclbm_batch* b, bclbm_handle* h, int32_t* id) {
 }
 
 int bclbm_batch_admit_steps(bclbm_batch* b, const bclbm_desc* desc, int32_t first_steps, int32_t* id) {
+    BCLBM_TRACE("bclbm_batch_admit");
     if (!b || !desc || !id || first_steps < 1) return BCLBM_ERR_INVALID;
     *id = -1;
     if (desc->lattice_q != b->q || desc->collision != b->collision || desc->precision != b->precision ||
@@ -477,6 +479,7 @@ int bclbm_batch_retire(bclbm_batch* b, int32_t id) {
 }
 
 int bclbm_batch_step(bclbm_batch* b, int32_t nsteps) {
+    BCLBM_TRACE("bclbm_batch_step");
     if (!b || nsteps < 0) return BCLBM_ERR_INVALID;
     BTRY(b, cudaSetDevice(b->device));
     int rc = BCLBM_OK;
@@ -497,6 +500,7 @@ int bclbm_batch_step(bclbm_batch* b, int32_t nsteps) {
 }
 
 int bclbm_batch_stats(bclbm_batch* b, int32_t n, const int32_t* ids, bclbm_stats* out) {
+    BCLBM_TRACE("bclbm_batch_stats");
     if (!b || n < 0 || n > b->max_inst || (n > 0 && (!ids || !out))) return BCLBM_ERR_INVALID;
     if (n == 0) return BCLBM_OK;
     BTRY(b, cudaSetDevice(b->device));

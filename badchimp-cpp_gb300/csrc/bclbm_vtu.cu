@@ -38,6 +38,7 @@
 
 #include "bclbm.h"
 #include "bclbm_host.h"
+#include "bclbm_trace.h"
 
 namespace {
 
@@ -452,6 +453,7 @@ struct Snapshot {  // one write: the values of every file's variables and the wr
 };
 
 int take(bclbm_output* o, double time, Snapshot& s) {
+    BCLBM_TRACE("bclbm_output_gather");
     if (o->grid_blocks.empty()) build_grid_blocks(o);
     s.time = time;
     for (File& f : o->files) {
@@ -464,6 +466,7 @@ int take(bclbm_output* o, double time, Snapshot& s) {
 }
 
 int emit(const bclbm_output* o, const Snapshot& s, std::string& err) {
+    BCLBM_TRACE("bclbm_output_write_files");
     for (size_t k = 0; k < o->files.size(); ++k) {
         const int rc = write_file(o, o->files[k], s.nwrite[k], s.time, s.vals[k], err);
         if (rc != BCLBM_OK) return rc;
