@@ -409,6 +409,33 @@ __global__ void k_encode(const double* __restrict__ f, void* out, int nf, int nf
     }
 }
 
+struct GhostSrc {
+    int32_t v[19];
+};
+
+// The resolved pull table of a single-phase instance, built on the device from the
+// reference's neighbour rows of the bulk nodes (rows [n_bulk][Q], uploaded as they
+// are): for slot s and direction q the element (row x stride + slot) that streams
+// into s along c_q -- the upstream fluid slot, the node's own reversed value
+// (bounce-back) or the last bulk node's push into node 0.
+__global__ void k_build_pull(const int32_t* __restrict__ rows, const int32_t* __restrict__ slot_bulk,
+                             const int16_t* __restrict__ types, const int32_t* __restrict__ ext_of_node,
+                             GhostSrc ghost, int32_t* __restrict__ tab, int nf, int nf_pad, int Q) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nf) return;
+    const int32_t* row = rows + static_cast<size_t>(slot_bulk[s]) * Q;
+    const int R = Q - 1;
+    for (int q = 0; q < R; ++q) {
+        const int rq = Q == 9 ? (q + 4) % 8 : (q + 9) % 18;
+        const int y = row[rq];
+        int64_t e;
+        if (y != 0 && types[y] > 1) e = static_cast<int64_t>(q) * nf_pad + ext_of_node[y];
+        else if (y == 0) e = static_cast<int64_t>(rq) * nf_pad + ghost.v[rq];
+        else e = static_cast<int64_t>(rq) * nf_pad + s;
+        tab[static_cast<size_t>(q) * nf_pad + s] = static_cast<int32_t>(e);
+    }
+}
+
 // The initial populations straight from the reference's AoS rows of the bulk nodes
 // (aos [n_bulk][nfields][Q], uploaded as they are) into the storage format, slot
 // by slot: the transpose runs on the device instead of the host.
@@ -681,6 +708,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             if (last[pdir].load() >= 0) h->ghost_src[pdir] = slot_of_bulk[last[pdir].load()];
     }
     std::vector<int32_t> tab;
+    bool device_table = false;
     LinksPlan lp;
     if (h->collision == BCLBM_LINKS) {
         std::string lerr;
@@ -720,37 +748,78 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             delete h;
             return BCLBM_ERR_UNSUPPORTED;
         }
-        tab.assign(static_cast<size_t>(R) * pad, 0);
-        parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
-            for (size_t s = s0; s < s1; ++s) {
-                const size_t n = static_cast<size_t>(h->slot_node[s]);
-                for (int q = 0; q < R; ++q) {
-                    const int rq = rev_dir(Q, q);
-                    const int y = d->neigh[n * Q + rq];
-                    int64_t e;
-                    if (y != 0 && d->types[y] > 1) e = static_cast<int64_t>(q) * pad + p.ext_of_node[y];
-                    else if (y == 0) e = static_cast<int64_t>(rq) * pad + h->ghost_src[rq];
-                    else e = static_cast<int64_t>(rq) * pad + static_cast<int64_t>(s);
-                    tab[static_cast<size_t>(q) * pad + s] = static_cast<int32_t>(e);
+        if (h->bulk_contiguous) {
+            device_table = true;  // built by k_build_pull once the buffers exist
+        } else {
+            tab.assign(static_cast<size_t>(R) * pad, 0);
+            parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
+                for (size_t s = s0; s < s1; ++s) {
+                    const size_t n = static_cast<size_t>(h->slot_node[s]);
+                    for (int q = 0; q < R; ++q) {
+                        const int rq = rev_dir(Q, q);
+                        const int y = d->neigh[n * Q + rq];
+                        int64_t e;
+                        if (y != 0 && d->types[y] > 1) e = static_cast<int64_t>(q) * pad + p.ext_of_node[y];
+                        else if (y == 0) e = static_cast<int64_t>(rq) * pad + h->ghost_src[rq];
+                        else e = static_cast<int64_t>(rq) * pad + static_cast<int64_t>(s);
+                        tab[static_cast<size_t>(q) * pad + s] = static_cast<int32_t>(e);
+                    }
                 }
-            }
-        });
+            });
+        }
     }
     CREATE_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     const size_t sb = store_bytes(h->precision);
     const size_t pop_bytes = static_cast<size_t>(h->nfields) * Q * pad * sb;
     CREATE_TRY(cudaMalloc(&h->pops[0], pop_bytes));
     CREATE_TRY(cudaMalloc(&h->pops[1], pop_bytes));
-    CREATE_TRY(cudaMalloc(&h->d_nbr, tab.size() * sizeof(int32_t)));
+    const size_t ntab = device_table ? static_cast<size_t>(R) * pad : tab.size();
+    CREATE_TRY(cudaMalloc(&h->d_nbr, ntab * sizeof(int32_t)));
     CREATE_TRY(cudaMalloc(&h->d_slot_bulk, pad * sizeof(int32_t)));
     CREATE_TRY(cudaMalloc(&h->d_rho, static_cast<size_t>(h->nfields) * pad * sizeof(double)));
     CREATE_TRY(cudaMalloc(&h->d_vel, static_cast<size_t>(D) * pad * sizeof(double)));
     CREATE_TRY(cudaMalloc(&h->d_params, sizeof(DevParams)));
     CREATE_TRY(cudaMalloc(&h->d_partials, (static_cast<size_t>(grid_for(h->nf)) * 6 + 64) * sizeof(double)));
     CREATE_TRY(cudaMalloc(&h->d_red, 16 * sizeof(double)));
-    CREATE_TRY(cudaMemcpyAsync(h->d_nbr, tab.data(), tab.size() * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
     CREATE_TRY(cudaMemcpyAsync(h->d_slot_bulk, h->slot_bulk.data(), h->nf * sizeof(int32_t), cudaMemcpyHostToDevice,
                                h->stream));
+    if (!device_table) {
+        CREATE_TRY(cudaMemcpyAsync(h->d_nbr, tab.data(), tab.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                   h->stream));
+    } else {
+        // the bulk nodes' neighbour rows, the node types and the node -> slot map go up as
+        // they are; the table is resolved on the device
+        const size_t nrow = static_cast<size_t>(h->nf) * Q;
+        int32_t* rows = nullptr;
+        int16_t* dty = nullptr;
+        int32_t* dext = nullptr;
+        cudaError_t e = cudaMalloc(&rows, nrow * sizeof(int32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&dty, static_cast<size_t>(d->n_nodes) * sizeof(int16_t));
+        if (e == cudaSuccess) e = cudaMalloc(&dext, static_cast<size_t>(d->n_nodes) * sizeof(int32_t));
+        if (e == cudaSuccess) e = cudaMemsetAsync(h->d_nbr, 0, ntab * sizeof(int32_t), h->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(rows, d->neigh + static_cast<size_t>(h->bulk.front()) * Q, nrow * sizeof(int32_t),
+                                cudaMemcpyHostToDevice, h->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dty, d->types, static_cast<size_t>(d->n_nodes) * sizeof(int16_t),
+                                cudaMemcpyHostToDevice, h->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dext, p.ext_of_node.data(), static_cast<size_t>(d->n_nodes) * sizeof(int32_t),
+                                cudaMemcpyHostToDevice, h->stream);
+        if (e == cudaSuccess) {
+            GhostSrc g;
+            for (int k = 0; k < 19; ++k) g.v[k] = h->ghost_src[k];
+            k_build_pull<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, h->d_slot_bulk, dty, dext, g, h->d_nbr, h->nf,
+                                                                    h->nf_pad, Q);
+            launch_counter()++;
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        cudaFree(rows);
+        cudaFree(dty);
+        cudaFree(dext);
+        CREATE_TRY(e);
+    }
     DevParams prm;
     std::memset(&prm, 0, sizeof(prm));
     for (int k = 0; k < 3; ++k) {
