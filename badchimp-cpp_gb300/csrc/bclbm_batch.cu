@@ -80,10 +80,14 @@ __device__ __forceinline__ void load_inst(const BatchInst* __restrict__ inst, in
 // resident blocks per SM asked of the register allocator: the kernel arguments
 // live in shared memory, and without a bound the allocator keeps them all in
 // registers across the item loop (FP16/FP32: 85 instead of the ~62 of the
-// single-instance kernel, one block per SM fewer)
+// single-instance kernel, one block per SM fewer); 5 blocks per SM squeeze it to
+// 48 registers with spills (24-request serving sample, FP32: 27.3 -> 22.1 GLUPS)
+#ifndef BCLBM_BATCH_SHIFT_MINB
+#define BCLBM_BATCH_SHIFT_MINB 4
+#endif
 template <class S, int MODE>
 constexpr int batch_min_blocks() {
-    return MODE == 2 ? 3 : (std::is_same<S, double>::value ? 2 : 4);
+    return MODE == 2 ? 3 : (std::is_same<S, double>::value ? 2 : BCLBM_BATCH_SHIFT_MINB);
 }
 
 template <int Q, class S, int MODE, bool TRT>
