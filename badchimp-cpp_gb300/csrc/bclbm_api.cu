@@ -70,7 +70,9 @@ struct Plan {
     std::vector<int32_t> slot_node, slot_bulk, solid_node, ext_of_node;
 };
 
-int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full) {
+// full: also the stream-map checks (rest neighbour, symmetry), unless device_links:
+// bclbm_create then runs them on the device (k_check_links) from the uploaded rows
+int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full, bool device_links = false) {
     if (!d) { err = "null descriptor"; return BCLBM_ERR_INVALID; }
     const int Q = d->lattice_q;
     if (Q != 9 && Q != 19) { err = "lattice_q must be 9 or 19"; return BCLBM_ERR_INVALID; }
@@ -205,7 +207,7 @@ int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full)
     }
     p.ns = static_cast<int>(p.solid_node.size());
     p.ext_of_node[0] = nb + p.ns;
-    if (!full) return BCLBM_OK;
+    if (!full || device_links) return BCLBM_OK;
     // the reference streams rest populations to neighbor(rest, n); it must be n itself.
     // Pull equivalence: the fluid upstream neighbour pushes into this node, and this
     // node's fluid downstream neighbour pulls from it (a one-to-one stream map).
@@ -436,6 +438,30 @@ __global__ void k_build_pull(const int32_t* __restrict__ rows, const int32_t* __
     }
 }
 
+// The stream-map checks of validate_and_plan on the device, for a contiguous bulk
+// list (rows [n_bulk][Q] of nodes b0 .. b0 + n_bulk - 1): the rest neighbour of each
+// fluid node is the node itself, and a fluid upstream neighbour y = neighbor(rev q, n)
+// has neighbor(q, y) = n.  bad[0] / bad[1]: the smallest failing bulk index / b*32+q.
+__global__ void k_check_links(const int32_t* __restrict__ rows, const int16_t* __restrict__ types, int b0, int nf,
+                              int Q, int* bad) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nf) return;
+    const int n = b0 + b, R = Q - 1;
+    const int32_t* row = rows + static_cast<size_t>(b) * Q;
+    if (row[R] != n) {
+        atomicMin(bad, b);
+        return;
+    }
+    for (int q = 0; q < R; ++q) {
+        const int rq = Q == 9 ? (q + 4) % 8 : (q + 9) % 18;
+        const int y = row[rq];
+        if (y != 0 && types[y] > 1 && rows[static_cast<size_t>(y - b0) * Q + q] != n) {
+            atomicMin(bad + 1, b * 32 + q);
+            return;
+        }
+    }
+}
+
 // The initial populations straight from the reference's AoS rows of the bulk nodes
 // (aos [n_bulk][nfields][Q], uploaded as they are) into the storage format, slot
 // by slot: the transpose runs on the device instead of the host.
@@ -619,15 +645,21 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     *out = nullptr;
     Plan p;
     std::string err;
-    int rc = validate_and_plan(d, p, err, true);
+    int ndev = 0;
+    const bool have_gpu = cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0;
+    // single-phase with a contiguous bulk list on a machine with a GPU: the table is
+    // resolved and the stream map checked on the device (k_build_pull, k_check_links)
+    const bool device_links = have_gpu && d && d->bulk && d->n_bulk > 0 && d->collision != BCLBM_RK &&
+                              d->collision != BCLBM_LINKS &&
+                              static_cast<int64_t>(d->bulk[d->n_bulk - 1]) - d->bulk[0] + 1 == d->n_bulk;
+    int rc = validate_and_plan(d, p, err, true, device_links);
     if (rc) {
         std::fprintf(stderr, "bclbm_create: %s\n", err.c_str());
         return rc;
     }
     if (!d->f_init) return BCLBM_ERR_INVALID;
     if (d->collision == BCLBM_RK && !d->rho_init) return BCLBM_ERR_INVALID;
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BCLBM_ERR_NOCUDA;
+    if (!have_gpu) return BCLBM_ERR_NOCUDA;
     bclbm_handle* h = new (std::nothrow) bclbm_handle();
     if (!h) return BCLBM_ERR_NOMEM;
     h->q = d->lattice_q;
@@ -748,7 +780,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             delete h;
             return BCLBM_ERR_UNSUPPORTED;
         }
-        if (h->bulk_contiguous) {
+        if (device_links) {
             device_table = true;  // built by k_build_pull once the buffers exist
         } else {
             tab.assign(static_cast<size_t>(R) * pad, 0);
@@ -806,19 +838,36 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(dext, p.ext_of_node.data(), static_cast<size_t>(d->n_nodes) * sizeof(int32_t),
                                 cudaMemcpyHostToDevice, h->stream);
+        int* dbad = nullptr;
+        const int none[2] = {INT32_MAX, INT32_MAX};
+        int bad[2] = {INT32_MAX, INT32_MAX};
+        if (e == cudaSuccess) e = cudaMalloc(&dbad, sizeof(none));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dbad, none, sizeof(none), cudaMemcpyHostToDevice, h->stream);
         if (e == cudaSuccess) {
+            k_check_links<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, dty, h->bulk.front(), h->nf, Q, dbad);
             GhostSrc g;
             for (int k = 0; k < 19; ++k) g.v[k] = h->ghost_src[k];
             k_build_pull<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, h->d_slot_bulk, dty, dext, g, h->d_nbr, h->nf,
                                                                     h->nf_pad, Q);
-            launch_counter()++;
+            launch_counter() += 2;
             e = cudaGetLastError();
         }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(bad, dbad, sizeof(bad), cudaMemcpyDeviceToHost, h->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
         cudaFree(rows);
         cudaFree(dty);
         cudaFree(dext);
+        cudaFree(dbad);
         CREATE_TRY(e);
+        if (bad[0] != INT32_MAX || bad[1] != INT32_MAX) {
+            if (bad[0] != INT32_MAX)
+                std::fprintf(stderr, "bclbm_create: rest-direction neighbour of node %d is not the node itself\n",
+                             d->bulk[bad[0]]);
+            else
+                std::fprintf(stderr, "bclbm_create: neighbour table not symmetric at node %d direction %d\n",
+                             d->bulk[bad[1] / 32], bad[1] % 32);
+            return cleanup(BCLBM_ERR_TABLE);
+        }
     }
     DevParams prm;
     std::memset(&prm, 0, sizeof(prm));

@@ -205,3 +205,29 @@ def test_stepping_in_pieces_equals_one_call(bclbm, gpu):
         fa = a.download_f(np.zeros(case.n_nodes * case.nq))
         fb = b.download_f(np.zeros(case.n_nodes * case.nq))
     assert np.array_equal(fa, fb)
+
+
+def test_device_checks_reject_bad_tables(bclbm, gpu):
+    """With a GPU the stream-map checks of bclbm_create run on the device
+    (k_check_links): an asymmetric link and a wrong rest neighbour are still
+    BCLBM_ERR_TABLE, and the handle is not created."""
+    case = lbcases.Case("pack_20", bclbm)
+    lat = case.lat
+    L = bclbm.lbsolver
+    N = bclbm.native
+    neigh = lat.neigh.copy().reshape(-1, 19)
+    x, z = int(lat.bulk[5]), int(lat.bulk[40])
+    neigh[z, 0] = x  # a second pusher into one of x's slots
+    bad = L.Lattice(19, neigh.reshape(-1), lat.types, lat.pos, lat.bulk)
+    with pytest.raises(N.BclbmError) as e:
+        L.Solver(bad, L.initiate_single(bad, np.ones(bad.n_nodes)), tau=(0.8, 0.8))
+    assert e.value.status == -2
+    neigh = lat.neigh.copy().reshape(-1, 19)
+    neigh[int(lat.bulk[7]), 18] = int(lat.bulk[8])  # rest neighbour not the node itself
+    bad = L.Lattice(19, neigh.reshape(-1), lat.types, lat.pos, lat.bulk)
+    with pytest.raises(N.BclbmError) as e:
+        L.Solver(bad, L.initiate_single(bad, np.ones(bad.n_nodes)), tau=(0.8, 0.8))
+    assert e.value.status == -2
+    # the unmodified tables still create
+    with L.Solver(lat, L.initiate_single(lat, np.ones(lat.n_nodes)), tau=(0.8, 0.8)) as s:
+        s.step(2)
