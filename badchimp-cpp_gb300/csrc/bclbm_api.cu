@@ -825,9 +825,9 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         int32_t* rows = nullptr;
         int16_t* dty = nullptr;
         int32_t* dext = nullptr;
-        cudaError_t e = cudaMalloc(&rows, nrow * sizeof(int32_t));
-        if (e == cudaSuccess) e = cudaMalloc(&dty, static_cast<size_t>(d->n_nodes) * sizeof(int16_t));
-        if (e == cudaSuccess) e = cudaMalloc(&dext, static_cast<size_t>(d->n_nodes) * sizeof(int32_t));
+        cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&rows), nrow * sizeof(int32_t), h->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&dty), static_cast<size_t>(d->n_nodes) * sizeof(int16_t), h->stream);
+        if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&dext), static_cast<size_t>(d->n_nodes) * sizeof(int32_t), h->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(h->d_nbr, 0, ntab * sizeof(int32_t), h->stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(rows, d->neigh + static_cast<size_t>(h->bulk.front()) * Q, nrow * sizeof(int32_t),
@@ -841,7 +841,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         int* dbad = nullptr;
         const int none[2] = {INT32_MAX, INT32_MAX};
         int bad[2] = {INT32_MAX, INT32_MAX};
-        if (e == cudaSuccess) e = cudaMalloc(&dbad, sizeof(none));
+        if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&dbad), sizeof(none), h->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(dbad, none, sizeof(none), cudaMemcpyHostToDevice, h->stream);
         if (e == cudaSuccess) {
             k_check_links<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, dty, h->bulk.front(), h->nf, Q, dbad);
@@ -854,10 +854,11 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         }
         if (e == cudaSuccess) e = cudaMemcpyAsync(bad, dbad, sizeof(bad), cudaMemcpyDeviceToHost, h->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-        cudaFree(rows);
-        cudaFree(dty);
-        cudaFree(dext);
-        cudaFree(dbad);
+        // stream-ordered frees: no device-wide synchronisation while other handles run
+        if (rows) cudaFreeAsync(rows, h->stream);
+        if (dty) cudaFreeAsync(dty, h->stream);
+        if (dext) cudaFreeAsync(dext, h->stream);
+        if (dbad) cudaFreeAsync(dbad, h->stream);
         CREATE_TRY(e);
         if (bad[0] != INT32_MAX || bad[1] != INT32_MAX) {
             if (bad[0] != INT32_MAX)
@@ -952,7 +953,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         const size_t naos = static_cast<size_t>(h->nf) * es;
         const int mode = h->fx_storage ? 1 : (h->precision == BCLBM_F64 ? 0 : 2);
         double* tmp = nullptr;
-        CREATE_TRY(cudaMalloc(&tmp, naos * sizeof(double)));
+        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&tmp), naos * sizeof(double), h->stream));
         cudaError_t e = cudaMemsetAsync(h->pops[0], 0, static_cast<size_t>(h->nfields) * Q * pad * store_bytes(h->precision),
                                         h->stream);
         if (e == cudaSuccess)
@@ -966,7 +967,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-        cudaFree(tmp);
+        cudaFreeAsync(tmp, h->stream);
         CREATE_TRY(e);
     } else {
         const size_t nsoa = static_cast<size_t>(h->nfields) * Q * pad;
@@ -985,7 +986,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             CREATE_TRY(cudaStreamSynchronize(h->stream));
         } else if (h->fx_storage) {
             double* tmp = nullptr;
-            CREATE_TRY(cudaMalloc(&tmp, nsoa * sizeof(double)));
+            CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&tmp), nsoa * sizeof(double), h->stream));
             cudaError_t e = cudaMemcpyAsync(tmp, soa.data(), nsoa * sizeof(double), cudaMemcpyHostToDevice, h->stream);
             if (e == cudaSuccess) {
                 k_encode_fx<<<static_cast<unsigned>((nsoa + kBlock - 1) / kBlock), kBlock, 0, h->stream>>>(
@@ -994,11 +995,11 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
                 e = cudaGetLastError();
             }
             if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-            cudaFree(tmp);
+            cudaFreeAsync(tmp, h->stream);
             CREATE_TRY(e);
         } else {
             double* tmp = nullptr;
-            CREATE_TRY(cudaMalloc(&tmp, nsoa * sizeof(double)));
+            CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&tmp), nsoa * sizeof(double), h->stream));
             cudaError_t e = cudaMemcpyAsync(tmp, soa.data(), nsoa * sizeof(double), cudaMemcpyHostToDevice, h->stream);
             if (e == cudaSuccess) {
                 k_encode<<<grid_for(h->nf), kBlock, 0, h->stream>>>(tmp, h->pops[0], h->nf, h->nf_pad, Q, h->nfields,
@@ -1007,7 +1008,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
                 e = cudaGetLastError();
             }
             if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-            cudaFree(tmp);
+            cudaFreeAsync(tmp, h->stream);
             CREATE_TRY(e);
         }
     }
