@@ -524,31 +524,40 @@ __global__ void k_macros_aos(const double* __restrict__ rho, const double* __res
     for (int d = 0; d < nd; ++d) ov[b * nd + d] = vel[static_cast<size_t>(d) * nf_pad + s];
 }
 
+// The handle's device buffers are stream-ordered allocations on its own stream
+// (cudaMallocAsync / cudaFreeAsync): creating or destroying a handle does not
+// synchronise the device, which matters when a batch creates and retires handles
+// while other instances step (cudaFree synchronises, even for a null pointer).
+void free_dev(bclbm_handle* h, void* p) {
+    if (h->stream) cudaFreeAsync(p, h->stream);
+    else cudaFree(p);
+}
+
 void free_all(bclbm_handle* h) {
-    cudaFree(h->pops[0]);
-    cudaFree(h->pops[1]);
-    cudaFree(h->d_nbr);
-    cudaFree(h->d_slot_bulk);
-    cudaFree(h->d_rho);
-    cudaFree(h->d_vel);
-    cudaFree(h->d_cg);
-    cudaFree(h->d_cgf);
-    cudaFree(h->d_params);
-    cudaFree(h->d_partials);
-    cudaFree(h->d_red);
-    cudaFree(h->d_gather);
-    cudaFree(h->d_info);
-    cudaFree(h->d_pidx);
-    cudaFree(h->d_force_on);
-    cudaFree(h->d_ustore);
-    cudaFree(h->d_lab_slot);
-    cudaFree(h->d_lab_start);
-    cudaFree(h->d_lab_val);
-    cudaFree(h->d_lab_g);
-    cudaFree(h->d_lab_q);
-    cudaFree(h->d_flux_slot);
-    cudaFree(h->d_flux_phase);
-    cudaFree(h->d_flux_out);
+    if (h->pops[0]) free_dev(h, h->pops[0]);
+    if (h->pops[1]) free_dev(h, h->pops[1]);
+    if (h->d_nbr) free_dev(h, h->d_nbr);
+    if (h->d_slot_bulk) free_dev(h, h->d_slot_bulk);
+    if (h->d_rho) free_dev(h, h->d_rho);
+    if (h->d_vel) free_dev(h, h->d_vel);
+    if (h->d_cg) free_dev(h, h->d_cg);
+    if (h->d_cgf) free_dev(h, h->d_cgf);
+    if (h->d_params) free_dev(h, h->d_params);
+    if (h->d_partials) free_dev(h, h->d_partials);
+    if (h->d_red) free_dev(h, h->d_red);
+    if (h->d_gather) free_dev(h, h->d_gather);
+    if (h->d_info) free_dev(h, h->d_info);
+    if (h->d_pidx) free_dev(h, h->d_pidx);
+    if (h->d_force_on) free_dev(h, h->d_force_on);
+    if (h->d_ustore) free_dev(h, h->d_ustore);
+    if (h->d_lab_slot) free_dev(h, h->d_lab_slot);
+    if (h->d_lab_start) free_dev(h, h->d_lab_start);
+    if (h->d_lab_val) free_dev(h, h->d_lab_val);
+    if (h->d_lab_g) free_dev(h, h->d_lab_g);
+    if (h->d_lab_q) free_dev(h, h->d_lab_q);
+    if (h->d_flux_slot) free_dev(h, h->d_flux_slot);
+    if (h->d_flux_phase) free_dev(h, h->d_flux_phase);
+    if (h->d_flux_out) free_dev(h, h->d_flux_out);
     if (h->stage) cudaFreeHost(h->stage);
     if (h->stage_cgf) cudaFreeHost(h->stage_cgf);
     if (h->stage_event) cudaEventDestroy(h->stage_event);
@@ -557,7 +566,7 @@ void free_all(bclbm_handle* h) {
 
 int run_gather(bclbm_handle* h) {
     const size_t n = static_cast<size_t>(h->nf) * h->nfields * h->q;
-    if (!h->d_gather) CUDA_TRY(h, cudaMalloc(&h->d_gather, n * sizeof(double)));
+    if (!h->d_gather) CUDA_TRY(h, cudaMallocAsync(reinterpret_cast<void**>(&h->d_gather), n * sizeof(double), h->stream));
     StepArgs a = make_args(h);
     a.src = h->pops[h->cur];
     if (h->collision == BCLBM_LINKS) {
@@ -803,16 +812,16 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     CREATE_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     const size_t sb = store_bytes(h->precision);
     const size_t pop_bytes = static_cast<size_t>(h->nfields) * Q * pad * sb;
-    CREATE_TRY(cudaMalloc(&h->pops[0], pop_bytes));
-    CREATE_TRY(cudaMalloc(&h->pops[1], pop_bytes));
+    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->pops[0]), pop_bytes, h->stream));
+    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->pops[1]), pop_bytes, h->stream));
     const size_t ntab = device_table ? static_cast<size_t>(R) * pad : tab.size();
-    CREATE_TRY(cudaMalloc(&h->d_nbr, ntab * sizeof(int32_t)));
-    CREATE_TRY(cudaMalloc(&h->d_slot_bulk, pad * sizeof(int32_t)));
-    CREATE_TRY(cudaMalloc(&h->d_rho, static_cast<size_t>(h->nfields) * pad * sizeof(double)));
-    CREATE_TRY(cudaMalloc(&h->d_vel, static_cast<size_t>(D) * pad * sizeof(double)));
-    CREATE_TRY(cudaMalloc(&h->d_params, sizeof(DevParams)));
-    CREATE_TRY(cudaMalloc(&h->d_partials, (static_cast<size_t>(grid_for(h->nf)) * 6 + 64) * sizeof(double)));
-    CREATE_TRY(cudaMalloc(&h->d_red, 16 * sizeof(double)));
+    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_nbr), ntab * sizeof(int32_t), h->stream));
+    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_slot_bulk), pad * sizeof(int32_t), h->stream));
+    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_rho), static_cast<size_t>(h->nfields) * pad * sizeof(double), h->stream));
+    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_vel), static_cast<size_t>(D) * pad * sizeof(double), h->stream));
+    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_params), sizeof(DevParams), h->stream));
+    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_partials), (static_cast<size_t>(grid_for(h->nf)) * 6 + 64) * sizeof(double), h->stream));
+    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_red), 16 * sizeof(double), h->stream));
     CREATE_TRY(cudaMemcpyAsync(h->d_slot_bulk, h->slot_bulk.data(), h->nf * sizeof(int32_t), cudaMemcpyHostToDevice,
                                h->stream));
     if (!device_table) {
@@ -901,7 +910,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         auto up = [&](auto** dst, const auto& v, size_t n_min) -> cudaError_t {
             using E = typename std::remove_reference<decltype(v)>::type::value_type;
             const size_t n = std::max(v.size(), n_min);
-            cudaError_t e = cudaMalloc(reinterpret_cast<void**>(dst), n * sizeof(E));
+            cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(dst), n * sizeof(E), h->stream);
             if (e == cudaSuccess && !v.empty())
                 e = cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice, h->stream);
             return e;
@@ -914,18 +923,18 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         CREATE_TRY(up(&h->d_lab_g, lp.lab_g, 1));
         CREATE_TRY(up(&h->d_flux_slot, lp.flux_slot, 1));
         CREATE_TRY(up(&h->d_flux_phase, lp.flux_phase, 1));
-        CREATE_TRY(cudaMalloc(&h->d_ustore, std::max<size_t>(3 * static_cast<size_t>(h->npress), 1) * sizeof(double)));
-        CREATE_TRY(cudaMalloc(&h->d_lab_val, std::max<size_t>(lp.lab_slot.size(), 1) * sizeof(double)));
-        CREATE_TRY(cudaMalloc(&h->d_lab_q, (static_cast<size_t>(h->nlab) + 1) * sizeof(double)));
+        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_ustore), std::max<size_t>(3 * static_cast<size_t>(h->npress), 1) * sizeof(double), h->stream));
+        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_lab_val), std::max<size_t>(lp.lab_slot.size(), 1) * sizeof(double), h->stream));
+        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_lab_q), (static_cast<size_t>(h->nlab) + 1) * sizeof(double), h->stream));
         CREATE_TRY(cudaMemsetAsync(h->d_lab_q, 0, (static_cast<size_t>(h->nlab) + 1) * sizeof(double), h->stream));
-        CREATE_TRY(cudaMalloc(&h->d_flux_out, 2 * sizeof(double)));
+        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_flux_out), 2 * sizeof(double), h->stream));
         CREATE_TRY(cudaStreamSynchronize(h->stream));  // the host vectors go out of scope
     }
 
     // colour field: fluid slots (written every step), stored solids (fixed), ghost (0)
     if (h->collision == BCLBM_RK) {
         const size_t ncg = static_cast<size_t>(h->nf) + h->ns + 1;
-        CREATE_TRY(cudaMalloc(&h->d_cg, ncg * sizeof(double)));
+        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_cg), ncg * sizeof(double), h->stream));
         std::vector<double> cg(ncg, 0.0);
         h->solid_cg.assign(h->ns, 0.0);
         for (int k = 0; k < h->ns; ++k) {
@@ -939,7 +948,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         CREATE_TRY(cudaMemcpyAsync(h->d_cg, cg.data(), ncg * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         if (h->precision != BCLBM_F64) {
             std::vector<float> cgf(cg.begin(), cg.end());
-            CREATE_TRY(cudaMalloc(&h->d_cgf, ncg * sizeof(float)));
+            CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_cgf), ncg * sizeof(float), h->stream));
             CREATE_TRY(cudaMemcpyAsync(h->d_cgf, cgf.data(), ncg * sizeof(float), cudaMemcpyHostToDevice, h->stream));
         }
         CREATE_TRY(cudaStreamSynchronize(h->stream));
@@ -1204,7 +1213,7 @@ int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg)
         // straight into the caller's arrays (no pinned staging, no host scatter)
         CUDA_TRY(h, cudaSetDevice(h->device));
         const size_t n = static_cast<size_t>(h->nf) * h->nfields * h->q;
-        if (!h->d_gather) CUDA_TRY(h, cudaMalloc(&h->d_gather, n * sizeof(double)));
+        if (!h->d_gather) CUDA_TRY(h, cudaMallocAsync(reinterpret_cast<void**>(&h->d_gather), n * sizeof(double), h->stream));
         k_macros_aos<<<grid_for(h->nf), kBlock, 0, h->stream>>>(h->d_rho, h->d_vel, h->d_slot_bulk, h->d_gather, h->nf,
                                                                 h->nf_pad, h->nfields, h->nd);
         launch_counter()++;
