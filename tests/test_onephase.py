@@ -41,3 +41,31 @@ def test_fixture_exercises_every_rule(bclbm):
         assert c.labels.max() == 2 and np.any(c.force_on[b] == 0)
         touches0 = np.any(nb[b] == 0, axis=1) & ((tb >> 4) & 1).astype(bool)
         assert touches0.any() == (not c.meta["ghost_layers"])
+
+
+def test_tagged_pack_links_all_have_a_rule(bclbm):
+    """geometry.tagged_pack's tags give every link of every fluid node one of the
+    std_one_phase rules (solid-fluid, pressure-fluid, fluid-fluid) or a fluid
+    upstream node, which bclbm_create requires (main.cpp:24-129); its interior
+    domains all have source nodes (tag < 3)."""
+    mask, attrs = bclbm.geometry.tagged_pack((30, 28, 40), 4.0, 0.45, 11, blob_radius=3.5, blob_spacing=12)
+    lat = bclbm.lbsolver.Lattice.from_geometry(mask, "D3Q19", "xy")
+    tags = lat.attribute(attrs["nodetags"]).astype(np.int64)
+    tags[0] = -1  # Nodes initialises node 0's tag to -1
+    labels = lat.attribute(attrs["interior_domains"]).astype(np.int64)
+    nb = lat.neigh.reshape(-1, 19)
+    fluid = lat.types > 1
+    rev = np.array([(q + 9) % 18 for q in range(18)])
+    b = lat.bulk
+    tn = tags[b][:, None]
+    y = nb[b][:, rev]          # upstream node of each incoming direction q
+    ty = tags[y]
+    sf = ((tn >> 3) & 1).astype(bool) & ((ty & 3) == 0)
+    pf = ((tn >> 4) & 1).astype(bool) & ((ty & 3) == 3)
+    ff = (((tn & 3) == 1) & ((tn >> 2) & 1).astype(bool) & ((ty & 3) == 2)) | \
+         (((tn & 3) == 2) & ((ty & 3) == 1) & ((ty >> 2) & 1).astype(bool))
+    plain = (y != 0) & fluid[y]
+    assert np.all(sf | pf | ff | plain)
+    assert pf.any() and sf.any() and ff.any()
+    for lab in range(1, labels.max() + 1):
+        assert np.any((labels[1:] == lab) & (tags[1:] < 3)), lab
