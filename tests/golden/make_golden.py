@@ -17,7 +17,7 @@ reference lbsolver through ``oracle/_ref/ref_driver_<lattice>`` and stores
 
 in ``<case>.npz``.  Config 1 (the 256x64 channel) is additionally run through
 the UNMODIFIED ``src/std_case/main.cpp`` and its VTU output is compared with
-the driver's dump, which pins the driver itself.
+the ref_driver dump, which pins ref_driver itself.
 
 ``vtu_<case>.npz`` holds the reference's own output step (``src/io/Output.h``
 through ``ref_driver vtu``) on seeded fields: the fields and the bytes of every
@@ -214,7 +214,7 @@ def make_case(ref: Path, case: dict, keep_dir=None):
 
 def pin_std_case(ref: Path, vtk: Path, work: Path):
     """Runs the unmodified std_case main on config 1 and compares its VTU output
-    with the driver's dump after the same number of steps."""
+    with the ref_driver dump after the same number of steps."""
     exe = REPO / "oracle" / "_ref" / "std_case_d2q9"
     root = work / "std_case"
     (root / "input" / "mpi").mkdir(parents=True)
@@ -234,7 +234,7 @@ def pin_std_case(ref: Path, vtk: Path, work: Path):
     ddir = work / "pin"
     ddir.mkdir()
     # std_case runs iterations 0..max inclusive; the moments written at the last
-    # iteration are those of the driver's last step when it runs max+1 steps.
+    # iteration are those of ref_driver's last step when it runs max+1 steps.
     run([str(drv), "single", str(root / "input" / "mpi" / "tmp0.vtklb"), str(ddir),
          f"steps={n_it + 1}", "tau=1.0", "fx=1e-6"])
     nf = rho_vtu.size
@@ -246,7 +246,7 @@ def pin_std_case(ref: Path, vtk: Path, work: Path):
         "what": "unmodified src/std_case/main.cpp (D2Q9) vs oracle/ref_driver.cpp, config 1 geometry",
         "iterations": n_it, "fluid_nodes": int(nf), "rho_bit_exact": True, "vel_bit_exact": True,
         "vtu": last.name}, indent=1) + "\n")
-    print(f"std_case pin: {last.name} rho/vel bit-exact against the driver ({nf} nodes)")
+    print(f"std_case pin: {last.name} rho/vel bit-exact against ref_driver ({nf} nodes)")
 
 
 # The VTU fixtures: (case, fields per node, seed)
