@@ -15,7 +15,7 @@ reference lbsolver through ``oracle/_ref/ref_driver_<lattice>`` and stores
 * the reference's populations, densities, velocities (and colour field) after
   the stated number of steps, restricted to the fluid nodes,
 
-in ``<case>.npz``.  Config 1 (the 256x64 channel) is additionally run through
+in ``<case>.npz``.  The 256x64 channel is additionally run through
 the UNMODIFIED ``src/std_case/main.cpp`` and its VTU output is compared with
 the ref_driver dump, which pins ref_driver itself.
 
@@ -123,9 +123,9 @@ def two_phase_fields(mask, seed, p=0.5, wett=0.5):
 
 def cases():
     """Geometries and runs.  Sizes are chosen so the oracle finishes in seconds,
-    except config 1 at its full 20,000 steps."""
+    except the 256x64 channel at its full 20,000 steps."""
     out = []
-    # Config 1: D2Q9 channel 256x64, walls at y=0 and y=63, periodic x, tau=1, gx=1e-6.
+    # D2Q9 channel 256x64, walls at y=0 and y=63, periodic x, tau=1, gx=1e-6.
     ch = geometry.channel_2d(256, 64)
     out.append(dict(name="channel_256x64", lattice="D2Q9", periodic="x", mask=ch,
                     attrs={"init_rho": np.ones(ch.shape)},
@@ -213,7 +213,7 @@ def make_case(ref: Path, case: dict, keep_dir=None):
 
 
 def pin_std_case(ref: Path, vtk: Path, work: Path):
-    """Runs the unmodified std_case main on config 1 and compares its VTU output
+    """Runs the unmodified std_case main on the 256x64 channel and compares its VTU output
     with the ref_driver dump after the same number of steps."""
     exe = REPO / "oracle" / "_ref" / "std_case_d2q9"
     root = work / "std_case"
@@ -243,7 +243,7 @@ def pin_std_case(ref: Path, vtk: Path, work: Path):
     if not (np.array_equal(rho_vtu, rho_d) and np.array_equal(vel_vtu, vel_d)):
         raise SystemExit("driver does not reproduce the unmodified std_case output")
     (HERE / "std_case_pin.json").write_text(json.dumps({
-        "what": "unmodified src/std_case/main.cpp (D2Q9) vs oracle/ref_driver.cpp, config 1 geometry",
+        "what": "unmodified src/std_case/main.cpp (D2Q9) vs oracle/ref_driver.cpp, 256x64 channel geometry",
         "iterations": n_it, "fluid_nodes": int(nf), "rho_bit_exact": True, "vel_bit_exact": True,
         "vtu": last.name}, indent=1) + "\n")
     print(f"std_case pin: {last.name} rho/vel bit-exact against ref_driver ({nf} nodes)")
@@ -418,7 +418,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("BCLBM_REFERENCE", "/root/reference"))
     ap.add_argument("--only", default=None)
-    ap.add_argument("--pin-only", action="store_true", help="only rerun the std_case pin of config 1")
+    ap.add_argument("--pin-only", action="store_true", help="only rerun the std_case pin of the 256x64 channel")
     ap.add_argument("--vtu-only", action="store_true", help="only rewrite the VTU fixtures")
     ap.add_argument("--onephase-only", action="store_true", help="only rewrite the std_one_phase fixtures")
     args = ap.parse_args()

@@ -49,7 +49,7 @@ def test_oracle_thread_count_does_not_change_results(bclbm, oracle):
 
 
 def test_poiseuille_known_answer(bclbm):
-    """Config 1 after 20,000 reference steps against the analytic channel profile
+    """The 256x64 channel after 20,000 reference steps against the analytic channel profile
     u(y) = g/(2 nu) (y - y0)(y1 - y), walls half-way between nodes: the profile's
     relative L2 error stays near 1e-4 (the slowest diffusive mode has not decayed)."""
     case = lbcases.Case("channel_256x64", bclbm)
