@@ -11,7 +11,8 @@
 // coordinates shifted by -0.5.  Binary data is "appended" raw with a 32-bit byte
 // count before each array.  Where the appended data passes 2^31 bytes (the
 // reference's int offsets overflow there) the file is written with
-// header_type="UInt64" and 64-bit counts instead, which VTK readers accept.
+// header_type="UInt64" and 64-bit counts instead, which VTK readers accept
+// (BCLBM_VTU_BINARY64 asks for that form at any size).
 //
 // What differs is the work per write: the mesh and its appended blocks are
 // built once at creation; each write gathers every variable into one buffer
@@ -127,7 +128,8 @@ struct bclbm_output {
     std::vector<File> files;
     // the mesh's appended blocks (or ASCII texts), built on first write
     std::vector<Block> grid_blocks;
-    bool wide = false;  // header_type UInt64
+    bool wide = false;        // header_type UInt64
+    bool force_wide = false;  // BCLBM_VTU_BINARY64: UInt64 counts whatever the size
     std::thread writer;
     int async_status = BCLBM_OK;
     std::string error;
@@ -278,11 +280,11 @@ void layout(bclbm_output* o) {
 
 // switches to 64-bit counts where the reference's 32-bit offsets would overflow
 void relayout(bclbm_output* o) {
-    o->wide = false;
+    o->wide = o->force_wide;
     layout(o);
     bool big = o->grid_bytes > kInt32Max;
     for (const File& f : o->files) big |= f.offset > kInt32Max;
-    if (big) {
+    if (big && !o->wide) {
         o->wide = true;
         layout(o);
     }
@@ -498,7 +500,8 @@ int bclbm_output_create(int32_t nd, int64_t n_cells, const int32_t* pos, const i
         return BCLBM_ERR_INVALID;
     if (value_type != BCLBM_VTU_FLOAT64 && value_type != BCLBM_VTU_FLOAT32 && value_type != BCLBM_VTU_INT32)
         return BCLBM_ERR_INVALID;
-    if (format != BCLBM_VTU_BINARY && format != BCLBM_VTU_ASCII) return BCLBM_ERR_INVALID;
+    if (format != BCLBM_VTU_BINARY && format != BCLBM_VTU_ASCII && format != BCLBM_VTU_BINARY64)
+        return BCLBM_ERR_INVALID;
     if (nproc != 1) return BCLBM_ERR_UNSUPPORTED;  // PVTU pieces of several ranks share one file
     if (n_cells * (nd == 3 ? 8 : 4) > kInt32Max) return BCLBM_ERR_UNSUPPORTED;
     bclbm_output* o = new (std::nothrow) bclbm_output();
@@ -508,7 +511,8 @@ int bclbm_output_create(int32_t nd, int64_t n_cells, const int32_t* pos, const i
         o->nd = nd;
         o->n_cells = n_cells;
         o->value_type = value_type;
-        o->format = format;
+        o->format = format == BCLBM_VTU_BINARY64 ? BCLBM_VTU_BINARY : format;
+        o->force_wide = format == BCLBM_VTU_BINARY64;
         o->rank = rank;
         o->nproc = nproc;
         if (nodes) o->nodes.assign(nodes, nodes + n_cells);

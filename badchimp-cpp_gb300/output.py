@@ -28,7 +28,7 @@ import numpy as np
 from . import native as _native
 
 FLOAT64, FLOAT32, INT32 = 0, 1, 2
-BINARY, ASCII = 0, 1
+BINARY, ASCII, BINARY64 = 0, 1, 2
 _TYPES = {np.dtype(np.float64): FLOAT64, np.dtype(np.float32): FLOAT32, np.dtype(np.int32): INT32}
 
 

@@ -306,7 +306,8 @@ void bclbm_batch_destroy(bclbm_batch* b);
  *   (Grid::pos(nodes), LBgrid.h:114); nodes [n_cells] their node numbers (for
  *   bclbm_output_add_field), or NULL for arrays only (the
  *   Output(pos, dir, rank, nproc, ...) form).  value_type: the on-disk type T;
- *   format: BCLBM_VTU_BINARY (the reference's default) or BCLBM_VTU_ASCII.
+ *   format: BCLBM_VTU_BINARY (the reference's default), BCLBM_VTU_ASCII, or
+ *   BCLBM_VTU_BINARY64 (64-bit counts and offsets whatever the size).
  *   Creates <dir> and <dir>/vtu as the reference does (mkdir of each, 0700).
  *   nproc > 1 is BCLBM_ERR_UNSUPPORTED (the PVTU pieces of several ranks share
  *   one file through MPI-IO).
@@ -328,8 +329,9 @@ void bclbm_batch_destroy(bclbm_batch* b);
 #define BCLBM_VTU_FLOAT64 0
 #define BCLBM_VTU_FLOAT32 1
 #define BCLBM_VTU_INT32 2
-#define BCLBM_VTU_BINARY 0
+#define BCLBM_VTU_BINARY 0   /* appended raw, 32-bit counts (64-bit past 2^31 bytes) */
 #define BCLBM_VTU_ASCII 1
+#define BCLBM_VTU_BINARY64 2 /* appended raw with header_type="UInt64" at any size */
 typedef struct bclbm_output bclbm_output;
 
 int bclbm_output_create(int32_t nd, int64_t n_cells, const int32_t* pos, const int32_t* nodes, const char* dir,

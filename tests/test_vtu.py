@@ -205,3 +205,29 @@ def test_add_variable_with_names(bclbm, tmp_path):
     arr = read_appended(tmp_path / "n" / "vtu" / "0000_x_0000000.vtu")
     # the reference appends the field number to these names too (Output.h:166-169)
     assert np.array_equal(arr["red0"], rho[lat.bulk, 0]) and np.array_equal(arr["blue1"], rho[lat.bulk, 1])
+
+
+def test_uint64_header_form(bclbm, tmp_path):
+    """BCLBM_VTU_BINARY64: the same arrays with header_type="UInt64", 64-bit
+    counts and offsets (the form the writer switches to past 2^31 bytes)."""
+    O = bclbm.output
+    case = lbcases.Case("box_12x10x8", bclbm)
+    lat = case.lat
+    rng = np.random.default_rng(3)
+    rho = rng.uniform(0.9, 1.1, (lat.n_nodes, 1))
+    vel = rng.normal(0, 1e-3, (lat.n_nodes, 1, 3))
+    arrs = {}
+    for fmt, sub in ((O.BINARY, "n"), (O.BINARY64, "w")):
+        with O.Output(lat, lat.bulk, tmp_path / sub, fmt=fmt) as o:
+            o.add_file("x")
+            o.add_scalar_variables(["rho"], [rho])
+            o.add_vector_variables(["vel"], [vel])
+            o.write(0)
+        path = tmp_path / sub / "vtu" / "0000_x_0000000.vtu"
+        head = path.read_bytes().split(b"<AppendedData")[0]
+        assert (b'header_type="UInt64"' in head) == (fmt == O.BINARY64)
+        arrs[sub] = read_appended(path)
+    assert sorted(arrs["n"]) == sorted(arrs["w"])
+    for k in arrs["n"]:
+        assert np.array_equal(arrs["n"][k], arrs["w"][k]), k
+    assert np.array_equal(arrs["w"]["rho"], rho[lat.bulk, 0])
