@@ -69,3 +69,15 @@ def test_tagged_pack_links_all_have_a_rule(bclbm):
     assert pf.any() and sf.any() and ff.any()
     for lab in range(1, labels.max() + 1):
         assert np.any((labels[1:] == lab) & (tags[1:] < 3)), lab
+
+
+def test_solver_checks_links_arguments(bclbm):
+    """The Python mirror refuses a std_one_phase solver without its node
+    attributes, or with attributes of the wrong length, before calling the
+    library."""
+    c = lbcases.OnephaseCase("onephase_ghost", bclbm)
+    L = c.L
+    with pytest.raises(ValueError):
+        L.Solver(c.lat, c.f_init(), collision=L.LINKS, tau=(0.9, 0.9))
+    with pytest.raises(ValueError):
+        L.Solver(c.lat, c.f_init(), collision=L.LINKS, tau=(0.9, 0.9), tags=c.tags[:-1], labels=c.labels)
