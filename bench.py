@@ -211,18 +211,71 @@ def cpu_port_rate(lat, steps_target_s: float, nthreads: int, tau: float, force, 
     return lat.n_bulk * steps / dt / 1e6, steps, dt
 
 
+class _ReferenceLattice:
+    """The tables the reference arm needs: Grid / Nodes / bulk list of one rank."""
+
+    def __init__(self, tables):
+        self.nq = tables["nq"]
+        self.neigh = tables["neigh"]
+        self.types = tables["types"]
+        self.n_nodes = int(self.types.size)
+        self.bulk = np.arange(1, tables["nf"] + 1, dtype=np.int32)  # findBulkNodes: fluid nodes 1..Nf
+        self.n_bulk = int(self.bulk.size)
+
+
+def reference_workload(size: int, radius: float, porosity: float, seed: int):
+    """The benchmark lattice for the reference arm, built without the bclbm
+    package: geometry.py is loaded as a file of its own (it needs numpy only) and
+    its numpy numbering is used, so that this process loads no libbclbm.so.
+    Returns (tables, porosity, f0) with f0 = w_q at the bulk nodes
+    (src/std_case/main.cpp:92-96)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bclbm_geometry_numpy", REPO / "badchimp-cpp_gb300" / "geometry.py")
+    geometry = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(geometry)
+    t = time.time()
+    geo, centres, phi = geometry.sphere_pack((size, size, size), radius=radius, porosity=porosity, seed=seed)
+    lat = _ReferenceLattice(geometry.build_lattice_numpy(geo, "D3Q19", "xyz"))
+    w = np.array([2.0 / 36.0] * 3 + [1.0 / 36.0] * 6 + [2.0 / 36.0] * 3 + [1.0 / 36.0] * 6 + [12.0 / 36.0])
+    f0 = np.zeros((lat.n_nodes, lat.nq))
+    f0[lat.bulk] = w[None, :]
+    log(f"geometry {size}^3 (numpy numbering): porosity {phi:.4f}, {len(centres)} spheres, fluid {lat.n_bulk}, "
+        f"nodes {lat.n_nodes} ({time.time() - t:.1f}s)")
+    return lat, phi, f0.reshape(-1)
+
+
+def loaded_shared_objects():
+    """Shared objects of this repository mapped into the process (from /proc/self/maps)."""
+    try:
+        lines = Path("/proc/self/maps").read_text().splitlines()
+    except OSError:
+        return None
+    out = set()
+    for ln in lines:
+        p = ln.split()[-1] if ln.split() else ""
+        if p.endswith(".so") and p.startswith(str(REPO)):
+            out.add(str(Path(p).relative_to(REPO)))
+    return sorted(out)
+
+
 def run_reference(args, world, rank):
-    """--impl reference: the oracle port of the reference step on all host cores."""
+    """--impl reference: the CPU implementation of the step on all host cores.
+
+    Timed: oracle/liboracle.so, the plain-C restatement of the reference's
+    std_case step (push + half-way bounce-back, src/std_case/main.cpp:109-146),
+    bit-identical to the reference's own build on every fixture.  The reference's
+    own build (oracle/_ref) is compiled from its sources, which do not exist on
+    the GPU machine, so the restatement stands in for it there.  Nothing of the
+    bclbm package is imported: the lattice comes from geometry.py's numpy path."""
     if rank != 0:
         return
     sys.path.insert(0, str(REPO / "oracle"))
     import oracle
-    bclbm, lat, phi = build_workload(args.size, args.radius, args.porosity, args.seed)
+    lat, phi, f0 = reference_workload(args.size, args.radius, args.porosity, args.seed)
     nthreads = oracle.default_threads()
     g = oracle.OracleGrid(lat.nq, lat.neigh, lat.types, lat.bulk)
     F = (args.gx, 0.0, 0.0)
-    runner = oracle.SingleRunner(g, bclbm.lbsolver.initiate_single(lat, np.ones(lat.n_nodes)), args.tau, F,
-                                 nthreads=nthreads)
+    runner = oracle.SingleRunner(g, f0, args.tau, F, nthreads=nthreads)
     # one call per block of steps: the oracle's threads start once per call
     runner.run(args.warmup)
     t = time.time()
@@ -238,6 +291,8 @@ def run_reference(args, world, rank):
                          "sample": f"{args.steps} timed steps of the full workload, oracle (plain-C restatement "
                                    f"of the reference std_case step, push + bounce-back) on {nthreads} host threads"},
         "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "timed_library": "oracle/liboracle.so (oracle_single_run)",
+        "shared_objects_loaded": loaded_shared_objects(),
     }
     print(json.dumps(line), flush=True)
 
@@ -822,7 +877,7 @@ def main():
     ap.add_argument("--baseline-precision", default="f64", choices=["f64", "f32", "f16", "bf16"])
     args = ap.parse_args()
     if args.warmup < 3:
-        args.warmup = 3
+        ap.error(f"--warmup {args.warmup}: at least 3 untimed warm-up steps are required before the timed steps")
     world, rank = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)

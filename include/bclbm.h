@@ -193,9 +193,12 @@ int64_t bclbm_launch_count(void);
  * It computes the FP64 sums that bclbm_reduce computes - per field
  * sum_q f, sum_q f c_q, and max |f| (+Inf if any value is NaN or Inf) - over a
  * population array the caller holds on the device, in the library's device
- * layout [nfields][Q][slot_stride] and storage format (F64: f itself; the
+ * layout [nfields][Q][slot_stride].  precision names the values' format:
+ * BCLBM_F64 = plain FP64 values of f (the device format of handles created
+ * with BCLBM_FLAG_EXACT or BCLBM_FLAG_FP64_FMA; a default BCLBM_F64 handle keeps
+ * int64 fixed point on the device, which this entry point does not read); the
  * shifted formats as described at BCLBM_F32..BCLBM_BF16, with rho_ref and
- * store_scale as given to bclbm_create, 0 meaning the default).
+ * store_scale as given to bclbm_create, 0 meaning the default (F16: 4096).
  * d_out: caller-allocated device buffer of 6 doubles,
  *   [mass0, mass1, flux_x, flux_y, flux_z, max|f|].
  * stream: a cudaStream_t, or NULL for the default stream; the call is
@@ -206,8 +209,12 @@ int64_t bclbm_launch_count(void);
  * process exits.  n_slots above BCLBM_STATIC_MAX_SLOTS is rejected with
  * BCLBM_ERR_INVALID and a message on stderr.  All calls share that array:
  * calls whose kernels overlap on the GPU race and give wrong sums, so order
- * them on one stream.  The first call on a device looks up the array's device
- * address with that device current; make it before any stream capture. */
+ * them on one stream.  The first call in a CUDA context (normally the device's
+ * primary context) looks up the array's device address with that context
+ * current and keeps it for that context; make that first call before any
+ * stream capture.  After cudaDeviceReset the next call runs in a new context
+ * and looks the address up again.  An error already pending on the calling
+ * thread is returned (BCLBM_ERR_CUDA) without launching and is not cleared. */
 #define BCLBM_STATIC_MAX_SLOTS 8388608
 int bclbm_moments_static(int32_t lattice_q, int32_t precision, int32_t nfields, int32_t n_slots,
                          int32_t slot_stride, const void* d_pops, double rho_ref, double store_scale,

@@ -416,7 +416,7 @@ def make_onephase(ref: Path, case: dict):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("BCLBM_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("BCLBM_REFERENCE", str(Path(__file__).resolve().parents[3] / "reference")))
     ap.add_argument("--only", default=None)
     ap.add_argument("--pin-only", action="store_true", help="only rerun the std_case pin of the 256x64 channel")
     ap.add_argument("--vtu-only", action="store_true", help="only rewrite the VTU fixtures")

@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 REPO = Path(__file__).resolve().parent.parent
-REF = Path(os.environ.get("BCLBM_REFERENCE", "/root/reference"))
+REF = Path(os.environ.get("BCLBM_REFERENCE", Path(__file__).resolve().parents[2] / "reference"))
 
 pytestmark = pytest.mark.skipif(not (REF / "src" / "LBSOLVER.h").exists(), reason="reference sources absent")
 

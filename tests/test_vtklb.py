@@ -14,7 +14,7 @@ import pytest
 import lbcases
 
 REPO = Path(__file__).resolve().parent.parent
-REF = Path(os.environ.get("BCLBM_REFERENCE", "/root/reference"))
+REF = Path(os.environ.get("BCLBM_REFERENCE", Path(__file__).resolve().parents[2] / "reference"))
 sys.path.insert(0, str(REPO / "tests" / "golden"))
 
 pytestmark = pytest.mark.skipif(not (REF / "PythonScripts" / "vtklb.py").exists(),

@@ -21,7 +21,7 @@ import lbcases
 
 REPO = Path(__file__).resolve().parent.parent
 GOLDEN = REPO / "tests" / "golden"
-REF = Path(os.environ.get("BCLBM_REFERENCE", "/root/reference"))
+REF = Path(os.environ.get("BCLBM_REFERENCE", Path(__file__).resolve().parents[2] / "reference"))
 CREATED = re.compile(rb"<!-- Created [^>]* -->")
 
 
