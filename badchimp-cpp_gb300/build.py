@@ -3,7 +3,8 @@
 Translation units are compiled in parallel:
   csrc/bclbm_exact.cu    FP64 kernels in the reference's expression order,
                          compiled with -fmad=false (no FMA contraction)
-  csrc/bclbm_kernels.cu  FP64 (FMA) and FP32-compute kernels, reductions
+  csrc/bclbm_kernels.cu  FP64 (FMA) and FP32-compute kernels, the staged
+                         (TMA table-tile) single-phase kernels, reductions
   csrc/bclbm_api.cu      the C ABI of include/bclbm.h (host code)
   csrc/bclbm_static.cu   bclbm_moments_static, the entry point that allocates nothing
   csrc/bclbm_batch.cu    the multi-instance batch (persistent kernel, CUDA graph)

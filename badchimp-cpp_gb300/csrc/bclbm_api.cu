@@ -260,31 +260,7 @@ size_t footprint_bytes(const bclbm_desc* d, const Plan& p) {
 
 template <int Q>
 fx::Consts fixed_consts_q(const bclbm_handle* h) {
-    using L = Lat<Q>;
-    fx::Consts K;
-    std::memset(&K, 0, sizeof(K));
-    const double oms = 1.0 / h->tau[0], oma = 1.0 / h->tau[1];
-    const double tsf = 1 - 0.5 / h->tau[0], taf = 1 - 0.5 / h->tau[1];
-    K.alpha = fx::param(1.0 - 0.5 * (oms + oma));
-    K.beta = fx::param(0.5 * (oma - oms));
-    K.alpha_rest = fx::param(1.0 - oms);
-    const double wc[3] = {L::w(L::REST), L::w(0), L::w(L::NP - 1)};
-    for (int c = 0; c < 3; ++c) {
-        K.oms_w[c] = fx::param(oms * wc[c]);
-        K.oma3_w[c] = fx::param(3.0 * oma * wc[c]);
-        K.ktsf_w[c] = fx::param(-3.0 * wc[c] * tsf);
-    }
-    const double* F = h->force;
-    for (int q = 0; q < Q; ++q) {
-        const double cF = L::cx(q) * F[0] + L::cy(q) * F[1] + L::cz(q) * F[2];
-        K.kf9[q] = fx::param(9.0 * L::w(q) * tsf * cF);
-        K.ka3[q] = fx::param(3.0 * L::w(q) * taf * cF);
-    }
-    for (int d = 0; d < 3; ++d) {
-        K.force[d] = fx::param(F[d]);
-        K.half_force[d] = fx::param(0.5 * F[d]);
-    }
-    return K;
+    return fx::make_consts<Q>(h->trt, h->tau[0], h->tau[1], h->force);
 }
 
 fx::Consts fixed_consts(const bclbm_handle* h) { return h->q == 9 ? fixed_consts_q<9>(h) : fixed_consts_q<19>(h); }
@@ -816,6 +792,12 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->pops[1]), pop_bytes, h->stream));
     const size_t ntab = device_table ? static_cast<size_t>(R) * pad : tab.size();
     CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_nbr), ntab * sizeof(int32_t), h->stream));
+    if ((h->collision == BCLBM_BGK || h->collision == BCLBM_TRT) && ntab == static_cast<size_t>(R) * pad) {
+        // the native-FP64 steps after the first stage the pull table through shared
+        // memory with the tensor copy engine; without the driver's encoder they read it
+        // directly
+        h->pull_map_ok = encode_table_map(h->d_nbr, static_cast<int>(pad), R, &h->pull_map) == cudaSuccess;
+    }
     CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_slot_bulk), pad * sizeof(int32_t), h->stream));
     CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_rho), static_cast<size_t>(h->nfields) * pad * sizeof(double), h->stream));
     CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_vel), static_cast<size_t>(D) * pad * sizeof(double), h->stream));
@@ -1053,10 +1035,11 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
         } else if (h->collision != BCLBM_RK) {
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
+            const CUtensorMap* pm = h->pull_map_ok ? &h->pull_map : nullptr;
             if (h->exact) CUDA_TRY(h, launch_single_exact(h->q, h->trt, local, a, h->stream));
             else if (h->precision == BCLBM_F64 && !h->fma64)
                 CUDA_TRY(h, launch_single_fixed(h->q, h->trt, local, a, h->stream));
-            else CUDA_TRY(h, launch_single_fast(h->q, h->precision, h->trt, local, a, h->stream));
+            else CUDA_TRY(h, launch_single_fast(h->q, h->precision, h->trt, local, a, pm, h->stream));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
         } else {
             StepArgs ad = a;
@@ -1259,6 +1242,8 @@ int bclbm_reduce(bclbm_handle* h, bclbm_stats* out) {
     out->n_bulk = h->nf;
     out->steps_done = h->steps_done;
     out->nonfinite = std::isfinite(red[5]) && std::isfinite(red[0]) && std::isfinite(red[1]) ? 0 : 1;
+    if (prm.fx_overflow & stage::kFlagWaitTimeout)
+        return fail(h, BCLBM_ERR_CUDA, "a step kernel's bounded wait for a staged table tile ran out");
     if (prm.fx_overflow) {
         out->nonfinite = 1;
         return fail(h, BCLBM_ERR_NONFINITE, "a node left the fixed-point range (sum |f| < 8, rho > 0.15)");

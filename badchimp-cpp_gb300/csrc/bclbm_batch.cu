@@ -545,7 +545,9 @@ int bclbm_batch_stats(bclbm_batch* b, int32_t n, const int32_t* ids, bclbm_stats
         st.n_bulk = h->nf;
         st.steps_done = b->host_step - b->start[ids[j]];
         st.nonfinite = std::isfinite(r[5]) && std::isfinite(r[0]) ? 0 : 1;
-        if (prm[j].fx_overflow) {
+        if (prm[j].fx_overflow & stage::kFlagWaitTimeout) {
+            rc = bfail(b, BCLBM_ERR_CUDA, "a step kernel's bounded wait for a staged table tile ran out");
+        } else if (prm[j].fx_overflow) {
             st.nonfinite = 1;
             rc = bfail(b, BCLBM_ERR_NONFINITE, "a node left the fixed-point range (sum |f| < 8, rho > 0.15)");
         } else if (st.nonfinite && rc == BCLBM_OK) {

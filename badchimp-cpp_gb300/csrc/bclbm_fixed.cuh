@@ -273,40 +273,73 @@ inline int64_t param(double d) {
     return from_f64(d, ovf);
 }
 
-// Per-handle constants of the fixed-point BGK/TRT collision (see collide_fx).
+// Per-handle constants of the fixed-point BGK/TRT collision (collide_to).  All
+// multiplying constants are positive, so their products with a signed value
+// take the cheaper signed x unsigned form.
 struct Consts {
-    int64_t alpha, beta, alpha_rest;  // 1 - (oms + oma)/2, (oma - oms)/2, 1 - oms
-    int64_t oms_w[3];                 // oms w_c            (c: 0 rest, 1 axis, 2 diagonal)
-    int64_t oma3_w[3];                // 3 oma w_c
-    int64_t ktsf_w[3];                // -3 w_c tsf
-    int64_t kf9[19];                  // 9 w_q tsf (c_q . F)
-    int64_t ka3[19];                  // 3 w_q taf (c_q . F)
-    int64_t force[3];                 // F
-    int64_t half_force[3];            // F / 2
+    int64_t homs, homa;   // oms / 2, oma / 2 (pairs: f_q - homs P - homa M)
+    int64_t oms;          // rest direction: f_R - oms f_R
+    int64_t oms_w2;       // oms w_diag
+    int64_t k45;          // 4.5 oms w_diag
+    int64_t oma3_w2;      // 3 oma w_diag
+    int64_t tsf3_w2;      // 3 w_diag tsf
+    int64_t kf9[19];      // 9 w_q tsf (c_q . F)
+    int64_t ka3[19];      // 3 w_q taf (c_q . F)
+    int64_t force[3];     // F
+    int64_t half_force[3];  // F / 2
 };
 
-// One BGK (TRT = false) or TRT collision in fixed point.  F holds the Q
-// populations on entry and the post-collision populations on exit; rho and u
-// receive the moments (u = (sum_q f c_q + F/2) / rho, Guo).  The algebra is the
-// regrouping by direction pairs of calcOmegaBGK(TRT) + calcDeltaOmegaF(TRT)
-// (src/lbsolver/LBcollision.h:27-75, 194-236):
-//   post_q  = alpha f_q + beta f_rq + X + Y,  post_rq = alpha f_rq + beta f_q + X - Y
-//   X = oms w rho (1 + 4.5 (c.u)^2 - 1.5 u^2) + w tsf (9 (c.F)(c.u) - 3 u.F)
-//   Y = 3 oma w rho (c.u) + 3 w taf (c.F)
-//   post_rest = (1 - oms) f_rest + oms w0 rho (1 - 1.5 u^2) - 3 w0 tsf u.F
-// ovf is set when the node's values do not fit the fixed-point range: the sum
-// of |f_q| must stay below 8 (it bounds rho and every momentum component) and
-// rho above 0.15 (1 / rho below 8).
+// The constants for relaxation times tau (symmetric) and tau_anti (TRT; BGK
+// uses tau for both) and body force F, computed in FP64 as the reference
+// computes 1/tau and 1 - 0.5/tau (src/lbsolver/LBcollision.h:27-75, 194-236),
+// then converted to fixed point.
+template <int Q>
+inline Consts make_consts(bool trt, double tau, double tau_anti, const double* F) {
+    using L = Lat<Q>;
+    Consts K;
+    __builtin_memset(&K, 0, sizeof(K));
+    const double oms = 1.0 / tau, oma = trt ? 1.0 / tau_anti : oms;
+    const double tsf = 1 - 0.5 / tau, taf = trt ? 1 - 0.5 / tau_anti : tsf;
+    const double w2 = L::w(L::NP - 1);  // the diagonal (smallest) weight
+    K.homs = param(0.5 * oms);
+    K.homa = param(0.5 * oma);
+    K.oms = param(oms);
+    K.oms_w2 = param(oms * w2);
+    K.k45 = param(4.5 * oms * w2);
+    K.oma3_w2 = param(3.0 * oma * w2);
+    K.tsf3_w2 = param(3.0 * w2 * tsf);
+    for (int q = 0; q < Q; ++q) {
+        const double cF = L::cx(q) * F[0] + L::cy(q) * F[1] + L::cz(q) * F[2];
+        K.kf9[q] = param(9.0 * L::w(q) * tsf * cF);
+        K.ka3[q] = param(3.0 * L::w(q) * taf * cF);
+    }
+    for (int d = 0; d < 3; ++d) {
+        K.force[d] = param(F[d]);
+        K.half_force[d] = param(0.5 * F[d]);
+    }
+    return K;
+}
+
+// One BGK (TRT = false) or TRT collision in fixed point: the regrouping by
+// direction pairs of calcOmegaBGK(TRT) + calcDeltaOmegaF(TRT)
+// (src/lbsolver/LBcollision.h:27-75, 194-236).  With P = f_q + f_rq,
+// M = f_q - f_rq and j = rho u = sum_q f c_q + F/2 (exact in fixed point):
+//   post_q  = f_q  - (oms/2) P - (oma/2) M + X + Y
+//   post_rq = f_rq - (oms/2) P + (oma/2) M + X - Y
+//   X = oms w (rho - 1.5 j.u) + 4.5 oms w (c.j)(c.u) + 9 w tsf (c.F)(c.u) - 3 w tsf u.F
+//   Y = 3 oma w (c.j) + 3 w taf (c.F)
+//   post_rest = f_R - oms f_R + oms w0 (rho - 1.5 j.u) - 3 w0 tsf u.F
+// (rho (c.u)^2 = (c.j)(c.u) and rho u^2 = j.u, so no product involves rho).
+// F holds the node's Q populations on entry; each post-collision population is
+// handed to sink(q, value) as soon as it is known (pairs in order, the rest
+// direction last), so a kernel can store it and free its registers while the
+// remaining pairs are computed.  rho and u receive the moments.  ovf is set
+// when the node's values do not fit the fixed-point range: the sum of |f_q|
+// must stay below 8 (it bounds rho and every momentum component) and rho above
+// 0.15 (1 / rho below 8).
 //
 // Weight classes: w_rest : w_axis : w_diag = 12 : 2 : 1 (D3Q19) and 16 : 4 : 1
-// (D2Q9), so the per-class products rho oms w_c, rho 3 oma w_c and
-// -3 w_c tsf u.F are exact integer multiples of the diagonal one.
-// Populations of a pair enter through P = f_q + f_rq and M = f_q - f_rq:
-//   alpha f_q + beta f_rq = (alpha + beta)/2 P + (alpha - beta)/2 M.
-// The collision of one node.  F holds the node's 19 (or 9) populations on entry;
-// each post-collision population is handed to sink(q, value) as soon as it is
-// known (pairs in order, the rest direction last), so a kernel can convert and
-// store it and free its registers while the remaining pairs are computed.
+// (D2Q9), so the class products are exact multiples of the diagonal one.
 template <int Q, bool TRT, class Sink>
 __host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K, int64_t& rho_o, int64_t* u_o,
                                                     int& ovf, Sink&& sink) {
@@ -336,7 +369,7 @@ __host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K,
         if (D == 3 && Lat<Q>::cz(k) < 0) J[2] -= Mk;
     }
     // 1 / rho: FP32 estimate (24 bits), one Newton step in fixed point (48 bits):
-    // u = (J + F/2) / rho is O(1e-2) or less, so its absolute error stays below 2^-60
+    // u = j / rho is O(1e-2) or less, so its absolute error stays below 2^-60
     const float rf = static_cast<float>(rho) * 8.67361737988403547e-19f;  // 2^-60
     if (!(rf > 0.15f)) ovf = 1;
 #ifdef __CUDA_ARCH__
@@ -346,52 +379,48 @@ __host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K,
 #endif
     int64_t inv = static_cast<int64_t>(ri * 1.152921504606846976e18f);  // 2^60
     inv = mul_uu(inv, 2 * ONE - mul_uu(rho, inv));
-    int64_t u[3], ua[3];
+    int64_t j[3], u[3], u45[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        u[d] = (d < D) ? mul_su(J[d] + K.half_force[d], inv) : 0;
-        ua[d] = u[d] < 0 ? -u[d] : u[d];
+        j[d] = (d < D) ? J[d] + K.half_force[d] : 0;
+        u[d] = (d < D) ? mul_su(j[d], inv) : 0;
+        u45[d] = (d < D) ? mul_su(u[d], K.k45) : 0;
     }
     rho_o = rho;
 #pragma unroll
     for (int d = 0; d < D; ++d) u_o[d] = u[d];
-    int64_t uu = mul_uu(ua[0], ua[0]) + mul_uu(ua[1], ua[1]);
-    if (D == 3) uu += mul_uu(ua[2], ua[2]);
-    int64_t uF = mul_ss(u[0], K.force[0]) + mul_ss(u[1], K.force[1]);
-    if (D == 3) uF += mul_ss(u[2], K.force[2]);
-    const int64_t base = ONE - (uu + (uu >> 1));  // 1 - 1.5 u^2
-    // diagonal-class products, the others by the exact weight ratios
-    const int64_t A2 = mul_uu(rho, K.oms_w[2]);
-    const int64_t B2 = mul_uu(rho, K.oma3_w[2]);
-    const int64_t K2 = mul_ss(uF, K.ktsf_w[2]);
-    const int64_t AB2 = mul_uu(A2, base);
-    // class c values (rest 0, axis 1, diagonal 2) by the exact weight ratios, formed
-    // where they are used rather than held in registers
+    int64_t ju = mul_ss(j[0], u[0]) + mul_ss(j[1], u[1]);
+    if (D == 3) ju += mul_ss(j[2], u[2]);
+    // u.F over the force's nonzero components (the branches are uniform)
+    int64_t uF = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        if (K.force[d] != 0) uF += mul_ss(u[d], K.force[d]);
+    const int64_t AB2 = mul_su(rho - (ju + (ju >> 1)), K.oms_w2);  // oms w2 (rho - 1.5 j.u)
+    const int64_t K2 = -mul_su(uF, K.tsf3_w2);                    // -3 w2 tsf u.F
+    // class c values (rest 0, axis 1, diagonal 2) by the exact weight ratios
     auto by_class = [](int64_t v2, int c) -> int64_t {
         return c == 2 ? v2 : (c == 1 ? (v2 << SH1) : (Q == 19 ? (v2 << 3) + (v2 << 2) : (v2 << 4)));
     };
-    const int64_t hs = TRT ? (K.alpha + K.beta) >> 1 : K.alpha >> 1;  // (alpha + beta) / 2
-    const int64_t ha = TRT ? (K.alpha - K.beta) >> 1 : K.alpha >> 1;  // (alpha - beta) / 2
+    const int64_t homa = TRT ? K.homa : K.homs;
 #pragma unroll
     for (int k = 0; k < NP; ++k) {
         const int c = Lat<Q>::wclass(k);
-        const int64_t cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];
-        const int64_t cua = cu < 0 ? -cu : cu;
-        const int64_t cu2 = mul_uu(cua, cua);
-        // X = Aw (4.5 cu^2 + base) + kf9 cu + Kw;  Y = Bw cu + ka3
-        int64_t X = by_class(AB2, c) + mul_uu(by_class(A2, c), (cu2 << 2) + (cu2 >> 1)) + by_class(K2, c);
-        // the force product vanishes for directions normal to the force; the
-        // (warp-uniform) branch also bounds how far the compiler interleaves the
-        // pairs, which keeps the kernel at ~114 registers and 2 blocks per SM
-        if (K.kf9[k] != 0) X += mul_ss(K.kf9[k], cu);
-        const int64_t Y = mul_su(cu, by_class(B2, c)) + K.ka3[k];
-        // alpha f_q + beta f_rq = hs P + ha M
-        const int64_t sp = mul_ss(hs, F[k] + F[k + NP]);
-        const int64_t sm = mul_ss(ha, F[k] - F[k + NP]);
-        sink(k, sp + sm + X + Y);
-        sink(k + NP, sp - sm + X - Y);
+        const int64_t cj = Lat<Q>::cx(k) * j[0] + Lat<Q>::cy(k) * j[1] + Lat<Q>::cz(k) * j[2];
+        const int64_t cu45 = Lat<Q>::cx(k) * u45[0] + Lat<Q>::cy(k) * u45[1] + Lat<Q>::cz(k) * u45[2];
+        int64_t X = by_class(AB2 + mul_ss(cj, cu45) + K2, c);
+        // the force term vanishes for directions normal to the force (uniform branch)
+        if (K.kf9[k] != 0) {
+            const int64_t cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];
+            X += mul_ss(K.kf9[k], cu);
+        }
+        const int64_t Y = by_class(mul_su(cj, K.oma3_w2), c) + K.ka3[k];
+        const int64_t P = F[k] + F[k + NP], M = F[k] - F[k + NP];
+        const int64_t sp = mul_su(P, K.homs), sm = mul_su(M, homa);
+        sink(k, F[k] - sp - sm + X + Y);
+        sink(k + NP, F[k + NP] - sp + sm + X - Y);
     }
-    sink(R, mul_ss(K.alpha_rest, F[R]) + by_class(AB2, 0) + by_class(K2, 0));
+    sink(R, F[R] - mul_su(F[R], K.oms) + by_class(AB2 + K2, 0));
 }
 
 // collide_to with the results written back into F

@@ -34,6 +34,9 @@ struct bclbm_handle {
     bool state_post = false;          // pops[cur] holds post-collision populations
     bool macros_valid = false;
     int32_t* d_nbr = nullptr;
+    // single-phase pull table as a tensor map (the staged step kernels); valid when pull_map_ok
+    CUtensorMap pull_map;
+    bool pull_map_ok = false;
     int32_t* d_slot_bulk = nullptr;
     double* d_rho = nullptr;
     double* d_vel = nullptr;

@@ -1,6 +1,9 @@
 // Restructured FP64 kernels (FMA), FP32-arithmetic kernels for the shifted
 // storage formats, the download gather and the deterministic FP64 reductions.
+#include <algorithm>
+#include <mutex>
 #include <type_traits>
+#include <unordered_map>
 
 #include "bclbm_launch.h"
 
@@ -41,15 +44,66 @@ __global__ void k_rk_fix(const double* sum, double n, double rho_ref, double mom
 
 namespace {
 
+// Persistent grid of a staged kernel (bclbm_stage.cuh): the blocks that fit on
+// the device at once (resident blocks per SM x SMs), at most one per tile.
+// BCLBM_STAGED_CARVEOUT picks the shared-memory carveout: 0 the driver's
+// choice, 1 the maximum, 2 just what the resident blocks need (the rest stays
+// L1 cache for the gathers and spills).  Looked up once per kernel.
+#ifndef BCLBM_STAGED_CARVEOUT
+#define BCLBM_STAGED_CARVEOUT 2
+#endif
+int staged_grid(const void* kernel, int nf) {
+    static std::mutex mu;
+    static std::unordered_map<const void*, int> per_device;
+    int resident = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = per_device.find(kernel);
+        if (it == per_device.end()) {
+            int dev = 0, sms = 0, per_sm = 0, smem_sm = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+            if (BCLBM_STAGED_CARVEOUT >= 1)
+                cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0);
+            if (BCLBM_STAGED_CARVEOUT == 2 && per_sm > 0 && smem_sm > 0) {
+                cudaFuncAttributes fa;
+                if (cudaFuncGetAttributes(&fa, kernel) == cudaSuccess) {
+                    const size_t need = static_cast<size_t>(per_sm) * (fa.sharedSizeBytes + 1024);
+                    const int pct = static_cast<int>(std::min<size_t>(100, (need * 100 + smem_sm - 1) / smem_sm));
+                    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+                }
+            }
+            it = per_device.emplace(kernel, std::max(1, sms * per_sm)).first;
+        }
+        resident = it->second;
+    }
+    return std::max(1, std::min(grid_for(nf), resident));
+}
+
 template <int Q, class S>
-cudaError_t single_fast_qs(bool trt, bool local, const StepArgs& a, cudaStream_t s) {
+cudaError_t single_fast_qs(bool trt, bool local, const StepArgs& a, const CUtensorMap* pull_map, cudaStream_t s) {
     const int g = grid_for(a.L.nf);
-    if (trt) {
-        if (local) k_single<Q, S, 1, true, true><<<g, kBlock, 0, s>>>(a);
-        else k_single<Q, S, 1, true, false><<<g, kBlock, 0, s>>>(a);
-    } else {
-        if (local) k_single<Q, S, 1, false, true><<<g, kBlock, 0, s>>>(a);
-        else k_single<Q, S, 1, false, false><<<g, kBlock, 0, s>>>(a);
+    // the staged kernel serves the native-FP64 step only (see k_single_staged)
+    constexpr bool kStaged = std::is_same<S, double>::value;
+    if (local || !pull_map || !kStaged) {
+        if (trt) {
+            if (local) k_single<Q, S, 1, true, true><<<g, kBlock, 0, s>>>(a);
+            else k_single<Q, S, 1, true, false><<<g, kBlock, 0, s>>>(a);
+        } else {
+            if (local) k_single<Q, S, 1, false, true><<<g, kBlock, 0, s>>>(a);
+            else k_single<Q, S, 1, false, false><<<g, kBlock, 0, s>>>(a);
+        }
+    } else if constexpr (kStaged) {
+        if (trt) {
+            const void* k = reinterpret_cast<const void*>(&k_single_staged<Q, S, true>);
+            k_single_staged<Q, S, true><<<staged_grid(k, a.L.nf), kBlock, 0, s>>>(a, *pull_map);
+        } else {
+            const void* k = reinterpret_cast<const void*>(&k_single_staged<Q, S, false>);
+            k_single_staged<Q, S, false><<<staged_grid(k, a.L.nf), kBlock, 0, s>>>(a, *pull_map);
+        }
     }
     launch_counter()++;
     return cudaGetLastError();
@@ -70,12 +124,13 @@ cudaError_t single_fixed_q(bool trt, bool local, const StepArgs& a, cudaStream_t
 }
 
 template <int Q>
-cudaError_t single_fast_q(int precision, bool trt, bool local, const StepArgs& a, cudaStream_t s) {
+cudaError_t single_fast_q(int precision, bool trt, bool local, const StepArgs& a, const CUtensorMap* pull_map,
+                          cudaStream_t s) {
     switch (precision) {
-        case kF64: return single_fast_qs<Q, double>(trt, local, a, s);
-        case kF32: return single_fast_qs<Q, float>(trt, local, a, s);
-        case kF16: return single_fast_qs<Q, __half>(trt, local, a, s);
-        case kBF16: return single_fast_qs<Q, __nv_bfloat16>(trt, local, a, s);
+        case kF64: return single_fast_qs<Q, double>(trt, local, a, pull_map, s);
+        case kF32: return single_fast_qs<Q, float>(trt, local, a, pull_map, s);
+        case kF16: return single_fast_qs<Q, __half>(trt, local, a, pull_map, s);
+        case kBF16: return single_fast_qs<Q, __nv_bfloat16>(trt, local, a, pull_map, s);
     }
     return cudaErrorInvalidValue;
 }
@@ -168,8 +223,10 @@ cudaError_t moments_q(int precision, int nfields, bool local, const StepArgs& a,
 
 }  // namespace
 
-cudaError_t launch_single_fast(int Q, int precision, bool trt, bool local, const StepArgs& a, cudaStream_t s) {
-    return Q == 9 ? single_fast_q<9>(precision, trt, local, a, s) : single_fast_q<19>(precision, trt, local, a, s);
+cudaError_t launch_single_fast(int Q, int precision, bool trt, bool local, const StepArgs& a,
+                               const CUtensorMap* pull_map, cudaStream_t s) {
+    return Q == 9 ? single_fast_q<9>(precision, trt, local, a, pull_map, s)
+                  : single_fast_q<19>(precision, trt, local, a, pull_map, s);
 }
 
 cudaError_t launch_single_fixed(int Q, bool trt, bool local, const StepArgs& a, cudaStream_t s) {
@@ -226,6 +283,35 @@ cudaError_t launch_reduce_final(int nv, const double* partials, int nblocks, dou
     else return cudaErrorInvalidValue;
     launch_counter()++;
     return cudaGetLastError();
+}
+
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the library
+// links the runtime only).
+cudaError_t encode_table_map(const int32_t* table, int pad, int rows, CUtensorMap* out) {
+    using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn encode = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<EncodeFn>(fn);
+    });
+    if (!encode) return cudaErrorNotSupported;
+    if (!table || pad % 64 != 0 || rows < 1 || rows > 256) return cudaErrorInvalidValue;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(pad), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(pad) * sizeof(int32_t)};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(stage::kSub), static_cast<cuuint32_t>(rows)};
+    const cuuint32_t elem[2] = {1, 1};
+    const CUresult r = encode(out, CU_TENSOR_MAP_DATA_TYPE_INT32, 2, const_cast<int32_t*>(table), dims, strides, box,
+                              elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 }  // namespace bclbm

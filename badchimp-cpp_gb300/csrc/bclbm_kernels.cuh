@@ -18,6 +18,7 @@
 
 #include "bclbm_device.cuh"
 #include "bclbm_fixed.cuh"
+#include "bclbm_stage.cuh"
 
 namespace bclbm {
 
@@ -138,6 +139,60 @@ __device__ __forceinline__ double cnorm_ref(int wclass) {  // DXQY::cNorm (SQRT2
 // ---------------------------------------------------------------------------
 // Population access
 // ---------------------------------------------------------------------------
+// Loads of the pull table and of the gathered populations.  BCLBM_L2_HINT asks
+// the L2 to fetch the surrounding 128 (1) or 256 (2) bytes with each miss: a
+// warp reads 64-256 contiguous bytes of a table row or of a population row,
+// and the warps on the next slots read the bytes after them.
+#ifndef BCLBM_L2_HINT
+#define BCLBM_L2_HINT 2
+#endif
+__device__ __forceinline__ int32_t ld_table(const int32_t* p) {
+#if BCLBM_L2_HINT == 2
+    int32_t v;
+    asm("ld.global.nc.L2::256B.b32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+#elif BCLBM_L2_HINT == 1
+    int32_t v;
+    asm("ld.global.nc.L2::128B.b32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+#else
+    return __ldg(p);
+#endif
+}
+
+template <class T>
+__device__ __forceinline__ T ld_pop(const T* p) {
+#if BCLBM_L2_HINT >= 1
+#if BCLBM_L2_HINT == 2
+#define BCLBM_L2Q ".L2::256B"
+#else
+#define BCLBM_L2Q ".L2::128B"
+#endif
+    if constexpr (sizeof(T) == 2) {
+        unsigned short v;
+        asm("ld.global" BCLBM_L2Q ".b16 %0, [%1];" : "=h"(v) : "l"(p));
+        T r;
+        __builtin_memcpy(&r, &v, 2);
+        return r;
+    } else if constexpr (sizeof(T) == 4) {
+        unsigned v;
+        asm("ld.global" BCLBM_L2Q ".b32 %0, [%1];" : "=r"(v) : "l"(p));
+        T r;
+        __builtin_memcpy(&r, &v, 4);
+        return r;
+    } else {
+        unsigned long long v;
+        asm("ld.global" BCLBM_L2Q ".b64 %0, [%1];" : "=l"(v) : "l"(p));
+        T r;
+        __builtin_memcpy(&r, &v, 8);
+        return r;
+    }
+#undef BCLBM_L2Q
+#else
+    return *p;
+#endif
+}
+
 // PULL: single-phase instances read the resolved pull table, two-phase
 // instances the extended neighbour table (which the colour gradient needs too).
 template <int Q, class S, bool LOCAL, bool PULL = false>
@@ -149,11 +204,24 @@ __device__ __forceinline__ void load_field(const S* __restrict__ g, const Lattic
         if (q == R || LOCAL) {
             v[q] = g[static_cast<size_t>(q) * L.nf_pad + i];
         } else if (PULL) {
-            v[q] = g[__ldg(L.pull + static_cast<size_t>(q) * L.nf_pad + i)];
+            v[q] = ld_pop(g + ld_table(L.pull + static_cast<size_t>(q) * L.nf_pad + i));
         } else {
             const int y = __ldg(L.nbr + static_cast<size_t>(Lat<Q>::rev(q)) * L.nf_pad + i);
             v[q] = pull_raw<Q, S>(g, L, q, y, i);
         }
+    }
+}
+
+// The same pull with the table entries already staged in shared memory:
+// rows[q][t] is the pull-table entry of direction q for this thread's slot.
+template <int Q, class S, int TILE>
+__device__ __forceinline__ void load_field_staged(const S* __restrict__ g, const LatticeView& L, int i,
+                                                  const int32_t (*rows)[TILE], int t, typename Store<S>::T* v) {
+    constexpr int R = Lat<Q>::REST;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if (q == R) v[q] = g[static_cast<size_t>(q) * L.nf_pad + i];
+        else v[q] = g[rows[q][t]];
     }
 }
 
@@ -304,13 +372,11 @@ __device__ __forceinline__ void collide_fast(C* f, const C* F, C oms, C oma, C t
 // MODE 0: exact reference order (F64, instantiated in the -fmad=false unit)
 // MODE 1: restructured, compute in double (F64) or float (shifted formats)
 // ---------------------------------------------------------------------------
-template <int Q, class S, int MODE, bool TRT, bool LOCAL>
-__device__ __forceinline__ void single_node(const StepArgs& a, int i) {
+// One single-phase update of slot i from its pulled raw values v.
+template <int Q, class S, int MODE, bool TRT>
+__device__ __forceinline__ void single_node_values(const StepArgs& a, int i, typename Store<S>::T* v) {
     const bool MACROS = a.rho_out != nullptr;
     constexpr int D = Lat<Q>::D;
-    using T = typename Store<S>::T;
-    T v[Q];
-    load_field<Q, S, LOCAL, true>(static_cast<const S*>(a.src), a.L, i, v);
     S* out = static_cast<S*>(a.dst);
     if constexpr (MODE == 0) {
         double f[Q], F[3], rho, vel[3];
@@ -366,6 +432,15 @@ __device__ __forceinline__ void single_node(const StepArgs& a, int i) {
     }
 }
 
+
+template <int Q, class S, int MODE, bool TRT, bool LOCAL>
+__device__ __forceinline__ void single_node(const StepArgs& a, int i) {
+    using T = typename Store<S>::T;
+    T v[Q];
+    load_field<Q, S, LOCAL, true>(static_cast<const S*>(a.src), a.L, i, v);
+    single_node_values<Q, S, MODE, TRT>(a, i, v);
+}
+
 // resident blocks per SM asked of the register allocator: the shifted formats
 // are HBM-latency bound, and 5 blocks (51 registers, no spills) keep more loads in
 // flight than the 4 the allocator picks by itself (FP16 256^3: 38.2 -> 39.6 GLUPS)
@@ -378,6 +453,26 @@ template <int Q, class S, int MODE, bool TRT, bool LOCAL>
 __global__ void __launch_bounds__(kBlock, single_min_blocks<S>()) k_single(StepArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.L.nf) single_node<Q, S, MODE, TRT, LOCAL>(a, i);
+}
+
+// k_single on a persistent grid with the pull table staged through shared memory
+// by the tensor copy engine (bclbm_stage.cuh; pull_map describes L.pull as
+// [Q-1][nf_pad] int32): the steps after the first of the native-FP64 (FMA)
+// kernel.  At one resident block per SM (146 registers) that kernel cannot hide
+// the table -> gather latency chain with other warps, and staging the table one
+// sub-tile ahead is measured faster; the shifted-storage and fixed-point kernels
+// keep 24-40 warps per SM, hide it already, and measured slower staged (the
+// pipeline's loop state, shared-memory reads and wait cost more than it saves).
+template <int Q, class S, bool TRT>
+__global__ void __launch_bounds__(kBlock, 1) k_single_staged(StepArgs a, const __grid_constant__ CUtensorMap pull_map) {
+    __shared__ stage::WarpStage<Q - 1, kBlock / 32> st;
+    stage::staged_warps<Q - 1, kBlock / 32>(st, &pull_map, a.L.nf, a.fx_flag,
+                                            [&](int i, const int32_t(*rows)[stage::kSub], int lane) {
+                                                typename Store<S>::T v[Q];
+                                                load_field_staged<Q, S, stage::kSub>(static_cast<const S*>(a.src),
+                                                                                     a.L, i, rows, lane, v);
+                                                single_node_values<Q, S, 1, TRT>(a, i, v);
+                                            });
 }
 
 // ---------------------------------------------------------------------------
@@ -393,12 +488,10 @@ __global__ void __launch_bounds__(kBlock, single_min_blocks<S>()) k_single(StepA
 #define BCLBM_FX_MINB 3
 #endif
 
-template <int Q, bool TRT, bool LOCAL>
-__device__ __forceinline__ void fixed_node(const StepArgs& a, int i) {
+// one update of slot i from its pulled values X (the int64 state of Store<int64_t>)
+template <int Q, bool TRT>
+__device__ __forceinline__ void fixed_node_values(const StepArgs& a, int i, int64_t* X) {
     constexpr int D = Lat<Q>::D;
-    // the state is held in the collision's int64 format (Store<int64_t>)
-    int64_t X[Q];
-    load_field<Q, int64_t, LOCAL, true>(static_cast<const int64_t*>(a.src), a.L, i, X);
     int ovf = 0;
     int64_t rho, u[3];
     int64_t* out = static_cast<int64_t*>(a.dst) + i;
@@ -410,6 +503,13 @@ __device__ __forceinline__ void fixed_node(const StepArgs& a, int i) {
         for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * a.L.nf_pad + i] = fx::store_f64(u[d]);
     }
     if (ovf) atomicOr(a.fx_flag, 1);
+}
+
+template <int Q, bool TRT, bool LOCAL>
+__device__ __forceinline__ void fixed_node(const StepArgs& a, int i) {
+    int64_t X[Q];
+    load_field<Q, int64_t, LOCAL, true>(static_cast<const int64_t*>(a.src), a.L, i, X);
+    fixed_node_values<Q, TRT>(a, i, X);
 }
 
 template <int Q, bool TRT, bool LOCAL>

@@ -27,8 +27,15 @@ cudaError_t launch_single_exact(int Q, bool trt, bool local, const StepArgs& a, 
 cudaError_t launch_rk_f64(int Q, bool local, bool sums, const StepArgs& a, cudaStream_t s, bool density);
 
 // bclbm_kernels.cu
-cudaError_t launch_single_fast(int Q, int precision, bool trt, bool local, const StepArgs& a, cudaStream_t s);
+// pull_map: the tensor map of the handle's pull table (encode_table_map), which
+// the native-FP64 steps after the first stage through shared memory; NULL: the
+// unstaged kernel
+cudaError_t launch_single_fast(int Q, int precision, bool trt, bool local, const StepArgs& a,
+                               const CUtensorMap* pull_map, cudaStream_t s);
 cudaError_t launch_single_fixed(int Q, bool trt, bool local, const StepArgs& a, cudaStream_t s);
+// the tensor map of a [rows][pad] int32 table read in boxes of 32 slots x rows
+// (pad a multiple of 64, the table 16-byte aligned)
+cudaError_t encode_table_map(const int32_t* table, int pad, int rows, CUtensorMap* out);
 cudaError_t launch_rk_shift(int Q, int precision, bool local, bool sums, const StepArgs& a, cudaStream_t s,
                             bool density);
 cudaError_t launch_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params, cudaStream_t s);

@@ -17,30 +17,7 @@ namespace {
 
 template <int Q>
 fx::Consts make_consts(bool trt, double tau, double tau_anti, const double* F) {
-    using L = Lat<Q>;
-    fx::Consts K;
-    std::memset(&K, 0, sizeof(K));
-    const double oms = 1.0 / tau, oma = trt ? 1.0 / tau_anti : oms;
-    const double tsf = 1 - 0.5 / tau, taf = trt ? 1 - 0.5 / tau_anti : tsf;
-    K.alpha = fx::param(1.0 - 0.5 * (oms + oma));
-    K.beta = fx::param(0.5 * (oma - oms));
-    K.alpha_rest = fx::param(1.0 - oms);
-    const double wc[3] = {L::w(L::REST), L::w(0), L::w(L::NP - 1)};
-    for (int c = 0; c < 3; ++c) {
-        K.oms_w[c] = fx::param(oms * wc[c]);
-        K.oma3_w[c] = fx::param(3.0 * oma * wc[c]);
-        K.ktsf_w[c] = fx::param(-3.0 * wc[c] * tsf);
-    }
-    for (int q = 0; q < Q; ++q) {
-        const double cF = L::cx(q) * F[0] + L::cy(q) * F[1] + L::cz(q) * F[2];
-        K.kf9[q] = fx::param(9.0 * L::w(q) * tsf * cF);
-        K.ka3[q] = fx::param(3.0 * L::w(q) * taf * cF);
-    }
-    for (int d = 0; d < 3; ++d) {
-        K.force[d] = fx::param(F[d]);
-        K.half_force[d] = fx::param(0.5 * F[d]);
-    }
-    return K;
+    return fx::make_consts<Q>(trt, tau, tau_anti, F);
 }
 
 template <int Q, bool TRT>
@@ -92,9 +69,8 @@ int run(int n_nodes, const int32_t* neigh, const int16_t* types, int n_bulk, con
 
 extern "C" int fx_collide_ovf(double scale) {
     // one D3Q19 rest-state node at rho = scale: does the collision flag it?
-    fx::Consts K;
-    std::memset(&K, 0, sizeof(K));
-    K.alpha = K.alpha_rest = fx::param(-0.25);
+    const double F0[3] = {0.0, 0.0, 0.0};
+    const fx::Consts K = fx::make_consts<19>(false, 0.8, 0.8, F0);
     int ovf = 0;
     int64_t F[19];
     for (int q = 0; q < 19; ++q) F[q] = fx::from_f64(Lat<19>::w(q) * scale, ovf);
