@@ -72,7 +72,8 @@ struct Plan {
 
 // full: also the stream-map checks (rest neighbour, symmetry), unless device_links:
 // bclbm_create then runs them on the device (k_check_links) from the uploaded rows
-int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full, bool device_links = false) {
+// The descriptor's own fields (no table is read).
+int validate_descriptor(const bclbm_desc* d, std::string& err) {
     if (!d) { err = "null descriptor"; return BCLBM_ERR_INVALID; }
     const int Q = d->lattice_q;
     if (Q != 9 && Q != 19) { err = "lattice_q must be 9 or 19"; return BCLBM_ERR_INVALID; }
@@ -95,9 +96,16 @@ int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full,
         return BCLBM_ERR_INVALID;
     }
     if ((d->flags & BCLBM_FLAG_SFC_ORDER) && !d->pos) { err = "BCLBM_FLAG_SFC_ORDER needs pos"; return BCLBM_ERR_INVALID; }
+    if (d->n_bulk >= d->n_nodes) { err = "n_bulk must be smaller than n_nodes"; return BCLBM_ERR_INVALID; }
+    return BCLBM_OK;
+}
+
+int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full, bool device_links = false) {
+    const int vrc = validate_descriptor(d, err);
+    if (vrc) return vrc;
+    const int Q = d->lattice_q;
     const int N = d->n_nodes;
     const int nb = d->n_bulk;
-    if (nb >= N) { err = "n_bulk must be smaller than n_nodes"; return BCLBM_ERR_INVALID; }
     p.nfields = d->collision == BCLBM_RK ? 2 : 1;
     const int32_t* nbr = d->neigh;
     const int16_t* ty = d->types;
@@ -241,6 +249,34 @@ int validate_and_plan(const bclbm_desc* d, Plan& p, std::string& err, bool full,
               std::to_string(v % 32);
         return BCLBM_ERR_TABLE;
     }
+    return BCLBM_OK;
+}
+
+// The plan of the common case, checked on the host only as far as the host must:
+// a single-phase descriptor whose bulk list is the contiguous, increasing run
+// bulk[0] .. bulk[0] + n_bulk - 1 (vtklb.py numbers the fluid nodes first), kept in
+// reference order.  Slot s then holds node bulk[0] + s, and bclbm_create runs every
+// table check (neighbour ids in range, node types against the bulk list, rest
+// neighbour, one-to-one stream map) on the device over the uploaded rows.  Returns
+// -1 when the bulk list is not such a run.
+int validate_affine(const bclbm_desc* d, Plan& p) {
+    if (!d || !d->bulk || d->n_bulk < 1 || d->n_nodes < 2) return -1;
+    const int N = d->n_nodes, nb = d->n_bulk;
+    const int64_t b0 = d->bulk[0];
+    if (b0 < 1 || b0 + nb > N) return -1;
+    FirstBad bad;
+    parallel_for(static_cast<size_t>(nb), [&](size_t k0, size_t k1) {
+        for (size_t k = k0; k < k1; ++k)
+            if (d->bulk[k] != b0 + static_cast<int64_t>(k)) {
+                bad.set(static_cast<int64_t>(k));
+                return;
+            }
+    });
+    if (bad.any()) return -1;
+    p.nfields = 1;
+    p.nf = nb;
+    p.nf_pad = (nb + 63) / 64 * 64;
+    p.ns = 0;
     return BCLBM_OK;
 }
 
@@ -417,7 +453,7 @@ __global__ void k_build_pull(const int32_t* __restrict__ rows, const int32_t* __
 // The stream-map checks of validate_and_plan on the device, for a contiguous bulk
 // list (rows [n_bulk][Q] of nodes b0 .. b0 + n_bulk - 1): the rest neighbour of each
 // fluid node is the node itself, and a fluid upstream neighbour y = neighbor(rev q, n)
-// has neighbor(q, y) = n.  bad[0] / bad[1]: the smallest failing bulk index / b*32+q.
+// has neighbor(q, y) = n.  bad[0] / bad[1]: the smallest failing bulk index.
 __global__ void k_check_links(const int32_t* __restrict__ rows, const int16_t* __restrict__ types, int b0, int nf,
                               int Q, int* bad) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -432,9 +468,80 @@ __global__ void k_check_links(const int32_t* __restrict__ rows, const int16_t* _
         const int rq = Q == 9 ? (q + 4) % 8 : (q + 9) % 18;
         const int y = row[rq];
         if (y != 0 && types[y] > 1 && rows[static_cast<size_t>(y - b0) * Q + q] != n) {
-            atomicMin(bad + 1, b * 32 + q);
+            atomicMin(bad + 1, b);
             return;
         }
+    }
+}
+
+// The table checks of an affine handle (bulk list = nodes b0 .. b0 + nf - 1) on the
+// device, one thread per node and per bulk row; every access is bounds-checked
+// before it indexes anything.  bad[2]: smallest bulk index whose node is not
+// fluid (type 2 or 3); bad[3]: smallest fluid node outside the bulk list;
+// bad[4]: smallest bulk index with a neighbour id out of [0, n_nodes).  ghost[p]:
+// largest bulk index whose neighbour along c_p is node 0 (the ghost source).
+// Also writes slot_bulk[s] = s.
+__global__ void k_prepare_affine(const int32_t* __restrict__ rows, const int16_t* __restrict__ types, int n_nodes,
+                                 int b0, int nf, int Q, int* bad, int* ghost, int32_t* slot_bulk) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 1 && t < n_nodes) {
+        const int ty = types[t];
+        const bool inside = t >= b0 && t - b0 < nf;
+        if (inside && ty != 2 && ty != 3) atomicMin(bad + 2, t - b0);
+        if (!inside && ty > 1) atomicMin(bad + 3, t);
+    }
+    if (t < nf) {
+        slot_bulk[t] = t;
+        const int32_t* row = rows + static_cast<size_t>(t) * Q;
+        for (int q = 0; q < Q; ++q) {
+            const int y = row[q];
+            if (y < 0 || y >= n_nodes) atomicMin(bad + 4, t);
+            else if (y == 0 && q < Q - 1) atomicMax(ghost + q, t);
+        }
+    }
+}
+
+// k_check_links for an affine handle: a node y is fluid exactly when b0 <= y <
+// b0 + nf (k_prepare_affine checks the types against that), so no node type is
+// read and no row outside the uploaded bulk rows is indexed.  bad[0] / bad[1]:
+// smallest bulk index with a wrong rest neighbour / an asymmetric link.
+__global__ void k_check_links_affine(const int32_t* __restrict__ rows, int b0, int nf, int Q, int* bad) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nf) return;
+    const int n = b0 + b, R = Q - 1;
+    const int32_t* row = rows + static_cast<size_t>(b) * Q;
+    if (row[R] != n) {
+        atomicMin(bad, b);
+        return;
+    }
+    for (int q = 0; q < R; ++q) {
+        const int rq = Q == 9 ? (q + 4) % 8 : (q + 9) % 18;
+        const int y = row[rq];
+        if (y >= b0 && y - b0 < nf && rows[static_cast<size_t>(y - b0) * Q + q] != n) {
+            atomicMin(bad + 1, b);
+            return;
+        }
+    }
+}
+
+// k_build_pull for an affine handle: upstream fluid y is slot y - b0; node 0 gives
+// the ghost source (device array from k_prepare_affine); anything else is a wall
+// (bounce-back of the node's own reversed value).  An out-of-range id (reported
+// by k_prepare_affine) is treated as a wall and never dereferenced.
+__global__ void k_build_pull_affine(const int32_t* __restrict__ rows, const int* __restrict__ ghost,
+                                    int32_t* __restrict__ tab, int b0, int nf, int nf_pad, int Q) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nf) return;
+    const int32_t* row = rows + static_cast<size_t>(s) * Q;
+    const int R = Q - 1;
+    for (int q = 0; q < R; ++q) {
+        const int rq = Q == 9 ? (q + 4) % 8 : (q + 9) % 18;
+        const int y = row[rq];
+        int64_t e;
+        if (y >= b0 && y - b0 < nf) e = static_cast<int64_t>(q) * nf_pad + (y - b0);
+        else if (y == 0) e = static_cast<int64_t>(rq) * nf_pad + max(ghost[rq], 0);
+        else e = static_cast<int64_t>(rq) * nf_pad + s;
+        tab[static_cast<size_t>(q) * nf_pad + s] = static_cast<int32_t>(e);
     }
 }
 
@@ -637,7 +744,10 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     const bool device_links = have_gpu && d && d->bulk && d->n_bulk > 0 && d->collision != BCLBM_RK &&
                               d->collision != BCLBM_LINKS &&
                               static_cast<int64_t>(d->bulk[d->n_bulk - 1]) - d->bulk[0] + 1 == d->n_bulk;
-    int rc = validate_and_plan(d, p, err, true, device_links);
+    // the common case: the bulk list is one run in reference order; its tables are
+    // checked and resolved on the device and the node <-> slot maps are implicit
+    const bool affine = device_links && !(d->flags & BCLBM_FLAG_SFC_ORDER) && validate_affine(d, p) == BCLBM_OK;
+    int rc = affine ? validate_descriptor(d, err) : validate_and_plan(d, p, err, true, device_links);
     if (rc) {
         std::fprintf(stderr, "bclbm_create: %s\n", err.c_str());
         return rc;
@@ -675,11 +785,15 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     h->rho_ref = d->rho_ref > 0 ? d->rho_ref : 1.0;
     h->scale = d->store_scale > 0 ? d->store_scale : (d->precision == BCLBM_F16 ? 4096.0 : 1.0);
     for (int k = 0; k < 3; ++k) h->force[k] = d->force[k];
-    h->slot_node = std::move(p.slot_node);
-    h->slot_bulk = std::move(p.slot_bulk);
-    h->bulk.assign(d->bulk, d->bulk + d->n_bulk);
-    h->solid_node = std::move(p.solid_node);
-    h->bulk_contiguous = (h->bulk.back() - h->bulk.front() + 1) == d->n_bulk;
+    h->affine = affine;
+    h->bulk0 = d->bulk[0];
+    if (!affine) {
+        h->slot_node = std::move(p.slot_node);
+        h->slot_bulk = std::move(p.slot_bulk);
+        h->bulk.assign(d->bulk, d->bulk + d->n_bulk);
+        h->solid_node = std::move(p.solid_node);
+    }
+    h->bulk_contiguous = static_cast<int64_t>(d->bulk[d->n_bulk - 1]) - d->bulk[0] + 1 == d->n_bulk;
     cudaGetDevice(&h->device);
 
     const int Q = h->q, D = h->nd, R = Q - 1;
@@ -699,12 +813,13 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     } while (0)
 
     // ghost sources: last bulk node (bulk order) whose neighbour along c_p is node 0
-    std::vector<int32_t> slot_of_bulk(h->nf);
-    parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
-        for (size_t s = s0; s < s1; ++s) slot_of_bulk[h->slot_bulk[s]] = static_cast<int32_t>(s);
-    });
+    // (an affine handle finds them on the device, k_prepare_affine)
     for (int pdir = 0; pdir < 19; ++pdir) h->ghost_src[pdir] = 0;
-    {
+    if (!affine) {
+        std::vector<int32_t> slot_of_bulk(h->nf);
+        parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
+            for (size_t s = s0; s < s1; ++s) slot_of_bulk[h->slot_bulk[s]] = static_cast<int32_t>(s);
+        });
         std::atomic<int> last[19];
         for (auto& x : last) x.store(-1);
         parallel_for(static_cast<size_t>(h->nf), [&](size_t b0, size_t b1) {
@@ -804,43 +919,58 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_params), sizeof(DevParams), h->stream));
     CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_partials), (static_cast<size_t>(grid_for(h->nf)) * 6 + 64) * sizeof(double), h->stream));
     CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_red), 16 * sizeof(double), h->stream));
-    CREATE_TRY(cudaMemcpyAsync(h->d_slot_bulk, h->slot_bulk.data(), h->nf * sizeof(int32_t), cudaMemcpyHostToDevice,
-                               h->stream));
+    if (!affine)
+        CREATE_TRY(cudaMemcpyAsync(h->d_slot_bulk, h->slot_bulk.data(), h->nf * sizeof(int32_t),
+                                   cudaMemcpyHostToDevice, h->stream));
     if (!device_table) {
         CREATE_TRY(cudaMemcpyAsync(h->d_nbr, tab.data(), tab.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
                                    h->stream));
     } else {
-        // the bulk nodes' neighbour rows, the node types and the node -> slot map go up as
-        // they are; the table is resolved on the device
+        // the bulk nodes' neighbour rows and the node types go up as they are (and, for
+        // a plan with explicit maps, the node -> slot map); the table is checked and
+        // resolved on the device
         const size_t nrow = static_cast<size_t>(h->nf) * Q;
         int32_t* rows = nullptr;
         int16_t* dty = nullptr;
         int32_t* dext = nullptr;
+        int* dbad = nullptr;  // [5] error slots, then [19] ghost sources
         cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&rows), nrow * sizeof(int32_t), h->stream);
         if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&dty), static_cast<size_t>(d->n_nodes) * sizeof(int16_t), h->stream);
-        if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&dext), static_cast<size_t>(d->n_nodes) * sizeof(int32_t), h->stream);
+        if (e == cudaSuccess && !affine)
+            e = cudaMallocAsync(reinterpret_cast<void**>(&dext), static_cast<size_t>(d->n_nodes) * sizeof(int32_t), h->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(h->d_nbr, 0, ntab * sizeof(int32_t), h->stream);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(rows, d->neigh + static_cast<size_t>(h->bulk.front()) * Q, nrow * sizeof(int32_t),
+            e = cudaMemcpyAsync(rows, d->neigh + static_cast<size_t>(h->bulk0) * Q, nrow * sizeof(int32_t),
                                 cudaMemcpyHostToDevice, h->stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(dty, d->types, static_cast<size_t>(d->n_nodes) * sizeof(int16_t),
                                 cudaMemcpyHostToDevice, h->stream);
-        if (e == cudaSuccess)
+        if (e == cudaSuccess && !affine)
             e = cudaMemcpyAsync(dext, p.ext_of_node.data(), static_cast<size_t>(d->n_nodes) * sizeof(int32_t),
                                 cudaMemcpyHostToDevice, h->stream);
-        int* dbad = nullptr;
-        const int none[2] = {INT32_MAX, INT32_MAX};
-        int bad[2] = {INT32_MAX, INT32_MAX};
-        if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&dbad), sizeof(none), h->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(dbad, none, sizeof(none), cudaMemcpyHostToDevice, h->stream);
+        int init[24];
+        for (int k = 0; k < 5; ++k) init[k] = INT32_MAX;
+        for (int k = 5; k < 24; ++k) init[k] = -1;
+        int bad[24];
+        std::memcpy(bad, init, sizeof(bad));
+        if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&dbad), sizeof(init), h->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dbad, init, sizeof(init), cudaMemcpyHostToDevice, h->stream);
         if (e == cudaSuccess) {
-            k_check_links<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, dty, h->bulk.front(), h->nf, Q, dbad);
-            GhostSrc g;
-            for (int k = 0; k < 19; ++k) g.v[k] = h->ghost_src[k];
-            k_build_pull<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, h->d_slot_bulk, dty, dext, g, h->d_nbr, h->nf,
-                                                                    h->nf_pad, Q);
-            launch_counter() += 2;
+            if (affine) {
+                k_prepare_affine<<<grid_for(std::max(d->n_nodes, h->nf)), kBlock, 0, h->stream>>>(
+                    rows, dty, d->n_nodes, h->bulk0, h->nf, Q, dbad, dbad + 5, h->d_slot_bulk);
+                k_check_links_affine<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, h->bulk0, h->nf, Q, dbad);
+                k_build_pull_affine<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, dbad + 5, h->d_nbr, h->bulk0,
+                                                                                h->nf, h->nf_pad, Q);
+                launch_counter() += 3;
+            } else {
+                k_check_links<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, dty, h->bulk0, h->nf, Q, dbad);
+                GhostSrc g;
+                for (int k = 0; k < 19; ++k) g.v[k] = h->ghost_src[k];
+                k_build_pull<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, h->d_slot_bulk, dty, dext, g, h->d_nbr,
+                                                                        h->nf, h->nf_pad, Q);
+                launch_counter() += 2;
+            }
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = cudaMemcpyAsync(bad, dbad, sizeof(bad), cudaMemcpyDeviceToHost, h->stream);
@@ -851,15 +981,50 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         if (dext) cudaFreeAsync(dext, h->stream);
         if (dbad) cudaFreeAsync(dbad, h->stream);
         CREATE_TRY(e);
-        if (bad[0] != INT32_MAX || bad[1] != INT32_MAX) {
-            if (bad[0] != INT32_MAX)
-                std::fprintf(stderr, "bclbm_create: rest-direction neighbour of node %d is not the node itself\n",
-                             d->bulk[bad[0]]);
-            else
-                std::fprintf(stderr, "bclbm_create: neighbour table not symmetric at node %d direction %d\n",
-                             d->bulk[bad[1] / 32], bad[1] % 32);
+        // reported in the host's order of checks: ids in range, bulk list, missing
+        // fluid nodes, rest neighbour, stream-map symmetry
+        const int32_t* nb_rows = d->neigh + static_cast<size_t>(h->bulk0) * Q;
+        if (bad[4] != INT32_MAX) {
+            int qd = 0;
+            for (int q = 0; q < Q; ++q) {
+                const int y = nb_rows[static_cast<size_t>(bad[4]) * Q + q];
+                if (y < 0 || y >= d->n_nodes) {
+                    qd = q;
+                    break;
+                }
+            }
+            std::fprintf(stderr, "bclbm_create: neighbour id out of range at entry %lld\n",
+                         static_cast<long long>(h->bulk0 + bad[4]) * Q + qd);
             return cleanup(BCLBM_ERR_TABLE);
         }
+        if (bad[2] != INT32_MAX) {
+            std::fprintf(stderr, "bclbm_create: bulk node %d is not own-rank fluid\n", h->bulk0 + bad[2]);
+            return cleanup(BCLBM_ERR_TABLE);
+        }
+        if (bad[3] != INT32_MAX) {
+            std::fprintf(stderr, "bclbm_create: fluid node %d missing from the bulk list\n", bad[3]);
+            return cleanup(BCLBM_ERR_TABLE);
+        }
+        if (bad[0] != INT32_MAX) {
+            std::fprintf(stderr, "bclbm_create: rest-direction neighbour of node %d is not the node itself\n",
+                         h->bulk0 + bad[0]);
+            return cleanup(BCLBM_ERR_TABLE);
+        }
+        if (bad[1] != INT32_MAX) {
+            const int n = h->bulk0 + bad[1];
+            int qd = 0;
+            for (int q = 0; q < Q - 1; ++q) {
+                const int y = nb_rows[static_cast<size_t>(bad[1]) * Q + rev_dir(Q, q)];
+                if (y >= h->bulk0 && y - h->bulk0 < h->nf && d->neigh[static_cast<size_t>(y) * Q + q] != n) {
+                    qd = q;
+                    break;
+                }
+            }
+            std::fprintf(stderr, "bclbm_create: neighbour table not symmetric at node %d direction %d\n", n, qd);
+            return cleanup(BCLBM_ERR_TABLE);
+        }
+        if (affine)
+            for (int k = 0; k < R; ++k) h->ghost_src[k] = std::max(bad[5 + k], 0);
     }
     DevParams prm;
     std::memset(&prm, 0, sizeof(prm));
@@ -948,7 +1113,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         cudaError_t e = cudaMemsetAsync(h->pops[0], 0, static_cast<size_t>(h->nfields) * Q * pad * store_bytes(h->precision),
                                         h->stream);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(tmp, d->f_init + static_cast<size_t>(h->bulk.front()) * es, naos * sizeof(double),
+            e = cudaMemcpyAsync(tmp, d->f_init + static_cast<size_t>(h->bulk0) * es, naos * sizeof(double),
                                 cudaMemcpyHostToDevice, h->stream);
         if (e == cudaSuccess) {
             k_upload_aos<<<grid_for(h->nf), kBlock, 0, h->stream>>>(tmp, h->d_slot_bulk, h->pops[0], h->nf, h->nf_pad, Q,
@@ -1119,7 +1284,7 @@ int bclbm_download_f(bclbm_handle* h, double* f) {
     const int es = h->nfields * h->q;
     const size_t n = static_cast<size_t>(h->nf) * es;
     if (h->bulk_contiguous) {
-        CUDA_TRY(h, cudaMemcpyAsync(f + static_cast<size_t>(h->bulk.front()) * es, h->d_gather, n * sizeof(double),
+        CUDA_TRY(h, cudaMemcpyAsync(f + static_cast<size_t>(h->bulk0) * es, h->d_gather, n * sizeof(double),
                                     cudaMemcpyDeviceToHost, h->stream));
         CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     } else {
@@ -1176,7 +1341,7 @@ int bclbm_macros_collect(bclbm_handle* h, double* rho, double* vel, double* cg) 
     const bool rk = h->collision == BCLBM_RK;
     parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
         for (size_t s = s0; s < s1; ++s) {
-            const size_t n = static_cast<size_t>(h->slot_node[s]);
+            const size_t n = static_cast<size_t>(slot_node_of(h, s));
             if (rho)
                 for (int k = 0; k < h->nfields; ++k) rho[n * h->nfields + k] = r[k * pad + s];
             if (vel)
@@ -1201,7 +1366,7 @@ int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg)
                                                                 h->nf_pad, h->nfields, h->nd);
         launch_counter()++;
         CUDA_TRY(h, cudaGetLastError());
-        const size_t b0 = static_cast<size_t>(h->bulk.front()), nr = static_cast<size_t>(h->nf) * h->nfields;
+        const size_t b0 = static_cast<size_t>(h->bulk0), nr = static_cast<size_t>(h->nf) * h->nfields;
         CUDA_TRY(h, cudaMemcpyAsync(rho + b0 * h->nfields, h->d_gather, nr * sizeof(double), cudaMemcpyDeviceToHost,
                                     h->stream));
         CUDA_TRY(h, cudaMemcpyAsync(vel + b0 * h->nd, h->d_gather + nr, static_cast<size_t>(h->nf) * h->nd * sizeof(double),
@@ -1282,7 +1447,13 @@ int bclbm_pressure_flux(bclbm_handle* h, double q[2]) {
 
 int bclbm_node_perm(bclbm_handle* h, int32_t* out) {
     if (!h || !out) return BCLBM_ERR_INVALID;
-    std::memcpy(out, h->slot_node.data(), h->slot_node.size() * sizeof(int32_t));
+    if (h->affine) {
+        parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {
+            for (size_t s = s0; s < s1; ++s) out[s] = h->bulk0 + static_cast<int32_t>(s);
+        });
+    } else {
+        std::memcpy(out, h->slot_node.data(), h->slot_node.size() * sizeof(int32_t));
+    }
     return BCLBM_OK;
 }
 

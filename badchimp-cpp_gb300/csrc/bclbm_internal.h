@@ -27,6 +27,10 @@ struct bclbm_handle {
     std::vector<int32_t> solid_node;  // extended solid index -> reference node number
     std::vector<double> solid_cg;     // RK colour of the stored solids
     bool bulk_contiguous = false;
+    // affine numbering: the bulk list is nodes bulk0 .. bulk0 + nf - 1 in reference
+    // order, so slot s holds node bulk0 + s and slot_node / slot_bulk / bulk stay empty
+    bool affine = false;
+    int32_t bulk0 = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
     void* pops[2] = {nullptr, nullptr};
@@ -79,4 +83,8 @@ struct bclbm_handle {
 namespace bclbm {
 // kernel arguments of a handle's current configuration (src/dst left for the caller)
 StepArgs handle_args(const bclbm_handle* h);
+// reference node number of device slot s
+inline int32_t slot_node_of(const bclbm_handle* h, size_t s) {
+    return h->affine ? h->bulk0 + static_cast<int32_t>(s) : h->slot_node[s];
+}
 }  // namespace bclbm

@@ -231,3 +231,37 @@ def test_device_checks_reject_bad_tables(bclbm, gpu):
     # the unmodified tables still create
     with L.Solver(lat, L.initiate_single(lat, np.ones(lat.n_nodes)), tau=(0.8, 0.8)) as s:
         s.step(2)
+
+
+def test_device_checks_of_a_contiguous_bulk_list(bclbm, gpu):
+    """A bulk list that is one run of nodes in reference order is checked on the
+    device only: a neighbour id out of range in a fluid row, a bulk node whose
+    type is solid and a fluid node outside the bulk list are each
+    BCLBM_ERR_TABLE (the ids are range-checked before anything is indexed)."""
+    case = lbcases.Case("pack_20", bclbm)
+    lat = case.lat
+    L = bclbm.lbsolver
+    N = bclbm.native
+    assert np.array_equal(lat.bulk, np.arange(1, lat.n_bulk + 1))
+    f0 = L.initiate_single(lat, np.ones(lat.n_nodes))
+    bad_tables = []
+    neigh = lat.neigh.copy().reshape(-1, 19)
+    neigh[int(lat.bulk[11]), 4] = lat.n_nodes + 7
+    bad_tables.append((neigh.reshape(-1), lat.types))
+    neigh = lat.neigh.copy().reshape(-1, 19)
+    neigh[int(lat.bulk[12]), 6] = -3
+    bad_tables.append((neigh.reshape(-1), lat.types))
+    types = lat.types.copy()
+    types[int(lat.bulk[30])] = 1  # a listed node that is not fluid
+    bad_tables.append((lat.neigh, types))
+    types = lat.types.copy()
+    types[lat.n_bulk + 3] = 3  # a stored solid marked fluid, outside the bulk list
+    bad_tables.append((lat.neigh, types))
+    for neigh, types in bad_tables:
+        bad = L.Lattice(19, neigh, types, lat.pos, lat.bulk)
+        with pytest.raises(N.BclbmError) as e:
+            L.Solver(bad, f0, tau=(0.8, 0.8))
+        assert e.value.status == -2
+    with L.Solver(lat, f0, tau=(0.8, 0.8)) as s:
+        s.step(3)
+        assert not s.reduce()["nonfinite"]
