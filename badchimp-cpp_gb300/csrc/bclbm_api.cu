@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <numeric>
 #include <string>
@@ -29,6 +30,52 @@ using bclbm::host::parallel_for;
 
 
 namespace {
+
+// The library's stream-ordered memory pool of each device.  Its release threshold
+// is unlimited: device memory that bclbm_destroy frees stays mapped in the pool,
+// and the next bclbm_create on the device takes it without mapping new pages
+// (mapping several GB costs tens of ms; with the default pool, any device-wide
+// synchronisation of the caller's gives freed memory back).  bclbm_trim returns
+// it.  The caller's own stream-ordered allocations (the device's default pool)
+// are not affected.
+constexpr int kMaxPoolDevices = 64;
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pool[kMaxPoolDevices] = {};
+
+cudaError_t library_pool(cudaMemPool_t* out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxPoolDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (!g_pool[dev]) {
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        e = cudaMemPoolCreate(&pool, &props);
+        if (e != cudaSuccess) return e;
+        uint64_t threshold = UINT64_MAX;
+        e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+        if (e != cudaSuccess) {
+            cudaMemPoolDestroy(pool);
+            return e;
+        }
+        g_pool[dev] = pool;
+    }
+    *out = g_pool[dev];
+    return cudaSuccess;
+}
+
+// cudaMallocAsync from the library's pool of the current device
+cudaError_t pool_malloc(void** p, size_t bytes, cudaStream_t s) {
+    cudaMemPool_t pool = nullptr;
+    const cudaError_t e = library_pool(&pool);
+    if (e != cudaSuccess) return e;
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
 
 size_t store_bytes(int precision) {
     switch (precision) {
@@ -649,7 +696,7 @@ void free_all(bclbm_handle* h) {
 
 int run_gather(bclbm_handle* h) {
     const size_t n = static_cast<size_t>(h->nf) * h->nfields * h->q;
-    if (!h->d_gather) CUDA_TRY(h, cudaMallocAsync(reinterpret_cast<void**>(&h->d_gather), n * sizeof(double), h->stream));
+    if (!h->d_gather) CUDA_TRY(h, pool_malloc(reinterpret_cast<void**>(&h->d_gather), n * sizeof(double), h->stream));
     StepArgs a = make_args(h);
     a.src = h->pops[h->cur];
     if (h->collision == BCLBM_LINKS) {
@@ -903,22 +950,22 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     CREATE_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     const size_t sb = store_bytes(h->precision);
     const size_t pop_bytes = static_cast<size_t>(h->nfields) * Q * pad * sb;
-    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->pops[0]), pop_bytes, h->stream));
-    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->pops[1]), pop_bytes, h->stream));
+    CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->pops[0]), pop_bytes, h->stream));
+    CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->pops[1]), pop_bytes, h->stream));
     const size_t ntab = device_table ? static_cast<size_t>(R) * pad : tab.size();
-    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_nbr), ntab * sizeof(int32_t), h->stream));
+    CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_nbr), ntab * sizeof(int32_t), h->stream));
     if ((h->collision == BCLBM_BGK || h->collision == BCLBM_TRT) && ntab == static_cast<size_t>(R) * pad) {
         // the native-FP64 steps after the first stage the pull table through shared
         // memory with the tensor copy engine; without the driver's encoder they read it
         // directly
         h->pull_map_ok = encode_table_map(h->d_nbr, static_cast<int>(pad), R, &h->pull_map) == cudaSuccess;
     }
-    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_slot_bulk), pad * sizeof(int32_t), h->stream));
-    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_rho), static_cast<size_t>(h->nfields) * pad * sizeof(double), h->stream));
-    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_vel), static_cast<size_t>(D) * pad * sizeof(double), h->stream));
-    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_params), sizeof(DevParams), h->stream));
-    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_partials), (static_cast<size_t>(grid_for(h->nf)) * 6 + 64) * sizeof(double), h->stream));
-    CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_red), 16 * sizeof(double), h->stream));
+    CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_slot_bulk), pad * sizeof(int32_t), h->stream));
+    CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_rho), static_cast<size_t>(h->nfields) * pad * sizeof(double), h->stream));
+    CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_vel), static_cast<size_t>(D) * pad * sizeof(double), h->stream));
+    CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_params), sizeof(DevParams), h->stream));
+    CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_partials), (static_cast<size_t>(grid_for(h->nf)) * 6 + 64) * sizeof(double), h->stream));
+    CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_red), 16 * sizeof(double), h->stream));
     if (!affine)
         CREATE_TRY(cudaMemcpyAsync(h->d_slot_bulk, h->slot_bulk.data(), h->nf * sizeof(int32_t),
                                    cudaMemcpyHostToDevice, h->stream));
@@ -934,10 +981,10 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         int16_t* dty = nullptr;
         int32_t* dext = nullptr;
         int* dbad = nullptr;  // [5] error slots, then [19] ghost sources
-        cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&rows), nrow * sizeof(int32_t), h->stream);
-        if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&dty), static_cast<size_t>(d->n_nodes) * sizeof(int16_t), h->stream);
+        cudaError_t e = pool_malloc(reinterpret_cast<void**>(&rows), nrow * sizeof(int32_t), h->stream);
+        if (e == cudaSuccess) e = pool_malloc(reinterpret_cast<void**>(&dty), static_cast<size_t>(d->n_nodes) * sizeof(int16_t), h->stream);
         if (e == cudaSuccess && !affine)
-            e = cudaMallocAsync(reinterpret_cast<void**>(&dext), static_cast<size_t>(d->n_nodes) * sizeof(int32_t), h->stream);
+            e = pool_malloc(reinterpret_cast<void**>(&dext), static_cast<size_t>(d->n_nodes) * sizeof(int32_t), h->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(h->d_nbr, 0, ntab * sizeof(int32_t), h->stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(rows, d->neigh + static_cast<size_t>(h->bulk0) * Q, nrow * sizeof(int32_t),
@@ -953,7 +1000,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         for (int k = 5; k < 24; ++k) init[k] = -1;
         int bad[24];
         std::memcpy(bad, init, sizeof(bad));
-        if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&dbad), sizeof(init), h->stream);
+        if (e == cudaSuccess) e = pool_malloc(reinterpret_cast<void**>(&dbad), sizeof(init), h->stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(dbad, init, sizeof(init), cudaMemcpyHostToDevice, h->stream);
         if (e == cudaSuccess) {
             if (affine) {
@@ -1057,7 +1104,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         auto up = [&](auto** dst, const auto& v, size_t n_min) -> cudaError_t {
             using E = typename std::remove_reference<decltype(v)>::type::value_type;
             const size_t n = std::max(v.size(), n_min);
-            cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(dst), n * sizeof(E), h->stream);
+            cudaError_t e = pool_malloc(reinterpret_cast<void**>(dst), n * sizeof(E), h->stream);
             if (e == cudaSuccess && !v.empty())
                 e = cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice, h->stream);
             return e;
@@ -1070,18 +1117,18 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         CREATE_TRY(up(&h->d_lab_g, lp.lab_g, 1));
         CREATE_TRY(up(&h->d_flux_slot, lp.flux_slot, 1));
         CREATE_TRY(up(&h->d_flux_phase, lp.flux_phase, 1));
-        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_ustore), std::max<size_t>(3 * static_cast<size_t>(h->npress), 1) * sizeof(double), h->stream));
-        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_lab_val), std::max<size_t>(lp.lab_slot.size(), 1) * sizeof(double), h->stream));
-        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_lab_q), (static_cast<size_t>(h->nlab) + 1) * sizeof(double), h->stream));
+        CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_ustore), std::max<size_t>(3 * static_cast<size_t>(h->npress), 1) * sizeof(double), h->stream));
+        CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_lab_val), std::max<size_t>(lp.lab_slot.size(), 1) * sizeof(double), h->stream));
+        CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_lab_q), (static_cast<size_t>(h->nlab) + 1) * sizeof(double), h->stream));
         CREATE_TRY(cudaMemsetAsync(h->d_lab_q, 0, (static_cast<size_t>(h->nlab) + 1) * sizeof(double), h->stream));
-        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_flux_out), 2 * sizeof(double), h->stream));
+        CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_flux_out), 2 * sizeof(double), h->stream));
         CREATE_TRY(cudaStreamSynchronize(h->stream));  // the host vectors go out of scope
     }
 
     // colour field: fluid slots (written every step), stored solids (fixed), ghost (0)
     if (h->collision == BCLBM_RK) {
         const size_t ncg = static_cast<size_t>(h->nf) + h->ns + 1;
-        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_cg), ncg * sizeof(double), h->stream));
+        CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_cg), ncg * sizeof(double), h->stream));
         std::vector<double> cg(ncg, 0.0);
         h->solid_cg.assign(h->ns, 0.0);
         for (int k = 0; k < h->ns; ++k) {
@@ -1095,7 +1142,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         CREATE_TRY(cudaMemcpyAsync(h->d_cg, cg.data(), ncg * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         if (h->precision != BCLBM_F64) {
             std::vector<float> cgf(cg.begin(), cg.end());
-            CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&h->d_cgf), ncg * sizeof(float), h->stream));
+            CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_cgf), ncg * sizeof(float), h->stream));
             CREATE_TRY(cudaMemcpyAsync(h->d_cgf, cgf.data(), ncg * sizeof(float), cudaMemcpyHostToDevice, h->stream));
         }
         CREATE_TRY(cudaStreamSynchronize(h->stream));
@@ -1109,7 +1156,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         const size_t naos = static_cast<size_t>(h->nf) * es;
         const int mode = h->fx_storage ? 1 : (h->precision == BCLBM_F64 ? 0 : 2);
         double* tmp = nullptr;
-        CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&tmp), naos * sizeof(double), h->stream));
+        CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&tmp), naos * sizeof(double), h->stream));
         cudaError_t e = cudaMemsetAsync(h->pops[0], 0, static_cast<size_t>(h->nfields) * Q * pad * store_bytes(h->precision),
                                         h->stream);
         if (e == cudaSuccess)
@@ -1142,7 +1189,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             CREATE_TRY(cudaStreamSynchronize(h->stream));
         } else if (h->fx_storage) {
             double* tmp = nullptr;
-            CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&tmp), nsoa * sizeof(double), h->stream));
+            CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&tmp), nsoa * sizeof(double), h->stream));
             cudaError_t e = cudaMemcpyAsync(tmp, soa.data(), nsoa * sizeof(double), cudaMemcpyHostToDevice, h->stream);
             if (e == cudaSuccess) {
                 k_encode_fx<<<static_cast<unsigned>((nsoa + kBlock - 1) / kBlock), kBlock, 0, h->stream>>>(
@@ -1155,7 +1202,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             CREATE_TRY(e);
         } else {
             double* tmp = nullptr;
-            CREATE_TRY(cudaMallocAsync(reinterpret_cast<void**>(&tmp), nsoa * sizeof(double), h->stream));
+            CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&tmp), nsoa * sizeof(double), h->stream));
             cudaError_t e = cudaMemcpyAsync(tmp, soa.data(), nsoa * sizeof(double), cudaMemcpyHostToDevice, h->stream);
             if (e == cudaSuccess) {
                 k_encode<<<grid_for(h->nf), kBlock, 0, h->stream>>>(tmp, h->pops[0], h->nf, h->nf_pad, Q, h->nfields,
@@ -1196,7 +1243,7 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
         a.vel_out = macros ? h->d_vel : nullptr;
         if (h->collision == BCLBM_LINKS) {
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
-            CUDA_TRY(h, launch_links_step(h->precision, h->exact, local, links_args(h, a), h->stream));
+            CUDA_TRY(h, launch_links_step(h->precision, h->exact, !h->fma64, local, links_args(h, a), h->stream));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
         } else if (h->collision != BCLBM_RK) {
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
@@ -1361,7 +1408,7 @@ int bclbm_download_macros(bclbm_handle* h, double* rho, double* vel, double* cg)
         // straight into the caller's arrays (no pinned staging, no host scatter)
         CUDA_TRY(h, cudaSetDevice(h->device));
         const size_t n = static_cast<size_t>(h->nf) * h->nfields * h->q;
-        if (!h->d_gather) CUDA_TRY(h, cudaMallocAsync(reinterpret_cast<void**>(&h->d_gather), n * sizeof(double), h->stream));
+        if (!h->d_gather) CUDA_TRY(h, pool_malloc(reinterpret_cast<void**>(&h->d_gather), n * sizeof(double), h->stream));
         k_macros_aos<<<grid_for(h->nf), kBlock, 0, h->stream>>>(h->d_rho, h->d_vel, h->d_slot_bulk, h->d_gather, h->nf,
                                                                 h->nf_pad, h->nfields, h->nd);
         launch_counter()++;
@@ -1453,6 +1500,22 @@ int bclbm_node_perm(bclbm_handle* h, int32_t* out) {
         });
     } else {
         std::memcpy(out, h->slot_node.data(), h->slot_node.size() * sizeof(int32_t));
+    }
+    return BCLBM_OK;
+}
+
+int bclbm_trim(void) {
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    for (int dev = 0; dev < kMaxPoolDevices; ++dev) {
+        if (!g_pool[dev]) continue;
+        int cur = 0;
+        if (cudaGetDevice(&cur) != cudaSuccess) return BCLBM_ERR_CUDA;
+        if (cudaSetDevice(dev) != cudaSuccess) return BCLBM_ERR_CUDA;
+        // memory of live handles stays; what destroyed handles left in the pool goes
+        const cudaError_t e = cudaDeviceSynchronize();
+        const cudaError_t t = cudaMemPoolTrimTo(g_pool[dev], 0);
+        cudaSetDevice(cur);
+        if (e != cudaSuccess || t != cudaSuccess) return BCLBM_ERR_CUDA;
     }
     return BCLBM_OK;
 }

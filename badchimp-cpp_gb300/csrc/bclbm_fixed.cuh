@@ -283,6 +283,7 @@ struct Consts {
     int64_t k45;          // 4.5 oms w_diag
     int64_t oma3_w2;      // 3 oma w_diag
     int64_t tsf3_w2;      // 3 w_diag tsf
+    int64_t tso;          // tsf / oms (the mass source's share of the equilibrium density)
     int64_t kf9[19];      // 9 w_q tsf (c_q . F)
     int64_t ka3[19];      // 3 w_q taf (c_q . F)
     int64_t force[3];     // F
@@ -308,6 +309,7 @@ inline Consts make_consts(bool trt, double tau, double tau_anti, const double* F
     K.k45 = param(4.5 * oms * w2);
     K.oma3_w2 = param(3.0 * oma * w2);
     K.tsf3_w2 = param(3.0 * w2 * tsf);
+    K.tso = param(tsf / oms);
     for (int q = 0; q < Q; ++q) {
         const double cF = L::cx(q) * F[0] + L::cy(q) * F[1] + L::cz(q) * F[2];
         K.kf9[q] = param(9.0 * L::w(q) * tsf * cF);
@@ -340,9 +342,16 @@ inline Consts make_consts(bool trt, double tau, double tau_anti, const double* F
 //
 // Weight classes: w_rest : w_axis : w_diag = 12 : 2 : 1 (D3Q19) and 16 : 4 : 1
 // (D2Q9), so the class products are exact multiples of the diagonal one.
-template <int Q, bool TRT, class Sink>
+//
+// SRC = true adds the two terms of the std_one_phase node loop
+// (src/std_one_phase/main.cpp:496-539): the body force is the handle's force
+// times the node's integer force attribute fo, and qm is the node's mass
+// source (calcDeltaOmegaQ, src/lbsolver/LBcollision.h:80-98): rho = sum f +
+// qm/2, and the equilibrium weight oms rho + tsf qm = oms rho_e with
+// rho_e = rho + (tsf/oms) qm, so j_e = rho_e u takes the place of j in X and Y.
+template <int Q, bool TRT, bool SRC = false, class Sink>
 __host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K, int64_t& rho_o, int64_t* u_o,
-                                                    int& ovf, Sink&& sink) {
+                                                    int& ovf, Sink&& sink, int fo = 1, int64_t qm = 0) {
     constexpr int D = Lat<Q>::D, NP = Lat<Q>::NP, R = Lat<Q>::REST;
     constexpr int SH1 = Q == 19 ? 1 : 2;  // w_axis / w_diag = 2 or 4
     {
@@ -356,6 +365,7 @@ __host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K,
         if (t > 108) ovf = 1;
     }
     int64_t rho = F[R];
+    if (SRC) rho += qm >> 1;
     int64_t J[3] = {0, 0, 0};
 #pragma unroll
     for (int k = 0; k < NP; ++k) {
@@ -382,13 +392,21 @@ __host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K,
     int64_t j[3], u[3], u45[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        j[d] = (d < D) ? J[d] + K.half_force[d] : 0;
+        j[d] = (d < D) ? J[d] + (SRC ? K.half_force[d] * fo : K.half_force[d]) : 0;
         u[d] = (d < D) ? mul_su(j[d], inv) : 0;
         u45[d] = (d < D) ? mul_su(u[d], K.k45) : 0;
     }
     rho_o = rho;
 #pragma unroll
     for (int d = 0; d < D; ++d) u_o[d] = u[d];
+    int64_t rho_e = rho;
+    if (SRC && qm != 0) {
+        // j_e = j + (tsf/oms) qm u, rho_e = rho + (tsf/oms) qm
+        const int64_t s = mul_ss(qm, K.tso);
+        rho_e += s;
+#pragma unroll
+        for (int d = 0; d < D; ++d) j[d] += mul_ss(u[d], s);
+    }
     int64_t ju = mul_ss(j[0], u[0]) + mul_ss(j[1], u[1]);
     if (D == 3) ju += mul_ss(j[2], u[2]);
     // u.F over the force's nonzero components (the branches are uniform)
@@ -396,8 +414,9 @@ __host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K,
 #pragma unroll
     for (int d = 0; d < D; ++d)
         if (K.force[d] != 0) uF += mul_ss(u[d], K.force[d]);
-    const int64_t AB2 = mul_su(rho - (ju + (ju >> 1)), K.oms_w2);  // oms w2 (rho - 1.5 j.u)
-    const int64_t K2 = -mul_su(uF, K.tsf3_w2);                    // -3 w2 tsf u.F
+    if (SRC) uF *= fo;
+    const int64_t AB2 = mul_su(rho_e - (ju + (ju >> 1)), K.oms_w2);  // oms w2 (rho_e - 1.5 j.u)
+    const int64_t K2 = -mul_su(uF, K.tsf3_w2);                      // -3 w2 tsf u.F
     // class c values (rest 0, axis 1, diagonal 2) by the exact weight ratios
     auto by_class = [](int64_t v2, int c) -> int64_t {
         return c == 2 ? v2 : (c == 1 ? (v2 << SH1) : (Q == 19 ? (v2 << 3) + (v2 << 2) : (v2 << 4)));
@@ -412,9 +431,9 @@ __host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K,
         // the force term vanishes for directions normal to the force (uniform branch)
         if (K.kf9[k] != 0) {
             const int64_t cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];
-            X += mul_ss(K.kf9[k], cu);
+            X += SRC ? mul_ss(K.kf9[k], cu) * fo : mul_ss(K.kf9[k], cu);
         }
-        const int64_t Y = by_class(mul_su(cj, K.oma3_w2), c) + K.ka3[k];
+        const int64_t Y = by_class(mul_su(cj, K.oma3_w2), c) + (SRC ? K.ka3[k] * fo : K.ka3[k]);
         const int64_t P = F[k] + F[k + NP], M = F[k] - F[k + NP];
         const int64_t sp = mul_su(P, K.homs), sm = mul_su(M, homa);
         sink(k, F[k] - sp - sm + X + Y);

@@ -199,6 +199,14 @@ cudaError_t collide_fma(bool local, const LinksArgs& A, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+cudaError_t collide_fixed(bool local, const LinksArgs& A, cudaStream_t s) {
+    const int n = A.s.L.nf;
+    if (local) k_links_collide_fixed<true><<<grid_for(n), kBlock, 0, s>>>(A);
+    else k_links_collide_fixed<false><<<grid_for(n), kBlock, 0, s>>>(A);
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
 template <class S>
 cudaError_t mass_shift(bool local, const LinksArgs& A, cudaStream_t s) {
     if (local) k_links_mass_shift<S, true><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
@@ -240,11 +248,11 @@ cudaError_t shift(int precision, int what, bool local, const LinksArgs& A, const
     return cudaErrorInvalidValue;
 }
 
-bool parts_for(int precision, bool exact, StepParts& P) {
+bool parts_for(int precision, bool exact, bool fixed, StepParts& P) {
     switch (precision) {
         case kF64:
-            P = exact ? StepParts{launch_links_mass_exact, launch_links_label_sum_exact, launch_links_collide_exact}
-                      : StepParts{mass_fma, sum_fast, collide_fma};
+            if (exact) P = StepParts{launch_links_mass_exact, launch_links_label_sum_exact, launch_links_collide_exact};
+            else P = StepParts{mass_fma, sum_fast, fixed ? collide_fixed : collide_fma};
             return true;
         case kF32: P = StepParts{mass_shift<float>, sum_fast, collide_shift<float>}; return true;
         case kF16: P = StepParts{mass_shift<__half>, sum_fast, collide_shift<__half>}; return true;
@@ -257,9 +265,9 @@ bool parts_for(int precision, bool exact, StepParts& P) {
 
 }  // namespace
 
-cudaError_t launch_links_step(int precision, bool exact, bool local, const LinksArgs& A, cudaStream_t s) {
+cudaError_t launch_links_step(int precision, bool exact, bool fixed, bool local, const LinksArgs& A, cudaStream_t s) {
     StepParts P;
-    if (!parts_for(precision, exact, P)) return cudaErrorInvalidValue;
+    if (!parts_for(precision, exact, fixed, P)) return cudaErrorInvalidValue;
     cudaError_t e;
     if (A.nlabeled > 0) {
         if ((e = P.mass(local, A, s)) != cudaSuccess) return e;

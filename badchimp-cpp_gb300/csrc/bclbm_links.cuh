@@ -197,6 +197,50 @@ __global__ void __launch_bounds__(kBlock) k_links_collide(LinksArgs A) {
     }
 }
 
+// k_links_collide with the collision in 64-bit fixed point (bclbm_fixed.cuh,
+// collide_to with the node's force attribute and mass source) on FP64 storage:
+// the pulled values (anti-bounce-back terms formed in FP64 as load_links forms
+// them) are converted to fixed point on load and rounded back to FP64 on store.
+// The default BCLBM_F64 arithmetic of the std_one_phase step: GB300's FP64 pipe
+// caps the FP64 forms of the collision at about a tenth of the HBM bandwidth.
+template <bool LOCAL>
+__global__ void __launch_bounds__(kBlock, BCLBM_FX_MINB) k_links_collide_fixed(LinksArgs A) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.s.L.nf) return;
+    const uint32_t inf = __ldg(A.info + i);
+    double u[3], f[19];
+    links_velocity<LOCAL>(A, i, inf, u);
+    load_links<false, LOCAL>(static_cast<const double*>(A.s.src), A.s.L, i, u, A.rho_w, f);
+    unsigned emax = 0;
+    int64_t X[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) X[q] = fx::load_f64_hw(f[q], emax);
+    int64_t qm = 0;
+    if (inf & kLinkAdd) qm = fx::load_f64_hw(A.lab_q[inf & kLinkLabelMask], emax);
+    int ovf = emax >= fx::kLoadEmaxLimit ? 1 : 0;
+    const int fo = __ldg(A.force_on + i);
+    const size_t pad = static_cast<size_t>(A.s.L.nf_pad);
+    double* out = static_cast<double*>(A.s.dst) + i;
+    int64_t rho, uf[3];
+    fx::collide_to<19, false, true>(
+        X, A.s.fxk, rho, uf, ovf, [out, pad](int q, int64_t v) { out[static_cast<size_t>(q) * pad] = fx::store_f64(v); },
+        fo, qm);
+    double vel[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) vel[d] = fx::store_f64(uf[d]);
+    if (inf & kLinkPress) {
+        const int p = __ldg(A.pidx + i);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) A.ustore[static_cast<size_t>(d) * A.npress + p] = vel[d];
+    }
+    if (A.s.rho_out) {
+        A.s.rho_out[i] = fx::store_f64(rho);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) A.s.vel_out[static_cast<size_t>(d) * pad + i] = vel[d];
+    }
+    if (ovf) atomicOr(A.s.fx_flag, 1);
+}
+
 // the reference's f (after streaming and the boundaries) in AoS bulk order
 template <bool EXACT, bool LOCAL>
 __global__ void __launch_bounds__(kBlock) k_links_gather(LinksArgs A, const int32_t* __restrict__ slot_bulk,

@@ -44,7 +44,8 @@ cudaError_t launch_links_flux(const LinksArgs& A, cudaStream_t s);
 // One step: with interior domains the mass pass and the domain sums, then the collision.  (Running
 // the mass pass and the labelled nodes on a second stream beside the other nodes was measured slower:
 // 192^3 F32 135 -> 151 us per step, F16 unchanged.)
-cudaError_t launch_links_step(int precision, bool exact, bool local, const LinksArgs& A, cudaStream_t s);
+// F64 arithmetic: exact (the reference's rounding), else 64-bit fixed point (fixed) or FP64 with FMA
+cudaError_t launch_links_step(int precision, bool exact, bool fixed, bool local, const LinksArgs& A, cudaStream_t s);
 cudaError_t launch_links_gather(int precision, bool exact, bool local, const LinksArgs& A, const int32_t* slot_bulk,
                                 double* out, cudaStream_t s);
 cudaError_t launch_links_moments(int precision, bool exact, bool local, const LinksArgs& A, cudaStream_t s);

@@ -69,7 +69,7 @@ class Timing(ctypes.Structure):
 
 EXPORTS = ["bclbm_create", "bclbm_step", "bclbm_step_timed", "bclbm_download_f", "bclbm_download_macros",
            "bclbm_macros_begin", "bclbm_macros_collect", "bclbm_reduce", "bclbm_set_force", "bclbm_pressure_flux", "bclbm_node_perm",
-           "bclbm_footprint", "bclbm_sync", "bclbm_destroy", "bclbm_error", "bclbm_last_error", "bclbm_launch_count",
+           "bclbm_footprint", "bclbm_sync", "bclbm_destroy", "bclbm_trim", "bclbm_error", "bclbm_last_error", "bclbm_launch_count",
            "bclbm_moments_static", "bclbm_batch_create", "bclbm_batch_admit", "bclbm_batch_admit_steps",
            "bclbm_batch_attach", "bclbm_batch_retire", "bclbm_batch_step", "bclbm_batch_stats",
            "bclbm_batch_download_f", "bclbm_batch_info", "bclbm_batch_sync", "bclbm_batch_last_error",
@@ -122,6 +122,8 @@ def lib():
     L.bclbm_sync.restype = ctypes.c_int
     L.bclbm_destroy.argtypes = [vp]
     L.bclbm_destroy.restype = None
+    L.bclbm_trim.argtypes = []
+    L.bclbm_trim.restype = ctypes.c_int
     L.bclbm_error.argtypes = [ctypes.c_int]
     L.bclbm_error.restype = ctypes.c_char_p
     L.bclbm_last_error.argtypes = [vp]

@@ -60,9 +60,11 @@ extern "C" {
 #define BCLBM_LINKS 3 /* the std_one_phase step (src/std_one_phase/main.cpp:470-575, D3Q19):
                          BGK + Guo force times the per-node force attribute, interior-domain mass
                          sources (calcDeltaOmegaQ) and the solid-fluid, pressure (anti-bounce-back)
-                         and fluid-fluid link boundaries of the node tags.  BCLBM_F64: FP64 with FMA,
-                         or the reference's rounding with FLAG_EXACT; BCLBM_F32 / F16 / BF16: shifted
-                         storage with FP32 arithmetic on the deviations */
+                         and fluid-fluid link boundaries of the node tags.  BCLBM_F64: FP64 storage
+                         with the 64-bit fixed-point collision of the std_case step (default), FP64
+                         with FMA under BCLBM_FLAG_FP64_FMA, or the reference's rounding with
+                         FLAG_EXACT; BCLBM_F32 / F16 / BF16: shifted storage with FP32 arithmetic on
+                         the deviations */
 
 /* population storage on the device */
 #define BCLBM_F64 0  /* plain FP64 populations; arithmetic: 64-bit fixed point with 2^-60
@@ -176,7 +178,14 @@ int bclbm_node_perm(bclbm_handle* h, int32_t* out);
 /* device bytes held by a handle created from desc (admission by HBM footprint) */
 int bclbm_footprint(const bclbm_desc* desc, size_t* bytes);
 int bclbm_sync(bclbm_handle* h);
+/* Frees the handle and its device memory.  The device memory goes back to the
+ * library's own stream-ordered pool of the device, which keeps it mapped for the
+ * next bclbm_create (no new pages to map); bclbm_trim returns it to the device. */
 void bclbm_destroy(bclbm_handle* h);
+/* Returns to the devices the memory that destroyed handles left in the library's
+ * pools (synchronises each device the library has allocated on; the memory of
+ * live handles stays). */
+int bclbm_trim(void);
 const char* bclbm_error(int status);
 const char* bclbm_last_error(const bclbm_handle* h);
 /* kernel launches issued by this process since load (for launch accounting) */

@@ -30,6 +30,10 @@ def test_python_binding_lists_every_export(bclbm):
     assert sorted(bclbm.native.EXPORTS) == declared_functions()
 
 
+def test_trim_without_device_memory_is_a_no_op(native_lib):
+    assert native_lib.bclbm_trim() == 0
+
+
 def test_error_strings(native_lib):
     assert native_lib.bclbm_error(0) == b"ok"
     assert native_lib.bclbm_error(-2).startswith(b"inconsistent")

@@ -265,3 +265,27 @@ def test_device_checks_of_a_contiguous_bulk_list(bclbm, gpu):
     with L.Solver(lat, f0, tau=(0.8, 0.8)) as s:
         s.step(3)
         assert not s.reduce()["nonfinite"]
+
+
+def test_destroyed_handles_memory_is_kept_until_trim(bclbm, gpu):
+    """bclbm_destroy leaves the handle's device memory mapped in the library's
+    pool (the next create reuses it); bclbm_trim gives it back to the device."""
+    import torch
+    geo, _, _ = bclbm.geometry.sphere_pack((96,) * 3, radius=8.0, porosity=0.4, seed=3)
+    L = bclbm.lbsolver
+    lat = L.Lattice.from_geometry(geo, "D3Q19", "xyz")
+    f0 = L.initiate_single(lat, np.ones(lat.n_nodes))
+    need = bclbm.native.footprint(lat, L.BGK, L.F64)
+    assert bclbm.native.lib().bclbm_trim() == 0
+    free0 = torch.cuda.mem_get_info()[0]
+    with L.Solver(lat, f0, tau=(0.8, 0.8)) as s:
+        s.step(2)
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free0 - free1 >= need // 2  # still reserved after destroy
+    with L.Solver(lat, f0, tau=(0.8, 0.8)) as s:  # reuses it
+        s.step(2)
+        assert torch.cuda.mem_get_info()[0] >= free1 - need // 4
+    assert bclbm.native.lib().bclbm_trim() == 0
+    free2 = torch.cuda.mem_get_info()[0]
+    assert free2 - free1 >= need // 2
