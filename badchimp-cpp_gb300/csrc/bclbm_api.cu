@@ -438,33 +438,32 @@ __global__ void k_encode_fx(const double* __restrict__ f, int64_t* __restrict__ 
 
 __global__ void k_encode(const double* __restrict__ f, void* out, int nf, int nf_pad, int Q, int nfields,
                          int precision, double rho_ref, double scale) {
-    // f: FP64 [nfields][Q][nf_pad] reference populations -> storage format
+    // f: FP64 [Q][nf_pad][nfields] reference populations -> storage format (same layout)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nf) return;
-    const size_t fs = static_cast<size_t>(Q) * nf_pad;
     for (int q = 0; q < Q; ++q) {
         const double w = Q == 9 ? (q == 8 ? 16.0 / 36.0 : (q % 2 == 0 ? 4.0 / 36.0 : 1.0 / 36.0))
                                 : (q == 18 ? 12.0 / 36.0 : ((q % 9) < 3 ? 2.0 / 36.0 : 1.0 / 36.0));
-        const size_t k = static_cast<size_t>(q) * nf_pad + i;
+        const size_t k = (static_cast<size_t>(q) * nf_pad + i) * nfields;
         double v0, v1 = 0.0;
         if (nfields == 1) {
             v0 = (f[k] - w * rho_ref) / w * scale;
         } else {
-            v0 = (f[k] + f[fs + k] - w * rho_ref) / w * scale;
-            v1 = (f[k] - f[fs + k]) / w * scale;
+            v0 = (f[k] + f[k + 1] - w * rho_ref) / w * scale;
+            v1 = (f[k] - f[k + 1]) / w * scale;
         }
         switch (precision) {
             case BCLBM_F32:
                 static_cast<float*>(out)[k] = static_cast<float>(v0);
-                if (nfields == 2) static_cast<float*>(out)[fs + k] = static_cast<float>(v1);
+                if (nfields == 2) static_cast<float*>(out)[k + 1] = static_cast<float>(v1);
                 break;
             case BCLBM_F16:
                 static_cast<__half*>(out)[k] = __double2half(v0);
-                if (nfields == 2) static_cast<__half*>(out)[fs + k] = __double2half(v1);
+                if (nfields == 2) static_cast<__half*>(out)[k + 1] = __double2half(v1);
                 break;
             case BCLBM_BF16:
                 static_cast<__nv_bfloat16*>(out)[k] = __double2bfloat16(v0);
-                if (nfields == 2) static_cast<__nv_bfloat16*>(out)[fs + k] = __double2bfloat16(v1);
+                if (nfields == 2) static_cast<__nv_bfloat16*>(out)[k + 1] = __double2bfloat16(v1);
                 break;
         }
     }
@@ -602,12 +601,12 @@ __global__ void k_upload_aos(const double* __restrict__ aos, const int32_t* __re
     if (i >= nf) return;
     const size_t es = static_cast<size_t>(nfields) * Q;
     const double* row = aos + static_cast<size_t>(slot_bulk[i]) * es;
-    const size_t fs = static_cast<size_t>(Q) * nf_pad;
     unsigned emax = 0;
     for (int q = 0; q < Q; ++q) {
-        const size_t k = static_cast<size_t>(q) * nf_pad + i;
+        // storage layout [Q][nf_pad][nfields]
+        const size_t k = (static_cast<size_t>(q) * nf_pad + i) * nfields;
         if (mode == 0) {  // FP64 storage
-            for (int f = 0; f < nfields; ++f) static_cast<double*>(out)[f * fs + k] = row[f * Q + q];
+            for (int f = 0; f < nfields; ++f) static_cast<double*>(out)[k + f] = row[f * Q + q];
             continue;
         }
         if (mode == 1) {  // int64 fixed point (single field)
@@ -626,15 +625,15 @@ __global__ void k_upload_aos(const double* __restrict__ aos, const int32_t* __re
         switch (precision) {
             case BCLBM_F32:
                 static_cast<float*>(out)[k] = static_cast<float>(v0);
-                if (nfields == 2) static_cast<float*>(out)[fs + k] = static_cast<float>(v1);
+                if (nfields == 2) static_cast<float*>(out)[k + 1] = static_cast<float>(v1);
                 break;
             case BCLBM_F16:
                 static_cast<__half*>(out)[k] = __double2half(v0);
-                if (nfields == 2) static_cast<__half*>(out)[fs + k] = __double2half(v1);
+                if (nfields == 2) static_cast<__half*>(out)[k + 1] = __double2half(v1);
                 break;
             case BCLBM_BF16:
                 static_cast<__nv_bfloat16*>(out)[k] = __double2bfloat16(v0);
-                if (nfields == 2) static_cast<__nv_bfloat16*>(out)[fs + k] = __double2bfloat16(v1);
+                if (nfields == 2) static_cast<__nv_bfloat16*>(out)[k + 1] = __double2bfloat16(v1);
                 break;
         }
     }
@@ -1181,7 +1180,8 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
                 const size_t n = static_cast<size_t>(h->slot_node[s]);
                 for (int k = 0; k < h->nfields; ++k)
                     for (int q = 0; q < Q; ++q)
-                        soa[(static_cast<size_t>(k) * Q + q) * pad + s] = d->f_init[n * es + static_cast<size_t>(k) * Q + q];
+                        soa[(static_cast<size_t>(q) * pad + s) * h->nfields + k] =
+                            d->f_init[n * es + static_cast<size_t>(k) * Q + q];
             }
         });
         if (h->precision == BCLBM_F64 && !h->fx_storage) {

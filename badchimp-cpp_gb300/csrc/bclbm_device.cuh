@@ -136,6 +136,22 @@ struct LatticeView {
     int32_t ghost_src[19];
 };
 
+// Element index (row * nf_pad + slot) of the population arriving at slot i along
+// c_q from extended neighbour y, in post-collision storage.
+template <int Q>
+__device__ __forceinline__ size_t pull_elem(const LatticeView& L, int q, int y, int i) {
+    const int rq = Lat<Q>::rev(q);
+    int slot, row;
+    if (y < L.nf) {
+        slot = y;
+        row = q;
+    } else {
+        row = rq;
+        slot = (y == L.nf + L.ns) ? L.ghost_src[rq] : i;
+    }
+    return static_cast<size_t>(row) * L.nf_pad + slot;
+}
+
 // Population arriving at slot i along c_q, read from post-collision storage g
 // (one field: rows g + q*nf_pad).  Returns the raw stored value.
 template <int Q, class S>

@@ -628,15 +628,66 @@ __global__ void __launch_bounds__(kFinalThreads) k_reduce_final(const double* __
 // colour difference (f0 - f1); both weight-normalised and scaled.  f0 and f1
 // are (ft +- (f0 - f1)) / 2.  The total carries the flow with the FP16 mantissa
 // spent on the velocity signal; the colour difference is bounded by w.
+// The two fields of an element are stored side by side, [Q][nf_pad][2]: both
+// stream from the same upstream element, so a pull is one vector load of the
+// pair (4 bytes in FP16/BF16, 8 in FP32, 16 in FP64) and a store one vector
+// store, half the memory instructions of two separate fields.
 // ---------------------------------------------------------------------------
+template <class S>
+struct Pair;
+template <>
+struct Pair<double> {
+    using V = double2;
+};
+template <>
+struct Pair<float> {
+    using V = float2;
+};
+template <>
+struct Pair<__half> {
+    using V = __half2;
+};
+template <>
+struct Pair<__nv_bfloat16> {
+    using V = __nv_bfloat162;
+};
+
+template <class S>
+__device__ __forceinline__ void store_pair(S* out, size_t elem, S a, S b) {
+    typename Pair<S>::V v;
+    v.x = a;
+    v.y = b;
+    reinterpret_cast<typename Pair<S>::V*>(out)[elem] = v;
+}
+
+// both fields of the Q populations that stream into slot i (extended neighbour table)
+template <int Q, class S, bool LOCAL>
+__device__ __forceinline__ void load_field2(const S* __restrict__ g, const LatticeView& L, int i,
+                                            typename Store<S>::T* v0, typename Store<S>::T* v1) {
+    constexpr int R = Lat<Q>::REST;
+    using V = typename Pair<S>::V;
+    const V* gp = reinterpret_cast<const V*>(g);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        size_t e;
+        if (q == R || LOCAL) {
+            e = static_cast<size_t>(q) * L.nf_pad + i;
+        } else {
+            const int y = ld_table(L.nbr + static_cast<size_t>(Lat<Q>::rev(q)) * L.nf_pad + i);
+            e = pull_elem<Q>(L, q, y, i);
+        }
+        const V p = gp[e];
+        v0[q] = p.x;
+        v1[q] = p.y;
+    }
+}
+
 template <int Q, class S, bool LOCAL>
 __device__ __forceinline__ void load_rk(const S* __restrict__ g, const LatticeView& L, int i, double* f0,
                                         double* f1, double rho_ref, double inv_scale) {
     using T = typename Store<S>::T;
     T v0[Q], v1[Q];
-    const size_t fs = static_cast<size_t>(Q) * L.nf_pad;
-    load_field<Q, S, LOCAL>(g, L, i, v0);
-    load_field<Q, S, LOCAL>(g + fs, L, i, v1);
+    load_field2<Q, S, LOCAL>(g, L, i, v0, v1);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         if constexpr (Store<S>::shifted) {
@@ -676,9 +727,7 @@ __global__ void __launch_bounds__(kBlock, (Store<S>::shifted ? BCLBM_RK_DENS_MIN
         const S* g = static_cast<const S*>(a.src);
         if constexpr (!Store<S>::shifted) {
             T v0[Q], v1[Q];
-            const size_t fs = static_cast<size_t>(Q) * a.L.nf_pad;
-            load_field<Q, S, LOCAL>(g, a.L, i, v0);
-            load_field<Q, S, LOCAL>(g + fs, a.L, i, v1);
+            load_field2<Q, S, LOCAL>(g, a.L, i, v0, v1);
             double r0 = 0.0, r1 = 0.0;
 #pragma unroll
             for (int q = 0; q < Q; ++q) r0 += v0[q];
@@ -694,9 +743,7 @@ __global__ void __launch_bounds__(kBlock, (Store<S>::shifted ? BCLBM_RK_DENS_MIN
             }
         } else {
             T v0[Q], v1[Q];
-            const size_t fs = static_cast<size_t>(Q) * a.L.nf_pad;
-            load_field<Q, S, LOCAL>(g, a.L, i, v0);
-            load_field<Q, S, LOCAL>(g + fs, a.L, i, v1);
+            load_field2<Q, S, LOCAL>(g, a.L, i, v0, v1);
             float rs = 0.f, dr = 0.f, jx = 0.f;
             const float isc = a.f_inv_scale;
 #pragma unroll
@@ -800,7 +847,6 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_f64(StepArgs a) {
         for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * a.L.nf_pad + i] = vel[d];
     }
     double* out = static_cast<double*>(a.dst);
-    const size_t fs = static_cast<size_t>(Q) * a.L.nf_pad;
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const double w = Lat<Q>::w(q);
@@ -813,8 +859,8 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_f64(StepArgs a) {
         const double dRC = (q == R)  ? 0.0
                            : FMA     ? rfb * w * cn[q] * (Lat<Q>::wclass(q) == 1 ? 1.0 : 0.70710678118654752440)
                                      : rfb * w * cn[q] / cnorm_ref(Lat<Q>::wclass(q));
-        out[q * a.L.nf_pad + i] = c0 * (ft[q] + om + dF + dST) + dRC + dQ0;
-        out[fs + q * a.L.nf_pad + i] = c1 * (ft[q] + om + dF + dST) - dRC + dQ1;
+        store_pair(out, static_cast<size_t>(q) * a.L.nf_pad + i, c0 * (ft[q] + om + dF + dST) + dRC + dQ0,
+                   c1 * (ft[q] + om + dF + dST) - dRC + dQ1);
     }
 }
 
@@ -831,10 +877,8 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_collide_shift
     if (i >= a.L.nf) return;
     using T = typename Store<S>::T;
     const S* g = static_cast<const S*>(a.src);
-    const size_t fs = static_cast<size_t>(Q) * a.L.nf_pad;
     T v0[Q], v1[Q];
-    load_field<Q, S, LOCAL>(g, a.L, i, v0);
-    load_field<Q, S, LOCAL>(g + fs, a.L, i, v1);
+    load_field2<Q, S, LOCAL>(g, a.L, i, v0, v1);
     float sc[Q];
 #pragma unroll
     for (int q = 0; q < Q - 1; ++q) sc[q] = a.cgf[__ldg(a.L.nbr + static_cast<size_t>(q) * a.L.nf_pad + i)];
@@ -899,8 +943,10 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_collide_shift
         const float dRC = (q == R) ? 0.f : rfb * w * cn * (Lat<Q>::wclass(q) == 1 ? 1.f : 0.70710678118654752f);
         const float X = Xd + w * rho_ref;
         const float s = sc_out / w;
-        Store<S>::store(out + q * a.L.nf_pad + i, Xd * s + fix_t);
-        Store<S>::store(out + fs + q * a.L.nf_pad + i, (dcf * X + 2.f * dRC) * s + fix_c);
+        S st, sd;
+        Store<S>::store(&st, Xd * s + fix_t);
+        Store<S>::store(&sd, (dcf * X + 2.f * dRC) * s + fix_c);
+        store_pair(out, static_cast<size_t>(q) * a.L.nf_pad + i, st, sd);
     }
     if (MACROS) {
         a.rho_out[i] = rho0;

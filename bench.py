@@ -649,11 +649,11 @@ def run_twophase(args, world, rank):
 
 
 def links_traffic(n_fluid):
-    """DRAM bytes of one k_links_collide launch (FP64 FMA) from the committed ncu
-    capture, scaled by the fluid nodes, or None."""
+    """DRAM bytes of one k_links_collide_fixed launch (the default FP64 step) from the
+    committed ncu capture, scaled by the fluid nodes, or None."""
     f = REPO / "profiles" / "traffic.json"
     try:
-        bpn = json.loads(f.read_text())["k_links_collide_d3q19_f64_fma"]["bytes_per_node"]
+        bpn = json.loads(f.read_text())["k_links_collide_d3q19_f64_fixed"]["bytes_per_node"]
         return int(bpn * n_fluid)
     except Exception:
         return None

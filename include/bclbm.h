@@ -202,7 +202,9 @@ int64_t bclbm_launch_count(void);
  * It computes the FP64 sums that bclbm_reduce computes - per field
  * sum_q f, sum_q f c_q, and max |f| (+Inf if any value is NaN or Inf) - over a
  * population array the caller holds on the device, in the library's device
- * layout [nfields][Q][slot_stride].  precision names the values' format:
+ * layout [Q][slot_stride][nfields] (the nfields values of an element side by
+ * side; with one field, Q rows of slot_stride values).  precision names the
+ * values' format:
  * BCLBM_F64 = plain FP64 values of f (the device format of handles created
  * with BCLBM_FLAG_EXACT or BCLBM_FLAG_FP64_FMA; a default BCLBM_F64 handle keeps
  * int64 fixed point on the device, which this entry point does not read); the

@@ -47,12 +47,12 @@ def shifted_init(case, precision, seed=7):
 
 def device_soa(torch, case, rows, nfields, precision):
     """The caller's copy of the populations in the library's device layout
-    [nfields][Q][stride], on the GPU: plain FP64 values of f (F64), or the
+    [Q][stride][nfields], on the GPU: plain FP64 values of f (F64), or the
     stored values of a shifted format."""
     nb = rows.shape[0]
     stride = nb + 37  # any stride >= n_slots is allowed
-    soa = np.zeros((nfields, case.nq, stride))
-    soa[:, :, :nb] = rows.reshape(nb, nfields, case.nq).transpose(1, 2, 0)
+    soa = np.zeros((case.nq, stride, nfields))
+    soa[:, :nb, :] = rows.reshape(nb, nfields, case.nq).transpose(2, 0, 1)
     dtype = {"f64": torch.float64, "f32": torch.float32, "f16": torch.float16, "bf16": torch.bfloat16}[precision]
     dev = torch.from_numpy(soa).to(dtype).cuda()
     # the conversion to the storage type must be exact (the values were chosen so)
@@ -148,7 +148,7 @@ def test_static_moments_flag_nonfinite(bclbm, gpu):
     rows = case.bulk_rows(f0, 1)
     for bad in (np.nan, np.inf, -np.inf):
         dev, nb, stride = device_soa(torch, case, rows, 1, "f64")
-        dev[0, 5, nb // 2] = float(bad)
+        dev[5, nb // 2, 0] = float(bad)
         got = static_sums(bclbm, torch, case, dev, nb, stride, 1, "f64")
         assert got[5] == np.inf, (bad, got)
     dev, nb, stride = device_soa(torch, case, rows, 1, "f64")
