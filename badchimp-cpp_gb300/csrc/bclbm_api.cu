@@ -699,7 +699,7 @@ int run_gather(bclbm_handle* h) {
     StepArgs a = make_args(h);
     a.src = h->pops[h->cur];
     if (h->collision == BCLBM_LINKS) {
-        CUDA_TRY(h, launch_links_gather(h->precision, h->exact, !h->state_post, links_args(h, a), h->d_slot_bulk,
+        CUDA_TRY(h, launch_links_gather(h->precision, h->exact, h->fx_storage, !h->state_post, links_args(h, a), h->d_slot_bulk,
                                         h->d_gather, h->stream));
         return BCLBM_OK;
     }
@@ -813,8 +813,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
                (d->collision == BCLBM_RK && d->precision == BCLBM_F64 && !(d->flags & BCLBM_FLAG_FP64_FMA));
     h->trt = d->collision == BCLBM_TRT;
     h->fma64 = (d->flags & BCLBM_FLAG_FP64_FMA) != 0;
-    h->fx_storage = d->precision == BCLBM_F64 && d->collision != BCLBM_RK && d->collision != BCLBM_LINKS &&
-                    !h->exact && !h->fma64;
+    h->fx_storage = d->precision == BCLBM_F64 && d->collision != BCLBM_RK && !h->exact && !h->fma64;
     h->rho_w = d->rho_w != 0.0 ? d->rho_w : 1.0;
     h->flux = d->collision == BCLBM_RK && d->flux_control != 0;
     h->mass_fix = d->collision == BCLBM_RK && d->precision != BCLBM_F64 && !(d->flags & BCLBM_FLAG_NO_MASS_FIX);
@@ -1243,7 +1242,7 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
         a.vel_out = macros ? h->d_vel : nullptr;
         if (h->collision == BCLBM_LINKS) {
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
-            CUDA_TRY(h, launch_links_step(h->precision, h->exact, !h->fma64, local, links_args(h, a), h->stream));
+            CUDA_TRY(h, launch_links_step(h->precision, h->exact, h->fx_storage, local, links_args(h, a), h->stream));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
         } else if (h->collision != BCLBM_RK) {
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
@@ -1432,7 +1431,7 @@ int bclbm_reduce(bclbm_handle* h, bclbm_stats* out) {
     StepArgs a = make_args(h);
     a.src = h->pops[h->cur];
     if (h->collision == BCLBM_LINKS)
-        CUDA_TRY(h, launch_links_moments(h->precision, h->exact, !h->state_post, links_args(h, a), h->stream));
+        CUDA_TRY(h, launch_links_moments(h->precision, h->exact, h->fx_storage, !h->state_post, links_args(h, a), h->stream));
     else
         CUDA_TRY(h, launch_moments(h->q, h->fx_storage ? kFX : h->precision, h->nfields, !h->state_post, a, h->stream));
     CUDA_TRY(h, launch_reduce_final(6, h->d_partials, grid_for(h->nf), h->d_red, true, h->stream));

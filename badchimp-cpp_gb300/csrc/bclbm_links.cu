@@ -199,6 +199,13 @@ cudaError_t collide_fma(bool local, const LinksArgs& A, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+cudaError_t mass_fixed(bool local, const LinksArgs& A, cudaStream_t s) {
+    if (local) k_links_mass<false, true, int64_t><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
+    else k_links_mass<false, false, int64_t><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
 cudaError_t collide_fixed(bool local, const LinksArgs& A, cudaStream_t s) {
     const int n = A.s.L.nf;
     if (local) k_links_collide_fixed<true><<<grid_for(n), kBlock, 0, s>>>(A);
@@ -252,7 +259,8 @@ bool parts_for(int precision, bool exact, bool fixed, StepParts& P) {
     switch (precision) {
         case kF64:
             if (exact) P = StepParts{launch_links_mass_exact, launch_links_label_sum_exact, launch_links_collide_exact};
-            else P = StepParts{mass_fma, sum_fast, fixed ? collide_fixed : collide_fma};
+            else if (fixed) P = StepParts{mass_fixed, sum_fast, collide_fixed};
+            else P = StepParts{mass_fma, sum_fast, collide_fma};
             return true;
         case kF32: P = StepParts{mass_shift<float>, sum_fast, collide_shift<float>}; return true;
         case kF16: P = StepParts{mass_shift<__half>, sum_fast, collide_shift<__half>}; return true;
@@ -276,23 +284,34 @@ cudaError_t launch_links_step(int precision, bool exact, bool fixed, bool local,
     return P.collide(local, A, s);
 }
 
-cudaError_t launch_links_gather(int precision, bool exact, bool local, const LinksArgs& A, const int32_t* slot_bulk,
-                                double* out, cudaStream_t s) {
+cudaError_t launch_links_gather(int precision, bool exact, bool fixed, bool local, const LinksArgs& A,
+                                const int32_t* slot_bulk, double* out, cudaStream_t s) {
     if (precision != kF64) return shift(precision, 1, local, A, slot_bulk, out, s);
     if (exact) return launch_links_gather_exact(local, A, slot_bulk, out, s);
     const int g = grid_for(A.s.L.nf);
-    if (local) k_links_gather<false, true><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
-    else k_links_gather<false, false><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
+    if (fixed) {
+        if (local) k_links_gather<false, true, int64_t><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
+        else k_links_gather<false, false, int64_t><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
+    } else {
+        if (local) k_links_gather<false, true><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
+        else k_links_gather<false, false><<<g, kBlock, 0, s>>>(A, slot_bulk, out);
+    }
     launch_counter()++;
     return cudaGetLastError();
 }
 
-cudaError_t launch_links_moments(int precision, bool exact, bool local, const LinksArgs& A, cudaStream_t s) {
+cudaError_t launch_links_moments(int precision, bool exact, bool fixed, bool local, const LinksArgs& A,
+                                 cudaStream_t s) {
     if (precision != kF64) return shift(precision, 2, local, A, nullptr, nullptr, s);
     if (exact) return launch_links_moments_exact(local, A, s);
     const int g = grid_for(A.s.L.nf);
-    if (local) k_links_moments<false, true><<<g, kBlock, 0, s>>>(A);
-    else k_links_moments<false, false><<<g, kBlock, 0, s>>>(A);
+    if (fixed) {
+        if (local) k_links_moments<false, true, int64_t><<<g, kBlock, 0, s>>>(A);
+        else k_links_moments<false, false, int64_t><<<g, kBlock, 0, s>>>(A);
+    } else {
+        if (local) k_links_moments<false, true><<<g, kBlock, 0, s>>>(A);
+        else k_links_moments<false, false><<<g, kBlock, 0, s>>>(A);
+    }
     launch_counter()++;
     return cudaGetLastError();
 }

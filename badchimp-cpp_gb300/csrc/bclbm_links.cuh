@@ -48,16 +48,33 @@ struct LinksArgs {
     float f_dw;
 };
 
+// FP64 value of a stored population: FP64 storage holds f itself; the default
+// FP64 step (collide in fixed point) keeps its state in the collision's int64
+// format (Store<int64_t>), as the std_case step does
+__device__ __forceinline__ double as_f64(double v) { return v; }
+__device__ __forceinline__ double as_f64(int64_t v) { return fx::store_f64(v); }
+
+// applyPressureFluidBoundary (main.cpp:154-173), qUnknown = q, qKnown = rev(q):
+// the anti-bounce-back population from the known one and the node's velocity
+__device__ __forceinline__ double anti_bounce_back(int q, double fk, const double* u, double rho_w) {
+    constexpr int Q = 19;
+    const int k = Lat<Q>::rev(q);
+    const double u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];  // DXQY::dot
+    const double cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];  // cDotRef
+    const double w = Lat<Q>::w(k);
+    return -fk + 2 * w * rho_w * (1 + 0.5 * (9.0 * cu * cu - 3.0 * u2));
+}
+
 // the populations that stream into slot i: plain pulls, bounce-back, and the
 // anti-bounce-back of the pressure boundary with the node's velocity u
-template <bool EXACT, bool LOCAL>
-__device__ __forceinline__ void load_links(const double* __restrict__ g, const LatticeView& L, int i, const double* u,
+template <bool EXACT, bool LOCAL, class G = double>
+__device__ __forceinline__ void load_links(const G* __restrict__ g, const LatticeView& L, int i, const double* u,
                                            double rho_w, double* f) {
     constexpr int Q = 19, R = Lat<Q>::REST;
     const size_t pad = static_cast<size_t>(L.nf_pad);
     if constexpr (LOCAL) {
 #pragma unroll
-        for (int q = 0; q < Q; ++q) f[q] = g[static_cast<size_t>(q) * pad + i];
+        for (int q = 0; q < Q; ++q) f[q] = as_f64(g[static_cast<size_t>(q) * pad + i]);
         return;
     }
     // table entries, then the gathers (an anti-bounce-back entry ~e reads element e), then the
@@ -66,20 +83,34 @@ __device__ __forceinline__ void load_links(const double* __restrict__ g, const L
 #pragma unroll
     for (int q = 0; q < Q - 1; ++q) e[q] = __ldg(L.pull + static_cast<size_t>(q) * pad + i);
 #pragma unroll
-    for (int q = 0; q < Q - 1; ++q) f[q] = g[e[q] >= 0 ? e[q] : ~e[q]];
-    f[R] = g[static_cast<size_t>(R) * pad + i];
+    for (int q = 0; q < Q - 1; ++q) f[q] = as_f64(g[e[q] >= 0 ? e[q] : ~e[q]]);
+    f[R] = as_f64(g[static_cast<size_t>(R) * pad + i]);
 #pragma unroll
-    for (int q = 0; q < Q - 1; ++q) {
-        if (e[q] < 0) {
-            // applyPressureFluidBoundary, qUnknown = q, qKnown = rev(q)
-            const int k = Lat<Q>::rev(q);
-            const double fk = f[q];
-            const double u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];  // DXQY::dot
-            const double cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];  // cDotRef
-            const double w = Lat<Q>::w(k);
-            f[q] = -fk + 2 * w * rho_w * (1 + 0.5 * (9.0 * cu * cu - 3.0 * u2));
-        }
+    for (int q = 0; q < Q - 1; ++q)
+        if (e[q] < 0) f[q] = anti_bounce_back(q, f[q], u, rho_w);
+}
+
+// load_links of the int64 state without conversions: the anti-bounce-back
+// entries (pressure-boundary nodes only) are formed in FP64 and converted back
+template <bool LOCAL>
+__device__ __forceinline__ void load_links_fx(const int64_t* __restrict__ g, const LatticeView& L, int i,
+                                              const double* u, double rho_w, int64_t* X, unsigned& emax) {
+    constexpr int Q = 19, R = Lat<Q>::REST;
+    const size_t pad = static_cast<size_t>(L.nf_pad);
+    if constexpr (LOCAL) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) X[q] = g[static_cast<size_t>(q) * pad + i];
+        return;
     }
+    int e[Q - 1];
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) e[q] = __ldg(L.pull + static_cast<size_t>(q) * pad + i);
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) X[q] = g[e[q] >= 0 ? e[q] : ~e[q]];
+    X[R] = g[static_cast<size_t>(R) * pad + i];
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q)
+        if (e[q] < 0) X[q] = fx::load_f64_hw(anti_bounce_back(q, fx::store_f64(X[q]), u, rho_w), emax);
 }
 
 template <bool LOCAL>
@@ -132,7 +163,7 @@ __device__ __forceinline__ void collide_links(double* f, const LinksArgs& A, int
 }
 
 // mass pass (main.cpp:474-481): 1 - rho of every labelled bulk node
-template <bool EXACT, bool LOCAL>
+template <bool EXACT, bool LOCAL, class G = double>
 __global__ void __launch_bounds__(kBlock) k_links_mass(LinksArgs A) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= A.nlabeled) return;
@@ -140,7 +171,7 @@ __global__ void __launch_bounds__(kBlock) k_links_mass(LinksArgs A) {
     const uint32_t inf = __ldg(A.info + i);
     double u[3], f[19];
     links_velocity<LOCAL>(A, i, inf, u);
-    load_links<EXACT, LOCAL>(static_cast<const double*>(A.s.src), A.s.L, i, u, A.rho_w, f);
+    load_links<EXACT, LOCAL, G>(static_cast<const G*>(A.s.src), A.s.L, i, u, A.rho_w, f);
     double rho = 0.0;
 #pragma unroll
     for (int q = 0; q < 19; ++q) rho += f[q];
@@ -198,9 +229,9 @@ __global__ void __launch_bounds__(kBlock) k_links_collide(LinksArgs A) {
 }
 
 // k_links_collide with the collision in 64-bit fixed point (bclbm_fixed.cuh,
-// collide_to with the node's force attribute and mass source) on FP64 storage:
-// the pulled values (anti-bounce-back terms formed in FP64 as load_links forms
-// them) are converted to fixed point on load and rounded back to FP64 on store.
+// collide_to with the node's force attribute and mass source), the state kept
+// in the collision's int64 format between steps (no conversion per population;
+// the anti-bounce-back terms of the pressure-boundary nodes are formed in FP64).
 // The default BCLBM_F64 arithmetic of the std_one_phase step: GB300's FP64 pipe
 // caps the FP64 forms of the collision at about a tenth of the HBM bandwidth.
 template <bool LOCAL>
@@ -208,23 +239,20 @@ __global__ void __launch_bounds__(kBlock, BCLBM_FX_MINB) k_links_collide_fixed(L
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.s.L.nf) return;
     const uint32_t inf = __ldg(A.info + i);
-    double u[3], f[19];
+    double u[3];
     links_velocity<LOCAL>(A, i, inf, u);
-    load_links<false, LOCAL>(static_cast<const double*>(A.s.src), A.s.L, i, u, A.rho_w, f);
     unsigned emax = 0;
     int64_t X[19];
-#pragma unroll
-    for (int q = 0; q < 19; ++q) X[q] = fx::load_f64_hw(f[q], emax);
+    load_links_fx<LOCAL>(static_cast<const int64_t*>(A.s.src), A.s.L, i, u, A.rho_w, X, emax);
     int64_t qm = 0;
     if (inf & kLinkAdd) qm = fx::load_f64_hw(A.lab_q[inf & kLinkLabelMask], emax);
     int ovf = emax >= fx::kLoadEmaxLimit ? 1 : 0;
     const int fo = __ldg(A.force_on + i);
     const size_t pad = static_cast<size_t>(A.s.L.nf_pad);
-    double* out = static_cast<double*>(A.s.dst) + i;
+    int64_t* out = static_cast<int64_t*>(A.s.dst) + i;
     int64_t rho, uf[3];
     fx::collide_to<19, false, true>(
-        X, A.s.fxk, rho, uf, ovf, [out, pad](int q, int64_t v) { out[static_cast<size_t>(q) * pad] = fx::store_f64(v); },
-        fo, qm);
+        X, A.s.fxk, rho, uf, ovf, [out, pad](int q, int64_t v) { out[static_cast<size_t>(q) * pad] = v; }, fo, qm);
     double vel[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) vel[d] = fx::store_f64(uf[d]);
@@ -242,7 +270,7 @@ __global__ void __launch_bounds__(kBlock, BCLBM_FX_MINB) k_links_collide_fixed(L
 }
 
 // the reference's f (after streaming and the boundaries) in AoS bulk order
-template <bool EXACT, bool LOCAL>
+template <bool EXACT, bool LOCAL, class G = double>
 __global__ void __launch_bounds__(kBlock) k_links_gather(LinksArgs A, const int32_t* __restrict__ slot_bulk,
                                                          double* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -250,14 +278,14 @@ __global__ void __launch_bounds__(kBlock) k_links_gather(LinksArgs A, const int3
     const uint32_t inf = __ldg(A.info + i);
     double u[3], f[19];
     links_velocity<LOCAL>(A, i, inf, u);
-    load_links<EXACT, LOCAL>(static_cast<const double*>(A.s.src), A.s.L, i, u, A.rho_w, f);
+    load_links<EXACT, LOCAL, G>(static_cast<const G*>(A.s.src), A.s.L, i, u, A.rho_w, f);
     const size_t b = static_cast<size_t>(slot_bulk[i]);
 #pragma unroll
     for (int q = 0; q < 19; ++q) out[b * 19 + q] = f[q];
 }
 
 // per-block sums of [mass, 0, fc_x, fc_y, fc_z, max|f|] of the reference's f
-template <bool EXACT, bool LOCAL>
+template <bool EXACT, bool LOCAL, class G = double>
 __global__ void __launch_bounds__(kBlock) k_links_moments(LinksArgs A) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double vals[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
@@ -265,7 +293,7 @@ __global__ void __launch_bounds__(kBlock) k_links_moments(LinksArgs A) {
         const uint32_t inf = __ldg(A.info + i);
         double u[3], f[19];
         links_velocity<LOCAL>(A, i, inf, u);
-        load_links<EXACT, LOCAL>(static_cast<const double*>(A.s.src), A.s.L, i, u, A.rho_w, f);
+        load_links<EXACT, LOCAL, G>(static_cast<const G*>(A.s.src), A.s.L, i, u, A.rho_w, f);
         double j[3], mx = 0.0;
         qsumc_ref<19>(f, j);
 #pragma unroll

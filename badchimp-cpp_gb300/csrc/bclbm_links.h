@@ -46,8 +46,10 @@ cudaError_t launch_links_flux(const LinksArgs& A, cudaStream_t s);
 // 192^3 F32 135 -> 151 us per step, F16 unchanged.)
 // F64 arithmetic: exact (the reference's rounding), else 64-bit fixed point (fixed) or FP64 with FMA
 cudaError_t launch_links_step(int precision, bool exact, bool fixed, bool local, const LinksArgs& A, cudaStream_t s);
-cudaError_t launch_links_gather(int precision, bool exact, bool local, const LinksArgs& A, const int32_t* slot_bulk,
-                                double* out, cudaStream_t s);
-cudaError_t launch_links_moments(int precision, bool exact, bool local, const LinksArgs& A, cudaStream_t s);
+// fixed: the FP64 state is held as int64 fixed point (the default FP64 step)
+cudaError_t launch_links_gather(int precision, bool exact, bool fixed, bool local, const LinksArgs& A,
+                                const int32_t* slot_bulk, double* out, cudaStream_t s);
+cudaError_t launch_links_moments(int precision, bool exact, bool fixed, bool local, const LinksArgs& A,
+                                 cudaStream_t s);
 
 }  // namespace bclbm
