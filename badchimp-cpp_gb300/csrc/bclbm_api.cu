@@ -392,6 +392,7 @@ StepArgs bclbm::handle_args(const bclbm_handle* h) {
     a.f_beta = static_cast<float>(a.beta);
     a.fx_flag = h->d_params ? &h->d_params->fx_overflow : nullptr;
     a.fxk = fixed_consts(h);
+    a.fxr = h->q == 9 ? fx::make_rk_consts<9>() : fx::make_rk_consts<19>();
     return a;
 }
 
@@ -609,8 +610,8 @@ __global__ void k_upload_aos(const double* __restrict__ aos, const int32_t* __re
             for (int f = 0; f < nfields; ++f) static_cast<double*>(out)[k + f] = row[f * Q + q];
             continue;
         }
-        if (mode == 1) {  // int64 fixed point (single field)
-            static_cast<int64_t*>(out)[k] = fx::load_f64_hw(row[q], emax);
+        if (mode == 1) {  // int64 fixed point
+            for (int f = 0; f < nfields; ++f) static_cast<int64_t*>(out)[k + f] = fx::load_f64_hw(row[f * Q + q], emax);
             continue;
         }
         const double w = Q == 9 ? (q == 8 ? 16.0 / 36.0 : (q % 2 == 0 ? 4.0 / 36.0 : 1.0 / 36.0))
@@ -809,11 +810,10 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     h->collision = d->collision;
     h->precision = d->precision;
     h->flags = d->flags;
-    h->exact = (d->flags & BCLBM_FLAG_EXACT) != 0 ||
-               (d->collision == BCLBM_RK && d->precision == BCLBM_F64 && !(d->flags & BCLBM_FLAG_FP64_FMA));
+    h->exact = (d->flags & BCLBM_FLAG_EXACT) != 0;
     h->trt = d->collision == BCLBM_TRT;
     h->fma64 = (d->flags & BCLBM_FLAG_FP64_FMA) != 0;
-    h->fx_storage = d->precision == BCLBM_F64 && d->collision != BCLBM_RK && !h->exact && !h->fma64;
+    h->fx_storage = d->precision == BCLBM_F64 && !h->exact && !h->fma64;
     h->rho_w = d->rho_w != 0.0 ? d->rho_w : 1.0;
     h->flux = d->collision == BCLBM_RK && d->flux_control != 0;
     h->mass_fix = d->collision == BCLBM_RK && d->precision != BCLBM_F64 && !(d->flags & BCLBM_FLAG_NO_MASS_FIX);
@@ -1257,7 +1257,8 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
             ad.rho_out = nullptr;
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 0], h->stream));
             const bool sums = h->flux || h->mass_fix;
-            if (h->precision == BCLBM_F64) CUDA_TRY(h, launch_rk_f64(h->q, local, sums, ad, h->stream, true));
+            if (h->fx_storage) CUDA_TRY(h, launch_rk_fx(h->q, local, sums, ad, h->stream, true));
+            else if (h->precision == BCLBM_F64) CUDA_TRY(h, launch_rk_f64(h->q, local, sums, ad, h->stream, true));
             else CUDA_TRY(h, launch_rk_shift(h->q, h->precision, local, sums, ad, h->stream, true));
             if (sums) {
                 CUDA_TRY(h, launch_reduce_final(3, h->d_partials, grid_for(h->nf), h->d_red, false, h->stream));
@@ -1266,7 +1267,8 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
             }
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 1], h->stream));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
-            if (h->precision == BCLBM_F64 && !h->exact) CUDA_TRY(h, launch_rk_collide_f64_fma(h->q, local, a, h->stream));
+            if (h->fx_storage) CUDA_TRY(h, launch_rk_fx(h->q, local, false, a, h->stream, false));
+            else if (h->precision == BCLBM_F64 && !h->exact) CUDA_TRY(h, launch_rk_collide_f64_fma(h->q, local, a, h->stream));
             else if (h->precision == BCLBM_F64) CUDA_TRY(h, launch_rk_f64(h->q, local, false, a, h->stream, false));
             else CUDA_TRY(h, launch_rk_shift(h->q, h->precision, local, false, a, h->stream, false));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));

@@ -322,6 +322,31 @@ inline Consts make_consts(bool trt, double tau, double tau_anti, const double* F
     return K;
 }
 
+// Constants of the two-phase (Rothman-Keller) collision in fixed point: the
+// lattice weights and B coefficients by weight class (0 rest, 1 axis, 2 diagonal).
+struct RkConsts {
+    int64_t w1, w2;      // w_axis, w_diag
+    int64_t w2_3, w2_45; // 3 w_diag, 4.5 w_diag
+    int64_t w2s;         // w_diag / sqrt(2) (recolouring of the diagonal links, |c| = sqrt 2)
+    int64_t B[3];        // calcDeltaOmegaST's B_q by class
+};
+
+template <int Q>
+inline RkConsts make_rk_consts() {
+    using L = Lat<Q>;
+    RkConsts K;
+    const double w1 = L::w(0), w2 = L::w(L::NP - 1);
+    K.w1 = param(w1);
+    K.w2 = param(w2);
+    K.w2_3 = param(3.0 * w2);
+    K.w2_45 = param(4.5 * w2);
+    K.w2s = param(w2 * 0.70710678118654752440);
+    K.B[0] = param(L::B(L::REST));
+    K.B[1] = param(L::B(0));
+    K.B[2] = param(L::B(L::NP - 1));
+    return K;
+}
+
 // One BGK (TRT = false) or TRT collision in fixed point: the regrouping by
 // direction pairs of calcOmegaBGK(TRT) + calcDeltaOmegaF(TRT)
 // (src/lbsolver/LBcollision.h:27-75, 194-236).  With P = f_q + f_rq,

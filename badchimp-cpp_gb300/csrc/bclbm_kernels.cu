@@ -155,6 +155,25 @@ cudaError_t rk_shift_qs(bool local, bool flux, const StepArgs& a, cudaStream_t s
 }
 
 template <int Q>
+cudaError_t rk_fx_q(bool local, bool flux, const StepArgs& a, cudaStream_t s, bool density) {
+    const int g = grid_for(a.L.nf);
+    if (density) {
+        if (local) {
+            if (flux) k_rk_density<Q, int64_t, true, true><<<g, kBlock, 0, s>>>(a);
+            else k_rk_density<Q, int64_t, true, false><<<g, kBlock, 0, s>>>(a);
+        } else {
+            if (flux) k_rk_density<Q, int64_t, false, true><<<g, kBlock, 0, s>>>(a);
+            else k_rk_density<Q, int64_t, false, false><<<g, kBlock, 0, s>>>(a);
+        }
+    } else {
+        if (local) k_rk_collide_fx<Q, true><<<g, kBlock, 0, s>>>(a);
+        else k_rk_collide_fx<Q, false><<<g, kBlock, 0, s>>>(a);
+    }
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+template <int Q>
 cudaError_t rk_shift_q(int precision, bool local, bool flux, const StepArgs& a, cudaStream_t s, bool density) {
     switch (precision) {
         case kF32: return rk_shift_qs<Q, float>(local, flux, a, s, density);
@@ -167,11 +186,7 @@ cudaError_t rk_shift_q(int precision, bool local, bool flux, const StepArgs& a, 
 template <int Q, class S>
 cudaError_t gather_qs(int nfields, bool local, const StepArgs& a, const int32_t* sb, double* out, cudaStream_t s) {
     const int g = grid_for(a.L.nf);
-    if constexpr (std::is_same<S, int64_t>::value) {  // fixed-point storage is single-phase only
-        if (nfields != 1) return cudaErrorInvalidValue;
-        if (local) k_gather<Q, S, 1, true><<<g, kBlock, 0, s>>>(a, sb, out);
-        else k_gather<Q, S, 1, false><<<g, kBlock, 0, s>>>(a, sb, out);
-    } else if (nfields == 1) {
+    if (nfields == 1) {
         if (local) k_gather<Q, S, 1, true><<<g, kBlock, 0, s>>>(a, sb, out);
         else k_gather<Q, S, 1, false><<<g, kBlock, 0, s>>>(a, sb, out);
     } else {
@@ -185,11 +200,7 @@ cudaError_t gather_qs(int nfields, bool local, const StepArgs& a, const int32_t*
 template <int Q, class S>
 cudaError_t moments_qs(int nfields, bool local, const StepArgs& a, cudaStream_t s) {
     const int g = grid_for(a.L.nf);
-    if constexpr (std::is_same<S, int64_t>::value) {
-        if (nfields != 1) return cudaErrorInvalidValue;
-        if (local) k_moments<Q, S, 1, true><<<g, kBlock, 0, s>>>(a);
-        else k_moments<Q, S, 1, false><<<g, kBlock, 0, s>>>(a);
-    } else if (nfields == 1) {
+    if (nfields == 1) {
         if (local) k_moments<Q, S, 1, true><<<g, kBlock, 0, s>>>(a);
         else k_moments<Q, S, 1, false><<<g, kBlock, 0, s>>>(a);
     } else {
@@ -227,6 +238,10 @@ cudaError_t launch_single_fast(int Q, int precision, bool trt, bool local, const
                                const CUtensorMap* pull_map, cudaStream_t s) {
     return Q == 9 ? single_fast_q<9>(precision, trt, local, a, pull_map, s)
                   : single_fast_q<19>(precision, trt, local, a, pull_map, s);
+}
+
+cudaError_t launch_rk_fx(int Q, bool local, bool sums, const StepArgs& a, cudaStream_t s, bool density) {
+    return Q == 9 ? rk_fx_q<9>(local, sums, a, s, density) : rk_fx_q<19>(local, sums, a, s, density);
 }
 
 cudaError_t launch_single_fixed(int Q, bool trt, bool local, const StepArgs& a, cudaStream_t s) {

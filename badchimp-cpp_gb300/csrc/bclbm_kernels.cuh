@@ -60,6 +60,7 @@ struct StepArgs {
     float f_tau_inv, f_tauA_inv, f_tf, f_taf, f_rho_ref, f_scale, f_inv_scale, f_nu0inv, f_nu1inv, f_sigma, f_beta;
     int* fx_flag;           // &params->fx_overflow
     fx::Consts fxk;         // constants of the fixed-point collision
+    fx::RkConsts fxr;       // constants of the fixed-point two-phase collision
 };
 
 // ---------------------------------------------------------------------------
@@ -651,6 +652,10 @@ template <>
 struct Pair<__nv_bfloat16> {
     using V = __nv_bfloat162;
 };
+template <>
+struct Pair<int64_t> {
+    using V = longlong2;
+};
 
 template <class S>
 __device__ __forceinline__ void store_pair(S* out, size_t elem, S a, S b) {
@@ -677,8 +682,8 @@ __device__ __forceinline__ void load_field2(const S* __restrict__ g, const Latti
             e = pull_elem<Q>(L, q, y, i);
         }
         const V p = gp[e];
-        v0[q] = p.x;
-        v1[q] = p.y;
+        v0[q] = static_cast<typename Store<S>::T>(p.x);
+        v1[q] = static_cast<typename Store<S>::T>(p.y);
     }
 }
 
@@ -696,6 +701,9 @@ __device__ __forceinline__ void load_rk(const S* __restrict__ g, const LatticeVi
             const double dc = w * (static_cast<double>(Store<S>::val(v1[q])) * inv_scale);
             f0[q] = 0.5 * (ft + dc);
             f1[q] = 0.5 * (ft - dc);
+        } else if constexpr (std::is_same<S, int64_t>::value) {  // int64 fixed-point state
+            f0[q] = fx::store_f64(v0[q]);
+            f1[q] = fx::store_f64(v1[q]);
         } else {
             f0[q] = v0[q];
             f1[q] = v1[q];
@@ -725,7 +733,20 @@ __global__ void __launch_bounds__(kBlock, (Store<S>::shifted ? BCLBM_RK_DENS_MIN
     if (i < a.L.nf) {
         using T = typename Store<S>::T;
         const S* g = static_cast<const S*>(a.src);
-        if constexpr (!Store<S>::shifted) {
+        if constexpr (std::is_same<S, int64_t>::value) {
+            // int64 fixed-point state: exact sums, the colour in FP64 as the reference forms it
+            T v0[Q], v1[Q];
+            load_field2<Q, S, LOCAL>(g, a.L, i, v0, v1);
+            int64_t r0 = 0, r1 = 0, jx = 0;
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                r0 += v0[q];
+                r1 += v1[q];
+                if (SUMS) jx += Lat<Q>::cx(q) * (v0[q] + v1[q]);
+            }
+            a.cg[i] = fx::store_f64(r0 - r1) / fx::store_f64(r0 + r1);
+            if (SUMS) fx = fx::store_f64(jx);
+        } else if constexpr (!Store<S>::shifted) {
             T v0[Q], v1[Q];
             load_field2<Q, S, LOCAL>(g, a.L, i, v0, v1);
             double r0 = 0.0, r1 = 0.0;
@@ -954,6 +975,162 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_collide_shift
 #pragma unroll
         for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * a.L.nf_pad + i] = u[d];
     }
+}
+
+// PASS 2 of the default FP64 two-phase step, on the int64 fixed-point state
+// (main_TWOPHASE.cpp:312-376, the expressions of k_rk_collide_f64 regrouped by
+// direction pairs).  The per-node scalars - the relaxation rate of the phase
+// mix, the colour gradient, its norm and direction, the surface-tension and
+// recolouring amplitudes, the colour fraction - are formed in FP64 (about a
+// hundred FP64 operations per node) and converted; every per-direction term is
+// a 64-bit fixed-point product.  With ft = f0 + f1, P / M the pair sums and
+// j = sum ft c + F/2 (exact):
+//   X_q = (1 - oms) ft_q + oms feq_q + dF_q + dST_q,
+//   out0 = c0 X_q + dRC_q,  out1 = X_q - out0   (c1 = 1 - c0),
+// where oms feq_q = oms w (rho - 1.5 j.u) + 4.5 oms w (c.j)(c.u) +- 3 oms w (c.j).
+#ifndef BCLBM_RK_FX_MINB
+#define BCLBM_RK_FX_MINB 2
+#endif
+template <int Q, bool LOCAL>
+__global__ void __launch_bounds__(kBlock, BCLBM_RK_FX_MINB) k_rk_collide_fx(StepArgs a) {
+    const bool MACROS = a.rho_out != nullptr;
+    constexpr int D = Lat<Q>::D, R = Lat<Q>::REST, NP = Lat<Q>::NP;
+    constexpr int SH1 = Q == 19 ? 1 : 2;  // w_axis / w_diag
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.L.nf) return;
+    const size_t pad = static_cast<size_t>(a.L.nf_pad);
+    int64_t X0[Q], X1[Q];
+    load_field2<Q, int64_t, LOCAL>(static_cast<const int64_t*>(a.src), a.L, i, X0, X1);
+    // colour at the downstream neighbours (grad, LButilities.h:12-22)
+    double sc[Q];
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) sc[q] = a.cg[ld_table(a.L.nbr + static_cast<size_t>(q) * pad + i)];
+    sc[R] = a.cg[i];
+    int ovf = 0;
+    int64_t rho0 = 0, rho1 = 0, ft[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        rho0 += X0[q];
+        rho1 += X1[q];
+        ft[q] = X0[q] + X1[q];
+    }
+    const int64_t rho = rho0 + rho1;
+    {
+        int t = 0;  // sum_q |ft_q| below 8 (see fx::collide_to)
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int h = static_cast<int>(ft[q] >> 56);
+            t += h < 0 ? -h : h;
+        }
+        if (t > 108) ovf = 1;
+    }
+    // the body force (the flux controller may change it every step)
+    unsigned emax = 0;
+    int64_t Ff[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) Ff[d] = fx::load_f64_hw(a.params->force[d], emax);
+    int64_t j[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const int64_t Mk = ft[k] - ft[k + NP];
+        if (Lat<Q>::cx(k) > 0) j[0] += Mk;
+        if (Lat<Q>::cx(k) < 0) j[0] -= Mk;
+        if (Lat<Q>::cy(k) > 0) j[1] += Mk;
+        if (Lat<Q>::cy(k) < 0) j[1] -= Mk;
+        if (D == 3 && Lat<Q>::cz(k) > 0) j[2] += Mk;
+        if (D == 3 && Lat<Q>::cz(k) < 0) j[2] -= Mk;
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) j[d] += Ff[d] >> 1;
+    // 1 / rho: FP32 estimate, one Newton step in fixed point
+    const float rf = static_cast<float>(rho) * 8.67361737988403547e-19f;  // 2^-60
+    if (!(rf > 0.15f)) ovf = 1;
+    int64_t inv = static_cast<int64_t>(__frcp_rn(rf) * 1.152921504606846976e18f);
+    inv = fx::mul_uu(inv, 2 * fx::ONE - fx::mul_uu(rho, inv));
+    int64_t u[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d) u[d] = fx::mul_su(j[d], inv);
+    // per-node scalars in FP64, as the reference forms them
+    const double r0 = fx::store_f64(rho0), r1 = fx::store_f64(rho1), r = fx::store_f64(rho);
+    const double Dn = r0 * a.nu0inv + r1 * a.nu1inv;
+    const double oms_d = Dn / (3.0 * r + 0.5 * Dn);  // 1 / tau, tau = 3 rho / Dn + 0.5
+    double G[3] = {0.0, 0.0, 0.0};
+    grad_ref<Q>(sc, G);
+    const double cgn = sqrt(dot_ref<Q>(G, G));
+    const double gs = 1.0 / (cgn + static_cast<double>(cgn < 2.220446049250313080847e-16));
+    const double inv_r = 1.0 / r;
+    const int64_t oms = fx::load_f64_hw(oms_d, emax);
+    const int64_t tf = fx::load_f64_hw(1.0 - 0.5 * oms_d, emax);
+    const int64_t af = fx::load_f64_hw(1.125 * cgn * a.sigma * oms_d, emax);
+    const int64_t rfb = fx::load_f64_hw(a.beta * r0 * r1 * inv_r, emax);
+    const int64_t c0 = fx::load_f64_hw(r0 * inv_r, emax);
+    int64_t n[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d) n[d] = fx::load_f64_hw(G[d] * gs, emax);
+    if (emax >= fx::kLoadEmaxLimit) ovf = 1;
+    const fx::RkConsts& K = a.fxr;
+    const int64_t hom = (fx::ONE - oms) >> 1;  // (1 - oms) / 2
+    int64_t ju = fx::mul_ss(j[0], u[0]) + fx::mul_ss(j[1], u[1]);
+    if (D == 3) ju += fx::mul_ss(j[2], u[2]);
+    const int64_t AB2 = fx::mul_ss(rho - (ju + (ju >> 1)), fx::mul_su(oms, K.w2));  // oms w2 (rho - 1.5 j.u)
+    const int64_t k45 = fx::mul_su(oms, K.w2_45);
+    const int64_t K3 = fx::mul_su(oms, K.w2_3);
+    int64_t u45[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d) u45[d] = fx::mul_su(u[d], k45);
+    // force terms: -3 w2 tf u.F, and 3 w2 tf F_d (ka3 of a direction = c . g3, kf9 = 3 c . g3)
+    const int64_t tf3w2 = fx::mul_ss(tf, K.w2_3);
+    int64_t uF = 0, g3[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        if (Ff[d] != 0) {
+            uF += fx::mul_ss(u[d], Ff[d]);
+            g3[d] = fx::mul_ss(Ff[d], tf3w2);
+        }
+    const int64_t K2 = -fx::mul_ss(uF, tf3w2);
+    // surface tension af (w cn^2 - B) and recolouring rfb w cn / |c|
+    const int64_t afw2 = fx::mul_ss(af, K.w2);
+    const int64_t afB1 = fx::mul_ss(af, K.B[1]), afB2 = fx::mul_ss(af, K.B[2]), afB0 = fx::mul_ss(af, K.B[0]);
+    const int64_t rfb1 = fx::mul_ss(rfb, K.w1), rfb2 = fx::mul_ss(rfb, K.w2s);
+    auto by_class = [](int64_t v2, int c) -> int64_t {
+        return c == 2 ? v2 : (c == 1 ? (v2 << SH1) : (Q == 19 ? (v2 << 3) + (v2 << 2) : (v2 << 4)));
+    };
+    int64_t* out = static_cast<int64_t*>(a.dst);
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const int c = Lat<Q>::wclass(k);
+        const int cx = Lat<Q>::cx(k), cy = Lat<Q>::cy(k), cz = Lat<Q>::cz(k);
+        const int64_t cj = cx * j[0] + cy * j[1] + cz * j[2];
+        const int64_t cu45 = cx * u45[0] + cy * u45[1] + cz * u45[2];
+        const int64_t cn = cx * n[0] + cy * n[1] + cz * n[2];
+        const int64_t P = ft[k] + ft[k + NP], M = ft[k] - ft[k + NP];
+        const int64_t cn2 = fx::mul_ss(cn, cn);
+        int64_t Sv = fx::mul_ss(P, hom) + by_class(AB2 + fx::mul_ss(cj, cu45) + K2 + fx::mul_ss(cn2, afw2), c) -
+                     (c == 1 ? afB1 : afB2);
+        const int64_t ka3 = by_class(cx * g3[0] + cy * g3[1] + cz * g3[2], c);
+        if (ka3 != 0) {  // 9 w tf (c.F)(c.u) for the directions with c.F != 0 (uniform over the grid)
+            const int64_t cu = cx * u[0] + cy * u[1] + cz * u[2];
+            Sv += fx::mul_ss(3 * ka3, cu);
+        }
+        const int64_t Av = fx::mul_ss(M, hom) + by_class(fx::mul_ss(cj, K3), c) + ka3;
+        const int64_t Xk = Sv + Av, Xr = Sv - Av;
+        const int64_t dRC = fx::mul_ss(cn, c == 1 ? rfb1 : rfb2);
+        const int64_t o0k = fx::mul_ss(c0, Xk) + dRC, o0r = fx::mul_ss(c0, Xr) - dRC;
+        store_pair(out, static_cast<size_t>(k) * pad + i, o0k, Xk - o0k);
+        store_pair(out, static_cast<size_t>(k + NP) * pad + i, o0r, Xr - o0r);
+    }
+    {
+        const int64_t XR = ft[R] - fx::mul_ss(ft[R], oms) + by_class(AB2 + K2, 0) - afB0;
+        const int64_t o0 = fx::mul_ss(c0, XR);
+        store_pair(out, static_cast<size_t>(R) * pad + i, o0, XR - o0);
+    }
+    if (MACROS) {
+        a.rho_out[i] = r0;
+        a.rho_out[pad + i] = r1;
+#pragma unroll
+        for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * pad + i] = fx::store_f64(u[d]);
+    }
+    if (ovf) atomicOr(a.fx_flag, 1);
 }
 
 // ---------------------------------------------------------------------------

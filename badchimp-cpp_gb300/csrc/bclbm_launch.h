@@ -41,6 +41,8 @@ cudaError_t launch_rk_shift(int Q, int precision, bool local, bool sums, const S
 cudaError_t launch_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params, cudaStream_t s);
 // PASS 2 of the FP64 two-phase step with FMA contraction (BCLBM_FLAG_FP64_FMA)
 cudaError_t launch_rk_collide_f64_fma(int Q, bool local, const StepArgs& a, cudaStream_t s);
+// the default FP64 two-phase step on the int64 fixed-point state: PASS 1 (density) or PASS 2
+cudaError_t launch_rk_fx(int Q, bool local, bool sums, const StepArgs& a, cudaStream_t s, bool density);
 cudaError_t launch_rk_fix(const double* sum, double n, double rho_ref, double mom_x, bool flux, bool fix,
                           DevParams* params, cudaStream_t s);
 cudaError_t launch_gather(int Q, int precision, int nfields, bool local, const StepArgs& a, const int32_t* slot_bulk,

@@ -591,9 +591,10 @@ def run_twophase(args, world, rank):
     l0 = bclbm.native.launch_count()
     with ClockSampler(0) as clk:
         for prec in args.tp_precisions.split(","):
-            base = prec.split("-")[0]  # "f64-fma": FP64 with FMA contraction
+            base = prec.split("-")[0]  # "f64": fixed point; "f64-fma": FMA contraction; "f64-exact": reference order
             with L.Solver(lat, f0, collision=L.RK, precision=base, tau=(1.0, 1.0), force=(args.gx, 0.0, 0.0),
-                          sigma=args.sigma, beta=args.beta, rho_init=rho, fma64=prec.endswith("-fma")) as s:
+                          sigma=args.sigma, beta=args.beta, rho_init=rho, fma64=prec.endswith("-fma"),
+                          exact=prec.endswith("-exact")) as s:
                 s.step(args.warmup)
                 s.sync()
                 tm = s.step_timed(args.steps)
@@ -618,11 +619,12 @@ def run_twophase(args, world, rank):
                          "steps_total": max(done, args.tp_steps), "seconds_after_timing": t_acc}
             log(f"{prec}: {mlups:.0f} MLUPS, S = {st['saturation']:.9f}, flux {flux}")
     launches = bclbm.native.launch_count() - l0
-    ref = res.get("f64")
+    ref_key = next((k for k in ("f64-exact", "f64", "f64-fma") if k in res), None)
+    ref = res.get(ref_key) if ref_key else None
     errs = {}
     if ref:
         for prec, r in res.items():
-            if prec == "f64":
+            if prec == ref_key:
                 continue
             errs[prec] = {"saturation_abs": abs(r["saturation"] - ref["saturation"]),
                           "phase_flux_rel": [abs(a - b) / abs(b) if b else None for a, b in
@@ -860,7 +862,7 @@ def main():
     ap.add_argument("--tp-steps", type=int, default=20000, help="twophase: total steps of the accuracy run")
     ap.add_argument("--write-every", type=int, default=1000, help="output: steps between output steps")
     ap.add_argument("--writes", type=int, default=4, help="output: output steps")
-    ap.add_argument("--tp-precisions", default="f64,f16")
+    ap.add_argument("--tp-precisions", default="f64-exact,f16")
     ap.add_argument("--saturation", type=float, default=0.5)
     ap.add_argument("--sigma", type=float, default=0.01)
     ap.add_argument("--beta", type=float, default=0.99)

@@ -9,8 +9,9 @@
 * D3Q19 Rothman-Keller two-phase on a periodic 96^3 pack (radius 8, porosity
   0.40, red/blue i.i.d. p = 0.5, tau 1/1, A = 0.01, beta = 0.99, neutral
   wetting, constant gx 1e-5), 100 steps of src/twophase/main_TWOPHASE.cpp:236-392:
-  exact FP64 bit-identical in f, rho, u and the colour field, FP64 with FMA
-  within 1e-12, FP16 shifted storage within its stated bounds.
+  exact FP64 bit-identical in f, rho, u and the colour field, the default
+  fixed-point FP64 and FP64 with FMA within 1e-12, FP16 shifted storage within
+  its stated bounds.
 * The two-phase mass-drift correction: FP16 storage over 2,000 steps with the
   correction keeps the saturation within 1e-7 of its start and much closer
   than without it (BCLBM_FLAG_NO_MASS_FIX).
@@ -136,10 +137,10 @@ def tp_outputs(lat, s):
     return f.reshape(-1, 2, 19)[b], r.reshape(-1, 2)[b], vel.reshape(-1, 3)[b], cg[b]
 
 
-@pytest.mark.parametrize("mode", ["exact", "fma"])
+@pytest.mark.parametrize("mode", ["exact", "fixed", "fma"])
 def test_two_phase_96_against_oracle(bclbm, tp_pack, tp_oracle, mode):
     lat, f0, rho = tp_pack
-    kw = dict(exact=True) if mode == "exact" else dict(fma64=True)
+    kw = {"exact": dict(exact=True), "fixed": {}, "fma": dict(fma64=True)}[mode]
     with tp_solver(bclbm, lat, f0, rho, **kw) as s:
         s.step(TP_STEPS)
         f, r, vel, cg = tp_outputs(lat, s)

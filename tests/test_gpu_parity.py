@@ -83,14 +83,17 @@ SINGLE = [(n, t) for n, t in RUNS if not t.startswith("rk")]
 TWOPHASE = [(n, t) for n, t in RUNS if t.startswith("rk")]
 
 
+@pytest.mark.parametrize("arith", ["fixed", "fma"])
 @pytest.mark.parametrize("name,tag", TWOPHASE, ids=[f"{n}-{t}" for n, t in TWOPHASE])
-def test_fma_f64_two_phase_within_1e12(bclbm, gpu, name, tag):
-    """BCLBM_F64 two-phase with BCLBM_FLAG_FP64_FMA: the reference's expressions with
-    FMA contraction; f, rho and the colour field within 1e-12 of the reference."""
+def test_fast_f64_two_phase_within_1e12(bclbm, gpu, name, tag, arith):
+    """BCLBM_F64 two-phase without BCLBM_FLAG_EXACT: the int64 fixed-point state with
+    the per-node scalars in FP64 (default), or the reference's expressions with FMA
+    contraction (BCLBM_FLAG_FP64_FMA); f, rho and the colour field within 1e-12 of
+    the reference."""
     case = lbcases.Case(name, bclbm)
     run = case.runs[tag]
     exp = case.expected(tag)
-    with make_solver(case, run, fma64=True) as s:
+    with make_solver(case, run, fma64=(arith == "fma")) as s:
         s.step(run["steps"])
         got = outputs(case, run, s)
     assert relerr(got["f"], exp["f"]) <= 1e-12
