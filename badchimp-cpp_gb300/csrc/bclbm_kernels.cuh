@@ -725,8 +725,20 @@ __device__ __forceinline__ void load_rk(const S* __restrict__ g, const LatticeVi
 #define BCLBM_RK_COLL_MINB 4
 #endif
 
+// the int64 fixed-point state's density pass (exact integer sums, one FP64 division):
+// unbounded registers measured best (192^3, ms per pass: 0.173 against 0.191 at 4 and
+// 0.267 at 5 resident blocks); its collide pass at 2 blocks (0.773 ms against 0.835 at 3
+// and 1.065 at 1)
+#ifndef BCLBM_RK_FX_DENS_MINB
+#define BCLBM_RK_FX_DENS_MINB 1
+#endif
+template <class S>
+constexpr int rk_density_min_blocks() {
+    return Store<S>::shifted ? BCLBM_RK_DENS_MINB : (std::is_same<S, int64_t>::value ? BCLBM_RK_FX_DENS_MINB : 1);
+}
+
 template <int Q, class S, bool LOCAL, bool SUMS>
-__global__ void __launch_bounds__(kBlock, (Store<S>::shifted ? BCLBM_RK_DENS_MINB : 1)) k_rk_density(StepArgs a) {
+__global__ void __launch_bounds__(kBlock, rk_density_min_blocks<S>()) k_rk_density(StepArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double fx = 0.0;
     float fxf = 0.f, mt = 0.f, mc = 0.f;

@@ -56,7 +56,11 @@ extern "C" {
 /* collision models */
 #define BCLBM_BGK 0 /* calcOmegaBGK + calcDeltaOmegaF          (src/lbsolver/LBcollision.h:27-46, 194-213) */
 #define BCLBM_TRT 1 /* calcOmegaBGKTRT + calcDeltaOmegaFTRT(phi=1) (LBcollision.h:50-75, 215-236) */
-#define BCLBM_RK 2  /* Rothman-Keller two-phase step of src/twophase/main_TWOPHASE.cpp:238-392 */
+#define BCLBM_RK 2  /* Rothman-Keller two-phase step of src/twophase/main_TWOPHASE.cpp:238-392;
+                       BCLBM_F64: both colour sets in 64-bit fixed point with the per-node scalars
+                       (relaxation rate of the phase mix, colour gradient, amplitudes) in FP64
+                       (default), the reference's rounding with BCLBM_FLAG_EXACT, FP64 with FMA
+                       under BCLBM_FLAG_FP64_FMA */
 #define BCLBM_LINKS 3 /* the std_one_phase step (src/std_one_phase/main.cpp:470-575, D3Q19):
                          BGK + Guo force times the per-node force attribute, interior-domain mass
                          sources (calcDeltaOmegaQ) and the solid-fluid, pressure (anti-bounce-back)
