@@ -86,8 +86,18 @@ int staged_grid(const void* kernel, int nf) {
 template <int Q, class S>
 cudaError_t single_fast_qs(bool trt, bool local, const StepArgs& a, const CUtensorMap* pull_map, cudaStream_t s) {
     const int g = grid_for(a.L.nf);
-    // the staged kernel serves the native-FP64 step only (see k_single_staged)
+    // the staged kernel serves the native-FP64 step only (see k_single_staged); the
+    // shifted formats take two slots per thread after the first step (k_single_pair)
     constexpr bool kStaged = std::is_same<S, double>::value;
+    if constexpr (!kStaged) {
+        if (!local) {
+            const int gp = grid_for((a.L.nf + 1) / 2);
+            if (trt) k_single_pair<Q, S, true><<<gp, kBlock, 0, s>>>(a);
+            else k_single_pair<Q, S, false><<<gp, kBlock, 0, s>>>(a);
+            launch_counter()++;
+            return cudaGetLastError();
+        }
+    }
     if (local || !pull_map || !kStaged) {
         if (trt) {
             if (local) k_single<Q, S, 1, true, true><<<g, kBlock, 0, s>>>(a);
