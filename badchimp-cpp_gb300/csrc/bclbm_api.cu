@@ -144,6 +144,13 @@ int validate_descriptor(const bclbm_desc* d, std::string& err) {
     }
     if ((d->flags & BCLBM_FLAG_SFC_ORDER) && !d->pos) { err = "BCLBM_FLAG_SFC_ORDER needs pos"; return BCLBM_ERR_INVALID; }
     if (d->n_bulk >= d->n_nodes) { err = "n_bulk must be smaller than n_nodes"; return BCLBM_ERR_INVALID; }
+    const bool fixed = d->precision == BCLBM_F64 && !(d->flags & (BCLBM_FLAG_EXACT | BCLBM_FLAG_FP64_FMA));
+    if (fixed && d->collision == BCLBM_RK && !(std::fabs(d->sigma) < 3.5 && std::fabs(d->beta) < 4.0)) {
+        // 9/8 sigma and beta are fixed-point constants of the default FP64 two-phase step
+        err = "the fixed-point FP64 two-phase step needs |sigma| < 3.5 and |beta| < 4 "
+              "(BCLBM_FLAG_FP64_FMA or BCLBM_FLAG_EXACT take any value)";
+        return BCLBM_ERR_INVALID;
+    }
     return BCLBM_OK;
 }
 
@@ -361,6 +368,7 @@ StepArgs bclbm::handle_args(const bclbm_handle* h) {
     for (int q = 0; q < 19; ++q) a.L.ghost_src[q] = h->ghost_src[q];
     a.cg = h->d_cg;
     a.cgf = h->d_cgf;
+    a.cgx = h->fx_storage ? reinterpret_cast<int64_t*>(h->d_cg) : nullptr;
     a.params = h->d_params;
     a.tau = h->tau[0];
     a.tau_anti = h->tau[1];
@@ -392,7 +400,8 @@ StepArgs bclbm::handle_args(const bclbm_handle* h) {
     a.f_beta = static_cast<float>(a.beta);
     a.fx_flag = h->d_params ? &h->d_params->fx_overflow : nullptr;
     a.fxk = fixed_consts(h);
-    a.fxr = h->q == 9 ? fx::make_rk_consts<9>() : fx::make_rk_consts<19>();
+    a.fxr = h->q == 9 ? fx::make_rk_consts<9>(a.nu0inv, a.nu1inv, a.sigma, a.beta)
+                      : fx::make_rk_consts<19>(a.nu0inv, a.nu1inv, a.sigma, a.beta);
     return a;
 }
 
@@ -1076,6 +1085,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     for (int k = 0; k < 3; ++k) {
         prm.force[k] = h->force[k];
         prm.forcef[k] = static_cast<float>(h->force[k]);
+        prm.forcex[k] = fx::param(h->force[k]);
     }
     if (h->mass_fix) {
         // the conserved totals of the uploaded state, sum over bulk nodes of
@@ -1136,6 +1146,17 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
                 h->solid_cg[k] = (r0 - r1) / (r0 + r1);
             }
             cg[static_cast<size_t>(h->nf) + k] = h->solid_cg[k];
+        }
+        if (h->fx_storage) {
+            // the fixed-point step keeps the colour field in fixed point (|colour| < 2)
+            for (size_t k = h->nf; k < ncg; ++k) {
+                if (!(std::fabs(cg[k]) < 2.0)) {
+                    std::fprintf(stderr, "bclbm_create: a boundary solid's colour %g is outside (-2, 2)\n", cg[k]);
+                    return cleanup(BCLBM_ERR_INVALID);
+                }
+                const int64_t v = fx::param(cg[k]);
+                std::memcpy(&cg[k], &v, sizeof(v));
+            }
         }
         CREATE_TRY(cudaMemcpyAsync(h->d_cg, cg.data(), ncg * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         if (h->precision != BCLBM_F64) {
@@ -1394,7 +1415,17 @@ int bclbm_macros_collect(bclbm_handle* h, double* rho, double* vel, double* cg) 
                 for (int k = 0; k < h->nfields; ++k) rho[n * h->nfields + k] = r[k * pad + s];
             if (vel)
                 for (int dd = 0; dd < h->nd; ++dd) vel[n * h->nd + dd] = v[dd * pad + s];
-            if (cg && rk) cg[n] = h->stage_cgf ? static_cast<double>(h->stage_cgf[s]) : c[s];
+            if (cg && rk) {
+                if (h->stage_cgf) {
+                    cg[n] = static_cast<double>(h->stage_cgf[s]);
+                } else if (h->fx_storage) {
+                    int64_t v;
+                    std::memcpy(&v, &c[s], sizeof(v));
+                    cg[n] = fx::to_f64(v);
+                } else {
+                    cg[n] = c[s];
+                }
+            }
         }
     });
     if (cg && rk)
@@ -1471,6 +1502,7 @@ int bclbm_set_force(bclbm_handle* h, const double force[3]) {
     for (int k = 0; k < 3; ++k) {
         prm.force[k] = h->force[k] = force[k];
         prm.forcef[k] = static_cast<float>(force[k]);
+        prm.forcex[k] = fx::param(force[k]);
     }
     CUDA_TRY(h, cudaMemcpyAsync(h->d_params, &prm, offsetof(DevParams, fx_overflow), cudaMemcpyHostToDevice,
                                 h->stream));

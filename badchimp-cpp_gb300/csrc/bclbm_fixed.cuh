@@ -329,10 +329,18 @@ struct RkConsts {
     int64_t w2_3, w2_45; // 3 w_diag, 4.5 w_diag
     int64_t w2s;         // w_diag / sqrt(2) (recolouring of the diagonal links, |c| = sqrt 2)
     int64_t B[3];        // calcDeltaOmegaST's B_q by class
+    int64_t beta;        // recolouring parameter
+    int64_t st;          // 9/8 sigma: the surface-tension amplitude is 9/8 sigma oms |grad|
+    int64_t third;       // 1/3
+    // Equal kinematic viscosities make the relaxation rate a constant,
+    // oms = nu^-1 / (3 + nu^-1 / 2) (Dn = nu^-1 rho at every node), and with it
+    // the products below; otherwise the kernel forms them per node.
+    int uniform;
+    int64_t oms, oms_w2, oms_k45, oms_k3, tf3w2, st_oms;
 };
 
 template <int Q>
-inline RkConsts make_rk_consts() {
+inline RkConsts make_rk_consts(double nu0inv, double nu1inv, double sigma, double beta) {
     using L = Lat<Q>;
     RkConsts K;
     const double w1 = L::w(0), w2 = L::w(L::NP - 1);
@@ -344,6 +352,17 @@ inline RkConsts make_rk_consts() {
     K.B[0] = param(L::B(L::REST));
     K.B[1] = param(L::B(0));
     K.B[2] = param(L::B(L::NP - 1));
+    K.beta = param(beta);
+    K.st = param(1.125 * sigma);
+    K.third = param(1.0 / 3.0);
+    K.uniform = nu0inv == nu1inv;
+    const double oms = K.uniform ? nu0inv / (3.0 + 0.5 * nu0inv) : 0.0;
+    K.oms = param(oms);
+    K.oms_w2 = param(oms * w2);
+    K.oms_k45 = param(oms * 4.5 * w2);
+    K.oms_k3 = param(oms * 3.0 * w2);
+    K.tf3w2 = param((1.0 - 0.5 * oms) * 3.0 * w2);
+    K.st_oms = param(1.125 * sigma * oms);
     return K;
 }
 

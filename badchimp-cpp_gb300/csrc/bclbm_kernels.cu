@@ -14,12 +14,20 @@ std::atomic<int64_t>& launch_counter() {
     return n;
 }
 
+// the fixed-point copy of the flux controller's force; |F| >= 8 is out of range
+__device__ void set_forcex(DevParams* params) {
+    int ovf = 0;
+    params->forcex[0] = fx::from_f64(params->force[0], ovf);
+    if (ovf) params->fx_overflow |= 1;
+}
+
 __global__ void k_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params) {
     // meanfcXGlobal /= numNodesGlobal; bodyForce.x = 2 * (setMomX - meanfcXGlobal)
     // (src/twophase/main_TWOPHASE.cpp:301-308)
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         params->force[0] = 2 * (mom_x - sum[0] * inv_n);
         params->forcef[0] = static_cast<float>(params->force[0]);
+        set_forcex(params);
     }
 }
 
@@ -29,6 +37,7 @@ __global__ void k_rk_fix(const double* sum, double n, double rho_ref, double mom
         if (flux) {
             params->force[0] = 2 * (mom_x - sum[0] / n);
             params->forcef[0] = static_cast<float>(params->force[0]);
+            set_forcex(params);
         }
         if (fix) {
             // totals now: n rho_ref + sum[1] and sum[2]; the deficit spread over the nodes

@@ -28,6 +28,7 @@ constexpr double C2 = 1.0 / 3.0;  // DXQY::c2 = 1.0 / c2Inv
 struct DevParams {
     double force[3];
     float forcef[3];  // the same force rounded to FP32, for the FP32-arithmetic kernels
+    int64_t forcex[3];  // and in 64-bit fixed point, for the fixed-point two-phase kernel
     int fx_overflow;  // set by the fixed-point kernel when a value left its range
     // two-phase shifted storage: the conserved totals sum f0 + f1 and sum f0 - f1
     // (set at create) and the uniform per-node correction the collision adds this
@@ -45,6 +46,8 @@ struct StepArgs {
     double* vel_out;        // [D][nf_pad] when MACROS
     double* cg;             // RK, F64: colour of [nf fluid | ns solids | ghost]
     float* cgf;             // RK, shifted formats: the same colour field in FP32
+    int64_t* cgx;           // RK, int64 fixed-point state: the colour field in fixed point
+                            // (the buffer of cg, which that step does not use)
     const DevParams* params;
     double tau, tau_anti;   // single phase: relaxation times; RK: unused
     double tau_inv, tf;     // exact single phase: 1/tau, 1 - 0.5/tau (host-computed like the reference)
@@ -817,7 +820,10 @@ __global__ void __launch_bounds__(kBlock, rk_density_min_blocks<S>()) k_rk_densi
         using T = typename Store<S>::T;
         const S* g = static_cast<const S*>(a.src);
         if constexpr (std::is_same<S, int64_t>::value) {
-            // int64 fixed-point state: exact sums, the colour in FP64 as the reference forms it
+            // int64 fixed-point state: exact sums, the colour formed in FP64 as the
+            // reference forms it (this pass is bound by its loads) and kept in fixed
+            // point for the gradient of the collision pass; |colour| >= 2 is out of
+            // that pass's range
             T v0[Q], v1[Q];
             load_field2<Q, S, LOCAL>(g, a.L, i, v0, v1);
             int64_t r0 = 0, r1 = 0, jx = 0;
@@ -827,7 +833,9 @@ __global__ void __launch_bounds__(kBlock, rk_density_min_blocks<S>()) k_rk_densi
                 r1 += v1[q];
                 if (SUMS) jx += Lat<Q>::cx(q) * (v0[q] + v1[q]);
             }
-            a.cg[i] = fx::store_f64(r0 - r1) / fx::store_f64(r0 + r1);
+            unsigned emax = 0;
+            a.cgx[i] = fx::load_f64_hw(fx::store_f64(r0 - r1) / fx::store_f64(r0 + r1), emax);
+            if (emax >= (1024u << 20)) atomicOr(a.fx_flag, 1);
             if (SUMS) fx = fx::store_f64(jx);
         } else if constexpr (!Store<S>::shifted) {
             T v0[Q], v1[Q];
@@ -1062,12 +1070,19 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_collide_shift
 
 // PASS 2 of the default FP64 two-phase step, on the int64 fixed-point state
 // (main_TWOPHASE.cpp:312-376, the expressions of k_rk_collide_f64 regrouped by
-// direction pairs).  The per-node scalars - the relaxation rate of the phase
-// mix, the colour gradient, its norm and direction, the surface-tension and
-// recolouring amplitudes, the colour fraction - are formed in FP64 (about a
-// hundred FP64 operations per node) and converted; every per-direction term is
-// a 64-bit fixed-point product.  With ft = f0 + f1, P / M the pair sums and
-// j = sum ft c + F/2 (exact):
+// direction pairs).  Every term is a 64-bit fixed-point product: the FP64 pipe
+// issues one warp instruction per 16 cycles, so the per-node scalars stay off
+// it too.
+//   colour gradient: the exact integer sum of the fixed-point colours
+//     (DXQY::grad with the weights' common factor 1/12 taken out);
+//   |G| and G / |G|: the gradient scaled by a power of two to [1/2, 1), an FP32
+//     reciprocal square root and two Newton steps in fixed point, and the
+//     reference's |G| < eps case (G / (|G| + 1) = G to 2^-104);
+//   c0 = rho0 / rho: 1/rho times rho0 and one correction by its residual;
+//   recolouring amplitude beta rho0 rho1 / rho = beta c0 rho1;
+//   relaxation rate oms = Dn / (3 rho + Dn / 2): a per-handle constant when the
+//     two viscosities are equal, else formed in FP64 from the exact densities.
+// With ft = f0 + f1, P / M the pair sums and j = sum ft c + F/2 (exact):
 //   X_q = (1 - oms) ft_q + oms feq_q + dF_q + dST_q,
 //   out0 = c0 X_q + dRC_q,  out1 = X_q - out0   (c1 = 1 - c0),
 // where oms feq_q = oms w (rho - 1.5 j.u) + 4.5 oms w (c.j)(c.u) +- 3 oms w (c.j).
@@ -1084,11 +1099,11 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_FX_MINB) k_rk_collide_fx(Step
     const size_t pad = static_cast<size_t>(a.L.nf_pad);
     int64_t X0[Q], X1[Q];
     load_field2<Q, int64_t, LOCAL>(static_cast<const int64_t*>(a.src), a.L, i, X0, X1);
-    // colour at the downstream neighbours (grad, LButilities.h:12-22)
-    double sc[Q];
+    // colour at the downstream neighbours (grad, LButilities.h:12-22), a quarter
+    // of it so that the gradient sums stay inside the range (|colour| < 2)
+    int64_t sc[Q - 1];
 #pragma unroll
-    for (int q = 0; q < Q - 1; ++q) sc[q] = a.cg[ld_table(a.L.nbr + static_cast<size_t>(q) * pad + i)];
-    sc[R] = a.cg[i];
+    for (int q = 0; q < Q - 1; ++q) sc[q] = a.cgx[ld_table(a.L.nbr + static_cast<size_t>(q) * pad + i)] >> 2;
     int ovf = 0;
     int64_t rho0 = 0, rho1 = 0, ft[Q];
 #pragma unroll
@@ -1108,10 +1123,9 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_FX_MINB) k_rk_collide_fx(Step
         if (t > 108) ovf = 1;
     }
     // the body force (the flux controller may change it every step)
-    unsigned emax = 0;
     int64_t Ff[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) Ff[d] = fx::load_f64_hw(a.params->force[d], emax);
+    for (int d = 0; d < 3; ++d) Ff[d] = a.params->forcex[d];
     int64_t j[3] = {0, 0, 0};
 #pragma unroll
     for (int k = 0; k < NP; ++k) {
@@ -1133,44 +1147,89 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_FX_MINB) k_rk_collide_fx(Step
     int64_t u[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d) u[d] = fx::mul_su(j[d], inv);
-    // per-node scalars in FP64, as the reference forms them
-    const double r0 = fx::store_f64(rho0), r1 = fx::store_f64(rho1), r = fx::store_f64(rho);
-    const double Dn = r0 * a.nu0inv + r1 * a.nu1inv;
-    const double oms_d = Dn / (3.0 * r + 0.5 * Dn);  // 1 / tau, tau = 3 rho / Dn + 0.5
-    double G[3] = {0.0, 0.0, 0.0};
-    grad_ref<Q>(sc, G);
-    const double cgn = sqrt(dot_ref<Q>(G, G));
-    const double gs = 1.0 / (cgn + static_cast<double>(cgn < 2.220446049250313080847e-16));
-    const double inv_r = 1.0 / r;
-    const int64_t oms = fx::load_f64_hw(oms_d, emax);
-    const int64_t tf = fx::load_f64_hw(1.0 - 0.5 * oms_d, emax);
-    const int64_t af = fx::load_f64_hw(1.125 * cgn * a.sigma * oms_d, emax);
-    const int64_t rfb = fx::load_f64_hw(a.beta * r0 * r1 * inv_r, emax);
-    const int64_t c0 = fx::load_f64_hw(r0 * inv_r, emax);
-    int64_t n[3] = {0, 0, 0};
-#pragma unroll
-    for (int d = 0; d < D; ++d) n[d] = fx::load_f64_hw(G[d] * gs, emax);
-    if (emax >= fx::kLoadEmaxLimit) ovf = 1;
     const fx::RkConsts& K = a.fxr;
+    // colour fraction and recolouring amplitude
+    int64_t c0 = fx::mul_su(rho0, inv);
+    c0 += fx::mul_su(rho0 - fx::mul_su(c0, rho), inv);
+    const int64_t rfb = fx::mul_ss(fx::mul_ss(c0, rho1), K.beta);
+    // colour gradient G = T / 3, T = sum_q (36 w_q) c_q sc_q
+    int64_t T[3] = {0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) {
+        const int m = Lat<Q>::wclass(q) == 1 ? (Q == 19 ? 2 : 4) : 1;
+        if (Lat<Q>::cx(q) != 0) T[0] += (Lat<Q>::cx(q) * m) * sc[q];
+        if (Lat<Q>::cy(q) != 0) T[1] += (Lat<Q>::cy(q) * m) * sc[q];
+        if (D == 3 && Lat<Q>::cz(q) != 0) T[2] += (Lat<Q>::cz(q) * m) * sc[q];
+    }
+    // |G| and n = G / |G| (the reference's gs = 1 / (|G| + (|G| < eps)))
+    int64_t n[3] = {0, 0, 0}, cgn = 0;
+    {
+        auto mag = [](int64_t v) { return static_cast<uint64_t>(v < 0 ? -v : v); };
+        uint64_t mx = max(mag(T[0]), mag(T[1]));
+        if (D == 3) mx = max(mx, mag(T[2]));
+        if (mx != 0) {
+            // |T_d| < 6 (|sc| < 1/2): mx < 2^63, and t = T 2^sh has max |t_d| in [1/2, 1)
+            const int sh = __clzll(static_cast<long long>(mx)) - 4;
+            int64_t t[3] = {0, 0, 0};
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+                t[d] = sh >= 0 ? static_cast<int64_t>(static_cast<uint64_t>(T[d]) << sh) : (T[d] >> -sh);
+            int64_t x = fx::mul_ss(t[0], t[0]) + fx::mul_ss(t[1], t[1]);  // |t|^2 in [1/4, 3)
+            if (D == 3) x += fx::mul_ss(t[2], t[2]);
+            const float xf = static_cast<float>(static_cast<int>(x >> 32)) * 3.7252902984619140625e-9f;  // 2^-28
+            int64_t y = static_cast<int64_t>(__float2int_rn(rsqrtf(xf) * 536870912.0f)) << 31;  // 2^29
+#pragma unroll
+            for (int it = 0; it < 2; ++it)  // y (3 - x y^2) / 2
+                y = fx::mul_uu(y, 3 * fx::ONE - fx::mul_uu(x, fx::mul_uu(y, y))) >> 1;
+            const int64_t r3 = fx::mul_uu(fx::mul_uu(x, y), K.third);  // |t| / 3
+            cgn = sh >= 0 ? r3 >> sh : static_cast<int64_t>(static_cast<uint64_t>(r3) << -sh);
+            if (cgn >= 256) {  // |G| >= 2^-52
+#pragma unroll
+                for (int d = 0; d < D; ++d) n[d] = fx::mul_su(t[d], y);
+            } else {
+#pragma unroll
+                for (int d = 0; d < D; ++d) n[d] = fx::mul_su(T[d], K.third);
+            }
+        }
+    }
+    // relaxation rate and the products that carry it
+    int64_t oms, omsw2, k45, K3, tf3w2, sto;
+    if (K.uniform) {
+        oms = K.oms;
+        omsw2 = K.oms_w2;
+        k45 = K.oms_k45;
+        K3 = K.oms_k3;
+        tf3w2 = K.tf3w2;
+        sto = K.st_oms;
+    } else {
+        const double r0d = fx::store_f64(rho0), r1d = fx::store_f64(rho1), rd = fx::store_f64(rho);
+        const double Dn = r0d * a.nu0inv + r1d * a.nu1inv;
+        unsigned emax = 0;
+        oms = fx::load_f64_hw(Dn / (3.0 * rd + 0.5 * Dn), emax);  // 1 / tau, tau = 3 rho / Dn + 0.5
+        if (emax >= fx::kLoadEmaxLimit) ovf = 1;
+        omsw2 = fx::mul_su(oms, K.w2);
+        k45 = fx::mul_su(oms, K.w2_45);
+        K3 = fx::mul_su(oms, K.w2_3);
+        tf3w2 = fx::mul_su(fx::ONE - (oms >> 1), K.w2_3);
+        sto = fx::mul_ss(oms, K.st);
+    }
+    const int64_t af = fx::mul_su(sto, cgn);  // 9/8 sigma oms |G|
     const int64_t hom = (fx::ONE - oms) >> 1;  // (1 - oms) / 2
     int64_t ju = fx::mul_ss(j[0], u[0]) + fx::mul_ss(j[1], u[1]);
     if (D == 3) ju += fx::mul_ss(j[2], u[2]);
-    const int64_t AB2 = fx::mul_ss(rho - (ju + (ju >> 1)), fx::mul_su(oms, K.w2));  // oms w2 (rho - 1.5 j.u)
-    const int64_t k45 = fx::mul_su(oms, K.w2_45);
-    const int64_t K3 = fx::mul_su(oms, K.w2_3);
+    const int64_t AB2 = fx::mul_su(rho - (ju + (ju >> 1)), omsw2);  // oms w2 (rho - 1.5 j.u)
     int64_t u45[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d) u45[d] = fx::mul_su(u[d], k45);
     // force terms: -3 w2 tf u.F, and 3 w2 tf F_d (ka3 of a direction = c . g3, kf9 = 3 c . g3)
-    const int64_t tf3w2 = fx::mul_ss(tf, K.w2_3);
     int64_t uF = 0, g3[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d)
         if (Ff[d] != 0) {
             uF += fx::mul_ss(u[d], Ff[d]);
-            g3[d] = fx::mul_ss(Ff[d], tf3w2);
+            g3[d] = fx::mul_su(Ff[d], tf3w2);
         }
-    const int64_t K2 = -fx::mul_ss(uF, tf3w2);
+    const int64_t K2 = -fx::mul_su(uF, tf3w2);
     // surface tension af (w cn^2 - B) and recolouring rfb w cn / |c|
     const int64_t afw2 = fx::mul_ss(af, K.w2);
     const int64_t afB1 = fx::mul_ss(af, K.B[1]), afB2 = fx::mul_ss(af, K.B[2]), afB0 = fx::mul_ss(af, K.B[0]);
@@ -1188,14 +1247,14 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_FX_MINB) k_rk_collide_fx(Step
         const int64_t cn = cx * n[0] + cy * n[1] + cz * n[2];
         const int64_t P = ft[k] + ft[k + NP], M = ft[k] - ft[k + NP];
         const int64_t cn2 = fx::mul_ss(cn, cn);
-        int64_t Sv = fx::mul_ss(P, hom) + by_class(AB2 + fx::mul_ss(cj, cu45) + K2 + fx::mul_ss(cn2, afw2), c) -
+        int64_t Sv = fx::mul_ss(P, hom) + by_class(AB2 + fx::mul_ss(cj, cu45) + K2 + fx::mul_su(afw2, cn2), c) -
                      (c == 1 ? afB1 : afB2);
         const int64_t ka3 = by_class(cx * g3[0] + cy * g3[1] + cz * g3[2], c);
         if (ka3 != 0) {  // 9 w tf (c.F)(c.u) for the directions with c.F != 0 (uniform over the grid)
             const int64_t cu = cx * u[0] + cy * u[1] + cz * u[2];
             Sv += fx::mul_ss(3 * ka3, cu);
         }
-        const int64_t Av = fx::mul_ss(M, hom) + by_class(fx::mul_ss(cj, K3), c) + ka3;
+        const int64_t Av = fx::mul_ss(M, hom) + by_class(fx::mul_su(cj, K3), c) + ka3;
         const int64_t Xk = Sv + Av, Xr = Sv - Av;
         const int64_t dRC = fx::mul_ss(cn, c == 1 ? rfb1 : rfb2);
         const int64_t o0k = fx::mul_ss(c0, Xk) + dRC, o0r = fx::mul_ss(c0, Xr) - dRC;
@@ -1203,13 +1262,13 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_FX_MINB) k_rk_collide_fx(Step
         store_pair(out, static_cast<size_t>(k + NP) * pad + i, o0r, Xr - o0r);
     }
     {
-        const int64_t XR = ft[R] - fx::mul_ss(ft[R], oms) + by_class(AB2 + K2, 0) - afB0;
+        const int64_t XR = ft[R] - fx::mul_su(ft[R], oms) + by_class(AB2 + K2, 0) - afB0;
         const int64_t o0 = fx::mul_ss(c0, XR);
         store_pair(out, static_cast<size_t>(R) * pad + i, o0, XR - o0);
     }
     if (MACROS) {
-        a.rho_out[i] = r0;
-        a.rho_out[pad + i] = r1;
+        a.rho_out[i] = fx::store_f64(rho0);
+        a.rho_out[pad + i] = fx::store_f64(rho1);
 #pragma unroll
         for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * pad + i] = fx::store_f64(u[d]);
     }

@@ -194,3 +194,52 @@ def test_two_phase_mass_drift_correction(bclbm, gpu):
             drift[fix] = abs(s.reduce()["saturation"] - s0)
     assert drift[True] <= 1e-7, drift
     assert drift[False] >= 10 * drift[True], drift
+
+
+UV_TAUS, UV_WETT, UV_SIGMA, UV_STEPS = (0.7, 1.3), 0.8, 0.02, 100
+
+
+@pytest.mark.parametrize("lattice,shape,radius", [("D3Q19", (40, 40, 40), 6.0), ("D2Q9", (160, 128), 9.0)])
+def test_two_phase_unequal_viscosities(bclbm, gpu, oracle, lattice, shape, radius):
+    """tau_r != tau_b (the relaxation rate varies with the phase mix at every node)
+    and non-neutral wetting (boundary solids of colour 0.6): exact FP64 equal to
+    the oracle, the fixed-point and FMA forms within 1e-12 after 100 steps."""
+    L = bclbm.lbsolver
+    geo, _, _ = bclbm.geometry.sphere_pack(shape, radius=radius, porosity=POROSITY, seed=SEED + 7)
+    lat = L.Lattice.from_geometry(geo, lattice, "xyz"[:len(shape)])
+    nq = lat.nq
+    red = np.random.default_rng(SEED + 8).random(geo.shape) < 0.5
+    rho0 = np.where(geo == 1, red, 0.0)
+    rho1 = np.where(geo == 1, ~red, 0.0).astype(np.float64)
+    f0, rho = L.initiate_twophase(lat, lat.attribute(rho0), lat.attribute(rho1),
+                                  lat.attribute(np.full(geo.shape, UV_WETT)))
+    force = (GX, 0.0, 0.0)
+    g = oracle.OracleGrid(lat.nq, lat.neigh, lat.types, lat.bulk)
+    ef, er, evel, ecg, _ = oracle.twophase_run(g, f0.copy(), rho.copy(), UV_STEPS, *UV_TAUS, UV_SIGMA, BETA, force,
+                                               nthreads=oracle.default_threads())
+    b = lat.bulk
+    nd = 2 if nq == 9 else 3
+    ef = ef.reshape(-1, 2, nq)[b]
+    er = er.reshape(-1, 2)[b]
+    evel = evel.reshape(-1, nd)[b]
+    ecg = ecg[b]
+    sb = lat.types == 1
+    assert sb.any()
+    for mode, kw in (("exact", dict(exact=True)), ("fixed", {}), ("fma", dict(fma64=True))):
+        with L.Solver(lat, f0, collision=L.RK, tau=UV_TAUS, force=force, sigma=UV_SIGMA, beta=BETA,
+                      rho_init=rho, **kw) as s:
+            s.step(UV_STEPS)
+            f = s.download_f().reshape(-1, 2, nq)[b]
+            r, vel, cg = s.download_macros()
+        r, vel, cgb = r.reshape(-1, 2)[b], vel.reshape(-1, nd)[b], cg[b]
+        # the boundary solids report the wetting colour (rho0 - rho1) / (rho0 + rho1)
+        assert np.allclose(cg[sb], (UV_WETT - (1 - UV_WETT)) / 1.0, atol=1e-7), mode
+        if mode == "exact":
+            assert np.array_equal(f, ef), mode
+            assert np.array_equal(r, er), mode
+            assert np.array_equal(cgb, ecg), mode
+        else:
+            assert relerr(f, ef) <= 1e-12, mode
+            assert relerr(r, er) <= 1e-12, mode
+            assert relerr(cgb, ecg) <= 1e-12, mode
+            assert np.abs(vel - evel).max() <= u_bound(evel, ef, UV_STEPS), mode
