@@ -145,6 +145,12 @@ int validate_descriptor(const bclbm_desc* d, std::string& err) {
     if ((d->flags & BCLBM_FLAG_SFC_ORDER) && !d->pos) { err = "BCLBM_FLAG_SFC_ORDER needs pos"; return BCLBM_ERR_INVALID; }
     if (d->n_bulk >= d->n_nodes) { err = "n_bulk must be smaller than n_nodes"; return BCLBM_ERR_INVALID; }
     const bool fixed = d->precision == BCLBM_F64 && !(d->flags & (BCLBM_FLAG_EXACT | BCLBM_FLAG_FP64_FMA));
+    if (fixed && d->collision != BCLBM_RK && !(d->tau[0] > 0.5 && (d->collision != BCLBM_TRT || d->tau[1] > 0.5))) {
+        // the fixed-point collision holds oms / 2, oma / 2 and 1 - 0.5 / tau as constants in [0, 1)
+        err = "the fixed-point FP64 step needs tau > 0.5 (and tau_anti > 0.5 for TRT; "
+              "BCLBM_FLAG_FP64_FMA or BCLBM_FLAG_EXACT take any value)";
+        return BCLBM_ERR_INVALID;
+    }
     if (fixed && d->collision == BCLBM_RK && !(std::fabs(d->sigma) < 3.5 && std::fabs(d->beta) < 4.0)) {
         // 9/8 sigma and beta are fixed-point constants of the default FP64 two-phase step
         err = "the fixed-point FP64 two-phase step needs |sigma| < 3.5 and |beta| < 4 "

@@ -79,9 +79,9 @@ __host__ __device__ __forceinline__ int64_t mul(int64_t a, int64_t b) {
 // The kernel's products, by operand signs (uu: both >= 0, su: b >= 0, ss).
 // All equal mul() bit for bit.
 // hi:lo of the unsigned 128-bit product a b + 2^59 (the rounding constant),
-// from four 32 x 32 -> 64 partial products that share their carries.
-__host__ __device__ __forceinline__ void umul128_round(uint64_t a, uint64_t b, uint64_t& hi, uint32_t& lo_hi) {
-#ifdef __CUDA_ARCH__
+// from four 32 x 32 -> 64 partial products that share their carries (the
+// device's form; callable on the host so that it can be checked there).
+__host__ __device__ __forceinline__ void umul128_round_pieces(uint64_t a, uint64_t b, uint64_t& hi, uint32_t& lo_hi) {
     const uint32_t a0 = static_cast<uint32_t>(a), a1 = static_cast<uint32_t>(a >> 32);
     const uint32_t b0 = static_cast<uint32_t>(b), b1 = static_cast<uint32_t>(b >> 32);
     const uint64_t p00 = static_cast<uint64_t>(a0) * b0;
@@ -90,6 +90,11 @@ __host__ __device__ __forceinline__ void umul128_round(uint64_t a, uint64_t b, u
     const uint64_t p10 = static_cast<uint64_t>(a1) * b0 + static_cast<uint32_t>(p01);
     hi = static_cast<uint64_t>(a1) * b1 + (p01 >> 32) + (p10 >> 32);
     lo_hi = static_cast<uint32_t>(p10);  // bits [32, 64) of the low word
+}
+
+__host__ __device__ __forceinline__ void umul128_round(uint64_t a, uint64_t b, uint64_t& hi, uint32_t& lo_hi) {
+#ifdef __CUDA_ARCH__
+    umul128_round_pieces(a, b, hi, lo_hi);
 #else
     const unsigned __int128 p = static_cast<unsigned __int128>(a) * b + (static_cast<unsigned __int128>(1) << (FB - 1));
     hi = static_cast<uint64_t>(p >> 64);
@@ -97,9 +102,45 @@ __host__ __device__ __forceinline__ void umul128_round(uint64_t a, uint64_t b, u
 #endif
 }
 
+// High word of the unsigned 128-bit product a b + 2^63, in the same pieces
+// (+ 2^31 at weight 2^32; the sum stays below 2^64).
+__host__ __device__ __forceinline__ uint64_t umulhi_r63_pieces(uint64_t a, uint64_t b) {
+    const uint32_t a0 = static_cast<uint32_t>(a), a1 = static_cast<uint32_t>(a >> 32);
+    const uint32_t b0 = static_cast<uint32_t>(b), b1 = static_cast<uint32_t>(b >> 32);
+    const uint64_t p00 = static_cast<uint64_t>(a0) * b0;
+    const uint64_t p01 = static_cast<uint64_t>(a0) * b1 + ((p00 >> 32) + (uint64_t(1) << 31));
+    const uint64_t p10 = static_cast<uint64_t>(a1) * b0 + static_cast<uint32_t>(p01);
+    return static_cast<uint64_t>(a1) * b1 + (p01 >> 32) + (p10 >> 32);
+}
+
+__host__ __device__ __forceinline__ uint64_t umulhi_r63(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+    return umulhi_r63_pieces(a, b);
+#else
+    const unsigned __int128 p = static_cast<unsigned __int128>(a) * b + (static_cast<unsigned __int128>(1) << 63);
+    return static_cast<uint64_t>(p >> 64);
+#endif
+}
+
 // bits [60, 124) of the 128-bit product
 __host__ __device__ __forceinline__ int64_t combine(uint64_t hi, uint32_t lo_hi) {
     return static_cast<int64_t>((hi << (64 - FB)) | (lo_hi >> (FB - 32)));
+}
+
+// Products with a constant 0 <= b < 1 held in k form, bk = b 2^4 (b in units of
+// 2^-FB): the rounded product a b 2^-FB is then the high word of a bk + 2^63,
+// with no shift to join two words.  For a signed a, a + 2^63 (a with its sign
+// bit flipped) is unsigned and (a + 2^63) bk 2^-64 = a bk 2^-64 + bk / 2 with
+// bk / 2 an integer, so the sign costs one constant subtraction.  Both equal
+// mul_su(a, b) bit for bit.
+__host__ __device__ __forceinline__ uint64_t kform(int64_t b) { return static_cast<uint64_t>(b) << 4; }
+
+__host__ __device__ __forceinline__ int64_t mul_uk(int64_t a, uint64_t bk) {  // a >= 0
+    return static_cast<int64_t>(umulhi_r63(static_cast<uint64_t>(a), bk));
+}
+
+__host__ __device__ __forceinline__ int64_t mul_sk(int64_t a, uint64_t bk) {
+    return static_cast<int64_t>(umulhi_r63(static_cast<uint64_t>(a) ^ (uint64_t(1) << 63), bk) - (bk >> 1));
 }
 
 // a b / 2^FB rounded to nearest, for a, b >= 0
@@ -288,6 +329,8 @@ struct Consts {
     int64_t ka3[19];      // 3 w_q taf (c_q . F)
     int64_t force[3];     // F
     int64_t half_force[3];  // F / 2
+    // the multipliers in [0, 1) in k form (kform): homs, homa, oms_w2, k45, oma3_w2, tsf3_w2
+    uint64_t homs_k, homa_k, oms_w2_k, k45_k, oma3_w2_k, tsf3_w2_k;
 };
 
 // The constants for relaxation times tau (symmetric) and tau_anti (TRT; BGK
@@ -319,6 +362,13 @@ inline Consts make_consts(bool trt, double tau, double tau_anti, const double* F
         K.force[d] = param(F[d]);
         K.half_force[d] = param(0.5 * F[d]);
     }
+    // tau, tau_anti > 0.5 (checked at create) puts these in [0, 1)
+    K.homs_k = kform(K.homs);
+    K.homa_k = kform(K.homa);
+    K.oms_w2_k = kform(K.oms_w2);
+    K.k45_k = kform(K.k45);
+    K.oma3_w2_k = kform(K.oma3_w2);
+    K.tsf3_w2_k = kform(K.tsf3_w2);
     return K;
 }
 
@@ -438,7 +488,7 @@ __host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K,
     for (int d = 0; d < 3; ++d) {
         j[d] = (d < D) ? J[d] + (SRC ? K.half_force[d] * fo : K.half_force[d]) : 0;
         u[d] = (d < D) ? mul_su(j[d], inv) : 0;
-        u45[d] = (d < D) ? mul_su(u[d], K.k45) : 0;
+        u45[d] = (d < D) ? mul_sk(u[d], K.k45_k) : 0;
     }
     rho_o = rho;
 #pragma unroll
@@ -459,13 +509,13 @@ __host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K,
     for (int d = 0; d < D; ++d)
         if (K.force[d] != 0) uF += mul_ss(u[d], K.force[d]);
     if (SRC) uF *= fo;
-    const int64_t AB2 = mul_su(rho_e - (ju + (ju >> 1)), K.oms_w2);  // oms w2 (rho_e - 1.5 j.u)
-    const int64_t K2 = -mul_su(uF, K.tsf3_w2);                      // -3 w2 tsf u.F
+    const int64_t AB2 = mul_sk(rho_e - (ju + (ju >> 1)), K.oms_w2_k);  // oms w2 (rho_e - 1.5 j.u)
+    const int64_t K2 = -mul_sk(uF, K.tsf3_w2_k);                      // -3 w2 tsf u.F
     // class c values (rest 0, axis 1, diagonal 2) by the exact weight ratios
     auto by_class = [](int64_t v2, int c) -> int64_t {
         return c == 2 ? v2 : (c == 1 ? (v2 << SH1) : (Q == 19 ? (v2 << 3) + (v2 << 2) : (v2 << 4)));
     };
-    const int64_t homa = TRT ? K.homa : K.homs;
+    const uint64_t homa_k = TRT ? K.homa_k : K.homs_k;
 #pragma unroll
     for (int k = 0; k < NP; ++k) {
         const int c = Lat<Q>::wclass(k);
@@ -477,9 +527,9 @@ __host__ __device__ __forceinline__ void collide_to(int64_t* F, const Consts& K,
             const int64_t cu = Lat<Q>::cx(k) * u[0] + Lat<Q>::cy(k) * u[1] + Lat<Q>::cz(k) * u[2];
             X += SRC ? mul_ss(K.kf9[k], cu) * fo : mul_ss(K.kf9[k], cu);
         }
-        const int64_t Y = by_class(mul_su(cj, K.oma3_w2), c) + (SRC ? K.ka3[k] * fo : K.ka3[k]);
+        const int64_t Y = by_class(mul_sk(cj, K.oma3_w2_k), c) + (SRC ? K.ka3[k] * fo : K.ka3[k]);
         const int64_t P = F[k] + F[k + NP], M = F[k] - F[k + NP];
-        const int64_t sp = mul_su(P, K.homs), sm = mul_su(M, homa);
+        const int64_t sp = mul_sk(P, K.homs_k), sm = mul_sk(M, homa_k);
         sink(k, F[k] - sp - sm + X + Y);
         sink(k + NP, F[k + NP] - sp + sm + X - Y);
     }

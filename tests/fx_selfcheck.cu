@@ -109,6 +109,23 @@ int fx_primitives(const double* a, const double* b, int n) {
         if (fx::mul_ss(xa, xb) != ref) ++bad;
         if (xb >= 0 && fx::mul_su(xa, xb) != ref) ++bad;
         if (xa >= 0 && xb >= 0 && fx::mul_uu(xa, xb) != ref) ++bad;
+        // the device's 32-bit-piece forms against 128-bit products
+        const uint64_t ua = static_cast<uint64_t>(xa), ub = static_cast<uint64_t>(xb);
+        const unsigned __int128 up = static_cast<unsigned __int128>(ua) * ub;
+        uint64_t hi;
+        uint32_t lh;
+        fx::umul128_round_pieces(ua, ub, hi, lh);
+        const unsigned __int128 r59 = up + (static_cast<unsigned __int128>(1) << 59);
+        if (hi != static_cast<uint64_t>(r59 >> 64) || lh != static_cast<uint32_t>(static_cast<uint64_t>(r59) >> 32)) ++bad;
+        const unsigned __int128 r63 = up + (static_cast<unsigned __int128>(1) << 63);
+        if (fx::umulhi_r63_pieces(ua, ub) != static_cast<uint64_t>(r63 >> 64)) ++bad;
+        // k-form products for multipliers in [0, 1): equal to mul_su
+        if (xb >= 0 && xb < fx::ONE) {
+            const uint64_t bk = fx::kform(xb);
+            if (fx::mul_sk(xa, bk) != ref) ++bad;
+            if (static_cast<int64_t>(fx::umulhi_r63_pieces(ua ^ (uint64_t(1) << 63), bk) - (bk >> 1)) != ref) ++bad;
+            if (xa >= 0 && fx::mul_uk(xa, bk) != ref) ++bad;
+        }
     }
     return bad;
 }

@@ -47,6 +47,9 @@ def test_primitives_against_128bit_reference(fxlib):
                         rng.uniform(0.01, 0.4, 20000), 10.0 ** rng.uniform(-17, 0, 20000)])
     b = np.concatenate([rng.uniform(-1.0, 1.0, 20000), rng.uniform(-2.0, 2.0, 20000),
                         rng.uniform(0.5, 1.5, 20000), rng.uniform(-1.0, 1.0, 20000)])
+    # multipliers of the k-form products: [0, 1), with both ends
+    a = np.concatenate([a, rng.uniform(-7.9, 7.9, 20000), [-7.999, 7.999, 0.0, -1e-18, 1e-18]])
+    b = np.concatenate([b, rng.uniform(0.0, 1.0, 20000), [0.999999999, 0.0, 0.5, 1e-18, 0.999999999]])
     assert fxlib.fx_primitives(_p(a), _p(b), a.size) == 0
 
 
