@@ -104,13 +104,20 @@ __device__ __forceinline__ void load_links_fx(const int64_t* __restrict__ g, con
     }
     int e[Q - 1];
 #pragma unroll
-    for (int q = 0; q < Q - 1; ++q) e[q] = __ldg(L.pull + static_cast<size_t>(q) * pad + i);
+    for (int q = 0; q < Q - 1; ++q) e[q] = ld_table(L.pull + static_cast<size_t>(q) * pad + i);
 #pragma unroll
-    for (int q = 0; q < Q - 1; ++q) X[q] = g[e[q] >= 0 ? e[q] : ~e[q]];
-    X[R] = g[static_cast<size_t>(R) * pad + i];
+    for (int q = 0; q < Q - 1; ++q) X[q] = ld_pop(g + (e[q] >= 0 ? e[q] : ~e[q]));
+    X[R] = ld_pop(g + static_cast<size_t>(R) * pad + i);
+    // the pressure boundary's links (FP64) behind one branch per node: predicated per
+    // direction, their conversions would occupy the FP64 pipe in every warp
+    unsigned neg = 0;
 #pragma unroll
-    for (int q = 0; q < Q - 1; ++q)
-        if (e[q] < 0) X[q] = fx::load_f64_hw(anti_bounce_back(q, fx::store_f64(X[q]), u, rho_w), emax);
+    for (int q = 0; q < Q - 1; ++q) neg |= (static_cast<unsigned>(e[q]) >> 31) << q;
+    if (__builtin_expect(neg != 0, 0)) {
+#pragma unroll
+        for (int q = 0; q < Q - 1; ++q)
+            if (neg & (1u << q)) X[q] = fx::load_f64_hw(anti_bounce_back(q, fx::store_f64(X[q]), u, rho_w), emax);
+    }
 }
 
 template <bool LOCAL>
@@ -253,18 +260,16 @@ __global__ void __launch_bounds__(kBlock, BCLBM_FX_MINB) k_links_collide_fixed(L
     int64_t rho, uf[3];
     fx::collide_to<19, false, true>(
         X, A.s.fxk, rho, uf, ovf, [out, pad](int q, int64_t v) { out[static_cast<size_t>(q) * pad] = v; }, fo, qm);
-    double vel[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) vel[d] = fx::store_f64(uf[d]);
+    // FP64 velocities only where they are kept: pressure-boundary nodes and macro downloads
     if (inf & kLinkPress) {
         const int p = __ldg(A.pidx + i);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) A.ustore[static_cast<size_t>(d) * A.npress + p] = vel[d];
+        for (int d = 0; d < 3; ++d) A.ustore[static_cast<size_t>(d) * A.npress + p] = fx::store_f64(uf[d]);
     }
     if (A.s.rho_out) {
         A.s.rho_out[i] = fx::store_f64(rho);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) A.s.vel_out[static_cast<size_t>(d) * pad + i] = vel[d];
+        for (int d = 0; d < 3; ++d) A.s.vel_out[static_cast<size_t>(d) * pad + i] = fx::store_f64(uf[d]);
     }
     if (ovf) atomicOr(A.s.fx_flag, 1);
 }
