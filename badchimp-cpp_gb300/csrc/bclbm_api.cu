@@ -438,6 +438,7 @@ LinksArgs links_args(const bclbm_handle* h, const StepArgs& a) {
     A.flux_out = h->d_flux_out;
     A.f_rho_w = static_cast<float>(h->rho_w);
     A.f_dw = static_cast<float>(2.0 * (h->rho_w - h->rho_ref));
+    for (int c = 0; c < 3; ++c) A.x_wrho[c] = fx::param((c == 0 ? 12.0 : c == 1 ? 2.0 : 1.0) / 36.0 * h->rho_w);
     return A;
 }
 

@@ -200,8 +200,8 @@ cudaError_t collide_fma(bool local, const LinksArgs& A, cudaStream_t s) {
 }
 
 cudaError_t mass_fixed(bool local, const LinksArgs& A, cudaStream_t s) {
-    if (local) k_links_mass<false, true, int64_t><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
-    else k_links_mass<false, false, int64_t><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
+    if (local) k_links_mass_fx<true><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
+    else k_links_mass_fx<false><<<grid_for(A.nlabeled), kBlock, 0, s>>>(A);
     launch_counter()++;
     return cudaGetLastError();
 }

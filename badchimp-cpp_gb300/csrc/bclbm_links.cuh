@@ -46,6 +46,7 @@ struct LinksArgs {
     double* flux_out;           // [2]
     float f_rho_w;              // shifted storage: rho_w and 2 (rho_w - rho_ref) in FP32
     float f_dw;
+    int64_t x_wrho[3];          // fixed-point step: w rho_w by weight class (rest, axis, diagonal)
 };
 
 // FP64 value of a stored population: FP64 storage holds f itself; the default
@@ -90,11 +91,12 @@ __device__ __forceinline__ void load_links(const G* __restrict__ g, const Lattic
         if (e[q] < 0) f[q] = anti_bounce_back(q, f[q], u, rho_w);
 }
 
-// load_links of the int64 state without conversions: the anti-bounce-back
-// entries (pressure-boundary nodes only) are formed in FP64 and converted back
+// load_links of the int64 state without conversions, the anti-bounce-back entries
+// (pressure-boundary nodes only) in fixed point from the node's velocity u and
+// xw = w rho_w by weight class
 template <bool LOCAL>
 __device__ __forceinline__ void load_links_fx(const int64_t* __restrict__ g, const LatticeView& L, int i,
-                                              const double* u, double rho_w, int64_t* X, unsigned& emax) {
+                                              const double* u, const int64_t* xw, int64_t* X, unsigned& emax) {
     constexpr int Q = 19, R = Lat<Q>::REST;
     const size_t pad = static_cast<size_t>(L.nf_pad);
     if constexpr (LOCAL) {
@@ -114,9 +116,21 @@ __device__ __forceinline__ void load_links_fx(const int64_t* __restrict__ g, con
 #pragma unroll
     for (int q = 0; q < Q - 1; ++q) neg |= (static_cast<unsigned>(e[q]) >> 31) << q;
     if (__builtin_expect(neg != 0, 0)) {
+        // anti_bounce_back in fixed point, -f_k + 2 w rho_w + w rho_w (9 (c.u)^2 - 3 u^2): the
+        // pressure-boundary nodes sit in nearly every warp (each column of the grid starts and
+        // ends with one), so their terms stay off the FP64 pipe but for the velocity's conversion
+        int64_t ux[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) ux[d] = fx::load_f64_hw(u[d], emax);
+        const int64_t u2 = fx::mul_ss(ux[0], ux[0]) + fx::mul_ss(ux[1], ux[1]) + fx::mul_ss(ux[2], ux[2]);
 #pragma unroll
         for (int q = 0; q < Q - 1; ++q)
-            if (neg & (1u << q)) X[q] = fx::load_f64_hw(anti_bounce_back(q, fx::store_f64(X[q]), u, rho_w), emax);
+            if (neg & (1u << q)) {
+                const int k = Lat<Q>::rev(q);
+                const int64_t cu = Lat<Q>::cx(k) * ux[0] + Lat<Q>::cy(k) * ux[1] + Lat<Q>::cz(k) * ux[2];
+                const int64_t wr = xw[Lat<Q>::wclass(k)];
+                X[q] = 2 * wr - X[q] + fx::mul_ss(9 * fx::mul_ss(cu, cu) - 3 * u2, wr);
+            }
     }
 }
 
@@ -185,6 +199,25 @@ __global__ void __launch_bounds__(kBlock) k_links_mass(LinksArgs A) {
     A.lab_val[k] = 1.0 - rho;
 }
 
+// the mass pass of the int64 state: the node's populations summed exactly, one
+// conversion of 1 - rho
+template <bool LOCAL>
+__global__ void __launch_bounds__(kBlock) k_links_mass_fx(LinksArgs A) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= A.nlabeled) return;
+    const int i = __ldg(A.lab_slot + k);
+    const uint32_t inf = __ldg(A.info + i);
+    double u[3];
+    links_velocity<LOCAL>(A, i, inf, u);
+    unsigned emax = 0;
+    int64_t X[19];
+    load_links_fx<LOCAL>(static_cast<const int64_t*>(A.s.src), A.s.L, i, u, A.x_wrho, X, emax);
+    int64_t rho = 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) rho += X[q];
+    A.lab_val[k] = fx::store_f64(fx::ONE - rho);
+}
+
 // per-label sums of the mass pass and the sources they give.  EXACT: one thread
 // per label adds its nodes in bulk order, as the reference's serial loop does;
 // otherwise one warp per label, strided partial sums and a fixed shuffle tree
@@ -250,7 +283,7 @@ __global__ void __launch_bounds__(kBlock, BCLBM_FX_MINB) k_links_collide_fixed(L
     links_velocity<LOCAL>(A, i, inf, u);
     unsigned emax = 0;
     int64_t X[19];
-    load_links_fx<LOCAL>(static_cast<const int64_t*>(A.s.src), A.s.L, i, u, A.rho_w, X, emax);
+    load_links_fx<LOCAL>(static_cast<const int64_t*>(A.s.src), A.s.L, i, u, A.x_wrho, X, emax);
     int64_t qm = 0;
     if (inf & kLinkAdd) qm = fx::load_f64_hw(A.lab_q[inf & kLinkLabelMask], emax);
     int ovf = emax >= fx::kLoadEmaxLimit ? 1 : 0;
