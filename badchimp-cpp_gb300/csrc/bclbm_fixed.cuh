@@ -387,6 +387,7 @@ struct RkConsts {
     // the products below; otherwise the kernel forms them per node.
     int uniform;
     int64_t oms, oms_w2, oms_k45, oms_k3, tf3w2, st_oms;
+    uint64_t w1_k, w2s_k;  // w_axis, w_diag / sqrt(2) in k form
 };
 
 template <int Q>
@@ -413,6 +414,8 @@ inline RkConsts make_rk_consts(double nu0inv, double nu1inv, double sigma, doubl
     K.oms_k3 = param(oms * 3.0 * w2);
     K.tf3w2 = param((1.0 - 0.5 * oms) * 3.0 * w2);
     K.st_oms = param(1.125 * sigma * oms);
+    K.w1_k = kform(K.w1);
+    K.w2s_k = kform(K.w2s);
     return K;
 }
 

@@ -1214,26 +1214,37 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_FX_MINB) k_rk_collide_fx(Step
         sto = fx::mul_ss(oms, K.st);
     }
     const int64_t af = fx::mul_su(sto, cgn);  // 9/8 sigma oms |G|
-    const int64_t hom = (fx::ONE - oms) >> 1;  // (1 - oms) / 2
+    // the multipliers in [0, 1) in k form (fx::mul_sk): |1 - oms| / 2 (its sign applied to the
+    // products: zero at tau = 1, as the reference's), oms w2, 4.5 oms w2, 3 oms w2, 3 w2 tf
+    const int64_t hom = (fx::ONE - oms) >> 1;
+    const bool hneg = hom < 0;
+    const uint64_t hom_k = fx::kform(hneg ? -hom : hom), omsw2_k = fx::kform(omsw2), k45_k = fx::kform(k45),
+                   K3_k = fx::kform(K3), tf3w2_k = fx::kform(tf3w2);
     int64_t ju = fx::mul_ss(j[0], u[0]) + fx::mul_ss(j[1], u[1]);
     if (D == 3) ju += fx::mul_ss(j[2], u[2]);
-    const int64_t AB2 = fx::mul_su(rho - (ju + (ju >> 1)), omsw2);  // oms w2 (rho - 1.5 j.u)
+    const int64_t AB2 = fx::mul_sk(rho - (ju + (ju >> 1)), omsw2_k);  // oms w2 (rho - 1.5 j.u)
     int64_t u45[3] = {0, 0, 0};
 #pragma unroll
-    for (int d = 0; d < D; ++d) u45[d] = fx::mul_su(u[d], k45);
+    for (int d = 0; d < D; ++d) u45[d] = fx::mul_sk(u[d], k45_k);
     // force terms: -3 w2 tf u.F, and 3 w2 tf F_d (ka3 of a direction = c . g3, kf9 = 3 c . g3)
     int64_t uF = 0, g3[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d)
         if (Ff[d] != 0) {
             uF += fx::mul_ss(u[d], Ff[d]);
-            g3[d] = fx::mul_su(Ff[d], tf3w2);
+            g3[d] = fx::mul_sk(Ff[d], tf3w2_k);
         }
-    const int64_t K2 = -fx::mul_su(uF, tf3w2);
+    const int64_t K2 = -fx::mul_sk(uF, tf3w2_k);
     // surface tension af (w cn^2 - B) and recolouring rfb w cn / |c|
     const int64_t afw2 = fx::mul_ss(af, K.w2);
     const int64_t afB1 = fx::mul_ss(af, K.B[1]), afB2 = fx::mul_ss(af, K.B[2]), afB0 = fx::mul_ss(af, K.B[0]);
-    const int64_t rfb1 = fx::mul_ss(rfb, K.w1), rfb2 = fx::mul_ss(rfb, K.w2s);
+    const int64_t rfb1 = fx::mul_sk(rfb, K.w1_k), rfb2 = fx::mul_sk(rfb, K.w2s_k);
+    // the colour split out0 = c0 X + dRC, out1 = X - out0 through the smaller fraction
+    // m = min(c0, 1 - c0) in [0, 1/2] (a k-form multiplier; the other colour by difference)
+    const bool sw = c0 > (fx::ONE >> 1);
+    int64_t cm = sw ? fx::ONE - c0 : c0;
+    cm = cm < 0 ? 0 : cm;
+    const uint64_t cm_k = fx::kform(cm);
     auto by_class = [](int64_t v2, int c) -> int64_t {
         return c == 2 ? v2 : (c == 1 ? (v2 << SH1) : (Q == 19 ? (v2 << 3) + (v2 << 2) : (v2 << 4)));
     };
@@ -1245,25 +1256,29 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_FX_MINB) k_rk_collide_fx(Step
         const int64_t cj = cx * j[0] + cy * j[1] + cz * j[2];
         const int64_t cu45 = cx * u45[0] + cy * u45[1] + cz * u45[2];
         const int64_t cn = cx * n[0] + cy * n[1] + cz * n[2];
+        const int64_t acn = cn < 0 ? -cn : cn;
+        const int64_t cn2 = fx::mul_uu(acn, acn);
         const int64_t P = ft[k] + ft[k + NP], M = ft[k] - ft[k + NP];
-        const int64_t cn2 = fx::mul_ss(cn, cn);
-        int64_t Sv = fx::mul_ss(P, hom) + by_class(AB2 + fx::mul_ss(cj, cu45) + K2 + fx::mul_su(afw2, cn2), c) -
+        const int64_t sP = fx::mul_sk(P, hom_k), sM = fx::mul_sk(M, hom_k);
+        int64_t Sv = (hneg ? -sP : sP) + by_class(AB2 + fx::mul_ss(cj, cu45) + K2 + fx::mul_su(afw2, cn2), c) -
                      (c == 1 ? afB1 : afB2);
         const int64_t ka3 = by_class(cx * g3[0] + cy * g3[1] + cz * g3[2], c);
         if (ka3 != 0) {  // 9 w tf (c.F)(c.u) for the directions with c.F != 0 (uniform over the grid)
             const int64_t cu = cx * u[0] + cy * u[1] + cz * u[2];
             Sv += fx::mul_ss(3 * ka3, cu);
         }
-        const int64_t Av = fx::mul_ss(M, hom) + by_class(fx::mul_su(cj, K3), c) + ka3;
+        const int64_t Av = (hneg ? -sM : sM) + by_class(fx::mul_sk(cj, K3_k), c) + ka3;
         const int64_t Xk = Sv + Av, Xr = Sv - Av;
         const int64_t dRC = fx::mul_ss(cn, c == 1 ? rfb1 : rfb2);
-        const int64_t o0k = fx::mul_ss(c0, Xk) + dRC, o0r = fx::mul_ss(c0, Xr) - dRC;
+        const int64_t pk = fx::mul_sk(Xk, cm_k), pr = fx::mul_sk(Xr, cm_k);
+        const int64_t o0k = (sw ? Xk - pk : pk) + dRC, o0r = (sw ? Xr - pr : pr) - dRC;
         store_pair(out, static_cast<size_t>(k) * pad + i, o0k, Xk - o0k);
         store_pair(out, static_cast<size_t>(k + NP) * pad + i, o0r, Xr - o0r);
     }
     {
         const int64_t XR = ft[R] - fx::mul_su(ft[R], oms) + by_class(AB2 + K2, 0) - afB0;
-        const int64_t o0 = fx::mul_ss(c0, XR);
+        const int64_t pR = fx::mul_sk(XR, cm_k);
+        const int64_t o0 = sw ? XR - pR : pR;
         store_pair(out, static_cast<size_t>(R) * pad + i, o0, XR - o0);
     }
     if (MACROS) {
