@@ -145,6 +145,15 @@ int validate_descriptor(const bclbm_desc* d, std::string& err) {
     if ((d->flags & BCLBM_FLAG_SFC_ORDER) && !d->pos) { err = "BCLBM_FLAG_SFC_ORDER needs pos"; return BCLBM_ERR_INVALID; }
     if (d->n_bulk >= d->n_nodes) { err = "n_bulk must be smaller than n_nodes"; return BCLBM_ERR_INVALID; }
     const bool fixed = d->precision == BCLBM_F64 && !(d->flags & (BCLBM_FLAG_EXACT | BCLBM_FLAG_FP64_FMA));
+    if ((d->flags & BCLBM_FLAG_LAGGED_COLOUR) && !(d->collision == BCLBM_RK && d->precision != BCLBM_F64)) {
+        err = "BCLBM_FLAG_LAGGED_COLOUR needs BCLBM_RK with shifted storage (F32, F16 or BF16)";
+        return BCLBM_ERR_INVALID;
+    }
+    if ((d->flags & BCLBM_FLAG_LAGGED_COLOUR) && d->flux_control) {
+        // with its sums one step late, the controller force = 2 (target - mean) would overshoot
+        err = "BCLBM_FLAG_LAGGED_COLOUR takes a constant body force (flux_control 0)";
+        return BCLBM_ERR_INVALID;
+    }
     if (fixed && d->collision != BCLBM_RK && !(d->tau[0] > 0.5 && (d->collision != BCLBM_TRT || d->tau[1] > 0.5))) {
         // the fixed-point collision holds oms / 2, oma / 2 and 1 - 0.5 / tau as constants in [0, 1)
         err = "the fixed-point FP64 step needs tau > 0.5 (and tau_anti > 0.5 for TRT; "
@@ -349,6 +358,7 @@ size_t footprint_bytes(const bclbm_desc* d, const Plan& p) {
     b += pad * 4;                                                                          // slot -> bulk
     if (d->collision == BCLBM_RK)                                                           // colour field
         b += (static_cast<size_t>(p.nf) + p.ns + 1) * (d->precision == BCLBM_F64 ? 8 : 12);
+    if (d->flags & BCLBM_FLAG_LAGGED_COLOUR) b += (static_cast<size_t>(p.nf) + p.ns + 1) * 4;  // its second copy
     b += (static_cast<size_t>(grid_for(p.nf)) * 6 + 64) * 8;                               // reduction partials
     if (d->collision == BCLBM_LINKS) b += pad * 12 + pad * 8;  // info, u_store index, force; labelled-node lists
     return b;
@@ -374,6 +384,7 @@ StepArgs bclbm::handle_args(const bclbm_handle* h) {
     for (int q = 0; q < 19; ++q) a.L.ghost_src[q] = h->ghost_src[q];
     a.cg = h->d_cg;
     a.cgf = h->d_cgf;
+    a.cgf_out = h->d_cgf2;
     a.cgx = h->fx_storage ? reinterpret_cast<int64_t*>(h->d_cg) : nullptr;
     a.params = h->d_params;
     a.tau = h->tau[0];
@@ -688,6 +699,7 @@ void free_all(bclbm_handle* h) {
     if (h->d_vel) free_dev(h, h->d_vel);
     if (h->d_cg) free_dev(h, h->d_cg);
     if (h->d_cgf) free_dev(h, h->d_cgf);
+    if (h->d_cgf2) free_dev(h, h->d_cgf2);
     if (h->d_params) free_dev(h, h->d_params);
     if (h->d_partials) free_dev(h, h->d_partials);
     if (h->d_red) free_dev(h, h->d_red);
@@ -830,6 +842,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     h->trt = d->collision == BCLBM_TRT;
     h->fma64 = (d->flags & BCLBM_FLAG_FP64_FMA) != 0;
     h->fx_storage = d->precision == BCLBM_F64 && !h->exact && !h->fma64;
+    h->lagged = (d->flags & BCLBM_FLAG_LAGGED_COLOUR) != 0;
     h->rho_w = d->rho_w != 0.0 ? d->rho_w : 1.0;
     h->flux = d->collision == BCLBM_RK && d->flux_control != 0;
     h->mass_fix = d->collision == BCLBM_RK && d->precision != BCLBM_F64 && !(d->flags & BCLBM_FLAG_NO_MASS_FIX);
@@ -1170,6 +1183,11 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             std::vector<float> cgf(cg.begin(), cg.end());
             CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_cgf), ncg * sizeof(float), h->stream));
             CREATE_TRY(cudaMemcpyAsync(h->d_cgf, cgf.data(), ncg * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+            if (h->lagged) {  // the second field carries the same boundary solids and ghost
+                CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_cgf2), ncg * sizeof(float), h->stream));
+                CREATE_TRY(cudaMemcpyAsync(h->d_cgf2, cgf.data(), ncg * sizeof(float), cudaMemcpyHostToDevice,
+                                           h->stream));
+            }
         }
         CREATE_TRY(cudaStreamSynchronize(h->stream));
     }
@@ -1280,6 +1298,22 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
                 CUDA_TRY(h, launch_single_fixed(h->q, h->trt, local, a, h->stream));
             else CUDA_TRY(h, launch_single_fast(h->q, h->precision, h->trt, local, a, pm, h->stream));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
+        } else if (h->lagged && !local) {
+            // one pass; its sums give the force and mass correction of the next step
+            const bool sums = h->flux || h->mass_fix;
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 0], h->stream));
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 1], h->stream));
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));
+            a.cgf = h->d_cgf;
+            a.cgf_out = h->d_cgf2;
+            CUDA_TRY(h, launch_rk_fused(h->q, h->precision, sums, a, h->stream));
+            if (sums) {
+                CUDA_TRY(h, launch_reduce_final(3, h->d_partials, grid_for(h->nf), h->d_red, false, h->stream));
+                CUDA_TRY(h, launch_rk_fix(h->d_red, static_cast<double>(h->nf), h->rho_ref, h->mom_x, h->flux,
+                                          h->mass_fix ? 2 : 0, h->d_params, h->stream));
+            }
+            std::swap(h->d_cgf, h->d_cgf2);
+            if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 3], h->stream));
         } else {
             StepArgs ad = a;
             ad.rho_out = nullptr;
@@ -1291,7 +1325,7 @@ int step_impl(bclbm_handle* h, int nsteps, cudaEvent_t* ev) {
             if (sums) {
                 CUDA_TRY(h, launch_reduce_final(3, h->d_partials, grid_for(h->nf), h->d_red, false, h->stream));
                 CUDA_TRY(h, launch_rk_fix(h->d_red, static_cast<double>(h->nf), h->rho_ref, h->mom_x, h->flux,
-                                          h->mass_fix, h->d_params, h->stream));
+                                          h->mass_fix ? 1 : 0, h->d_params, h->stream));
             }
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 1], h->stream));
             if (ev) CUDA_TRY(h, cudaEventRecord(ev[4 * s + 2], h->stream));

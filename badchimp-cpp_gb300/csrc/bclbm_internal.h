@@ -46,6 +46,8 @@ struct bclbm_handle {
     double* d_vel = nullptr;
     double* d_cg = nullptr;
     float* d_cgf = nullptr;
+    float* d_cgf2 = nullptr;  // BCLBM_FLAG_LAGGED_COLOUR: the colour field the next step writes
+    bool lagged = false;
     bclbm::DevParams* d_params = nullptr;
     double* d_partials = nullptr;
     double* d_red = nullptr;

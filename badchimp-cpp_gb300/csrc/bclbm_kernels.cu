@@ -40,9 +40,15 @@ __global__ void k_rk_fix(const double* sum, double n, double rho_ref, double mom
             set_forcex(params);
         }
         if (fix) {
-            // totals now: n rho_ref + sum[1] and sum[2]; the deficit spread over the nodes
-            const double dt = (params->mass_target[0] - (n * rho_ref + sum[1])) / n;
-            const double dc = (params->mass_target[1] - sum[2]) / n;
+            // totals now: n rho_ref + sum[1] and sum[2]; the deficit spread over the nodes.
+            // fix == 2 (one pass per step): the sums are of the state this step's collision
+            // still corrects by the correction in place, so the next one takes the rest
+            double dt = (params->mass_target[0] - (n * rho_ref + sum[1])) / n;
+            double dc = (params->mass_target[1] - sum[2]) / n;
+            if (fix == 2) {
+                dt -= params->mass_fix[0];
+                dc -= params->mass_fix[1];
+            }
             params->mass_fix[0] = dt;
             params->mass_fix[1] = dc;
             params->mass_fixf[0] = static_cast<float>(dt);
@@ -273,6 +279,29 @@ cudaError_t launch_rk_shift(int Q, int precision, bool local, bool flux, const S
                   : rk_shift_q<19>(precision, local, flux, a, s, density);
 }
 
+template <int Q, class S>
+cudaError_t rk_fused_qs(bool sums, const StepArgs& a, cudaStream_t s) {
+    const int g = grid_for(a.L.nf);
+    if (sums) k_rk_fused_shift<Q, S, true><<<g, kBlock, 0, s>>>(a);
+    else k_rk_fused_shift<Q, S, false><<<g, kBlock, 0, s>>>(a);
+    launch_counter()++;
+    return cudaGetLastError();
+}
+
+template <int Q>
+cudaError_t rk_fused_q(int precision, bool sums, const StepArgs& a, cudaStream_t s) {
+    switch (precision) {
+        case kF32: return rk_fused_qs<Q, float>(sums, a, s);
+        case kF16: return rk_fused_qs<Q, __half>(sums, a, s);
+        case kBF16: return rk_fused_qs<Q, __nv_bfloat16>(sums, a, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_rk_fused(int Q, int precision, bool sums, const StepArgs& a, cudaStream_t s) {
+    return Q == 9 ? rk_fused_q<9>(precision, sums, a, s) : rk_fused_q<19>(precision, sums, a, s);
+}
+
 cudaError_t launch_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params, cudaStream_t s) {
     k_flux_force<<<1, 32, 0, s>>>(sum, inv_n, mom_x, params);
     launch_counter()++;
@@ -292,9 +321,9 @@ cudaError_t launch_rk_collide_f64_fma(int Q, bool local, const StepArgs& a, cuda
     return cudaGetLastError();
 }
 
-cudaError_t launch_rk_fix(const double* sum, double n, double rho_ref, double mom_x, bool flux, bool fix,
+cudaError_t launch_rk_fix(const double* sum, double n, double rho_ref, double mom_x, bool flux, int fix,
                           DevParams* params, cudaStream_t s) {
-    k_rk_fix<<<1, 32, 0, s>>>(sum, n, rho_ref, mom_x, flux ? 1 : 0, fix ? 1 : 0, params);
+    k_rk_fix<<<1, 32, 0, s>>>(sum, n, rho_ref, mom_x, flux ? 1 : 0, fix, params);
     launch_counter()++;
     return cudaGetLastError();
 }

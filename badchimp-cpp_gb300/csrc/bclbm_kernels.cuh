@@ -46,6 +46,7 @@ struct StepArgs {
     double* vel_out;        // [D][nf_pad] when MACROS
     double* cg;             // RK, F64: colour of [nf fluid | ns solids | ghost]
     float* cgf;             // RK, shifted formats: the same colour field in FP32
+    float* cgf_out;         // RK, one pass per step: the colour field this step writes
     int64_t* cgx;           // RK, int64 fixed-point state: the colour field in fixed point
                             // (the buffer of cg, which that step does not use)
     const DevParams* params;
@@ -981,12 +982,14 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_f64(StepArgs a) {
 // fTot + omegaBGK + deltaOmegaF + deltaOmegaST, the two outputs
 // c0 X + RC and c1 X - RC become  ft'_post = X - w rho_ref  and
 // dc_post = (c0 - c1) X + 2 RC.
-template <int Q, class S, bool LOCAL>
-__global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_collide_shift(StepArgs a) {
+// FUSED (BCLBM_FLAG_LAGGED_COLOUR): PASS 1 and PASS 2 in one: the neighbours'
+// colours come from the previous step's field (a.cgf), the node's own colour goes
+// to this step's (a.cgf_out), and sums receives the PASS 1 sums of the node
+// (flux, total deviation, colour difference).
+template <int Q, class S, bool LOCAL, bool FUSED>
+__device__ __forceinline__ void rk_collide_shift_node(const StepArgs& a, int i, float* sums) {
     const bool MACROS = a.rho_out != nullptr;
     constexpr int D = Lat<Q>::D, R = Lat<Q>::REST;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.L.nf) return;
     using T = typename Store<S>::T;
     const S* g = static_cast<const S*>(a.src);
     T v0[Q], v1[Q];
@@ -1066,6 +1069,30 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_collide_shift
 #pragma unroll
         for (int d = 0; d < D; ++d) a.vel_out[static_cast<size_t>(d) * a.L.nf_pad + i] = u[d];
     }
+    if constexpr (FUSED) {
+        a.cgf_out[i] = dcf;
+        sums[0] = j[0];
+        sums[1] = rs;
+        sums[2] = dr;
+    }
+}
+
+template <int Q, class S, bool LOCAL>
+__global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_collide_shift(StepArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.L.nf) return;
+    rk_collide_shift_node<Q, S, LOCAL, false>(a, i, nullptr);
+}
+
+// One pass per step (BCLBM_FLAG_LAGGED_COLOUR), after a step of both passes; SUMS
+// writes the per-block sums that k_rk_fix turns into the next step's force and
+// mass correction.
+template <int Q, class S, bool SUMS>
+__global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_fused_shift(StepArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float sums[3] = {0.f, 0.f, 0.f};
+    if (i < a.L.nf) rk_collide_shift_node<Q, S, false, true>(a, i, sums);
+    if constexpr (SUMS) block_reduce_store_f32<3>(sums, a.partials);
 }
 
 // PASS 2 of the default FP64 two-phase step, on the int64 fixed-point state

@@ -38,12 +38,14 @@ cudaError_t launch_single_fixed(int Q, bool trt, bool local, const StepArgs& a, 
 cudaError_t encode_table_map(const int32_t* table, int pad, int rows, CUtensorMap* out);
 cudaError_t launch_rk_shift(int Q, int precision, bool local, bool sums, const StepArgs& a, cudaStream_t s,
                             bool density);
+// one pass per step of the shifted two-phase formats (BCLBM_FLAG_LAGGED_COLOUR)
+cudaError_t launch_rk_fused(int Q, int precision, bool sums, const StepArgs& a, cudaStream_t s);
 cudaError_t launch_flux_force(const double* sum, double inv_n, double mom_x, DevParams* params, cudaStream_t s);
 // PASS 2 of the FP64 two-phase step with FMA contraction (BCLBM_FLAG_FP64_FMA)
 cudaError_t launch_rk_collide_f64_fma(int Q, bool local, const StepArgs& a, cudaStream_t s);
 // the default FP64 two-phase step on the int64 fixed-point state: PASS 1 (density) or PASS 2
 cudaError_t launch_rk_fx(int Q, bool local, bool sums, const StepArgs& a, cudaStream_t s, bool density);
-cudaError_t launch_rk_fix(const double* sum, double n, double rho_ref, double mom_x, bool flux, bool fix,
+cudaError_t launch_rk_fix(const double* sum, double n, double rho_ref, double mom_x, bool flux, int fix,
                           DevParams* params, cudaStream_t s);
 cudaError_t launch_gather(int Q, int precision, int nfields, bool local, const StepArgs& a, const int32_t* slot_bulk,
                           double* out, cudaStream_t s);

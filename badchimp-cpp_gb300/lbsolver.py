@@ -32,6 +32,7 @@ FLAG_EXACT = 1
 FLAG_SFC_ORDER = 2
 FLAG_FP64_FMA = 4
 FLAG_NO_MASS_FIX = 8
+FLAG_LAGGED_COLOUR = 16
 
 
 def weights(nq: int) -> np.ndarray:
@@ -158,10 +159,12 @@ class Solver:
     def __init__(self, lat: Lattice, f_init, collision=BGK, precision=F64, tau=(1.0, 1.0), force=(0.0, 0.0, 0.0),
                  sigma=0.0, beta=0.0, flux_control=False, mom_x=0.0, rho_init=None, exact=False, sfc=False,
                  rho_ref=1.0, store_scale=0.0, fma64=False, mass_fix=True, tags=None, labels=None, force_on=None,
-                 rho_w=1.0):
+                 rho_w=1.0, lagged_colour=False):
         """collision LINKS is the std_one_phase step (src/std_one_phase/main.cpp):
         tags, labels (interior domains) and force_on are its node attributes [N]
-        (Nodes tags, interior_domains, force), rho_w the pressure-boundary density."""
+        (Nodes tags, interior_domains, force), rho_w the pressure-boundary density.
+        lagged_colour: two-phase shifted storage in one pass per step, the colour
+        gradient from the previous step's colours (BCLBM_FLAG_LAGGED_COLOUR)."""
         if isinstance(precision, str):
             precision = PRECISION[precision]
         links = None
@@ -177,7 +180,7 @@ class Solver:
         self.lat = lat
         self.nfields = 2 if collision == RK else 1
         flags = (FLAG_EXACT if exact else 0) | (FLAG_SFC_ORDER if sfc else 0) | (FLAG_FP64_FMA if fma64 else 0) | \
-            (0 if mass_fix else FLAG_NO_MASS_FIX)
+            (0 if mass_fix else FLAG_NO_MASS_FIX) | (FLAG_LAGGED_COLOUR if lagged_colour else 0)
         F = np.zeros(3)
         F[:len(force)] = force
         self._h = _native.create(lat, np.ascontiguousarray(f_init, dtype=np.float64), collision, precision, flags,

@@ -591,10 +591,12 @@ def run_twophase(args, world, rank):
     l0 = bclbm.native.launch_count()
     with ClockSampler(0) as clk:
         for prec in args.tp_precisions.split(","):
-            base = prec.split("-")[0]  # "f64": fixed point; "f64-fma": FMA contraction; "f64-exact": reference order
+            # "f64": fixed point; "f64-fma": FMA contraction; "f64-exact": reference order;
+            # "f16-lag" (any shifted format): one pass per step, BCLBM_FLAG_LAGGED_COLOUR
+            base = prec.split("-")[0]
             with L.Solver(lat, f0, collision=L.RK, precision=base, tau=(1.0, 1.0), force=(args.gx, 0.0, 0.0),
                           sigma=args.sigma, beta=args.beta, rho_init=rho, fma64=prec.endswith("-fma"),
-                          exact=prec.endswith("-exact")) as s:
+                          exact=prec.endswith("-exact"), lagged_colour=prec.endswith("-lag")) as s:
                 s.step(args.warmup)
                 s.sync()
                 tm = s.step_timed(args.steps)

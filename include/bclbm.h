@@ -94,6 +94,14 @@ extern "C" {
                                      that restores the two conserved totals, sum (f0 + f1) and
                                      sum (f0 - f1), from an FP64 reduction (rounding of the
                                      stored values does not conserve them) */
+#define BCLBM_FLAG_LAGGED_COLOUR 16u /* two-phase shifted storage (F32 / F16 / BF16): one pass per
+                                        step instead of two.  The colour gradient of step t takes the
+                                        neighbours' colours of step t - 1 (the step's own colour and
+                                        densities stay current), and the flux controller's force and
+                                        the mass correction computed in step t apply from step t + 1.
+                                        Not the reference's ordering (main_TWOPHASE.cpp:238-376 forms
+                                        every colour before any collision); the first step after
+                                        bclbm_create runs both passes. */
 
 typedef struct {
     int32_t lattice_q;        /* 9 or 19 */

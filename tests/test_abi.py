@@ -53,7 +53,8 @@ def test_footprint_on_host(bclbm, native_lib):
 def _create_rc(bclbm, lat, f_init, **kw):
     N = bclbm.native
     d = N.make_desc(lat, f_init, kw.get("collision", 0), kw.get("precision", 0), kw.get("flags", 0),
-                    (0.8, 0.8), (0.0, 0.0, 0.0), 0.0, 0.0, 0, 0.0, 1.0, 0.0, None)
+                    kw.get("tau", (0.8, 0.8)), (0.0, 0.0, 0.0), kw.get("sigma", 0.0), 0.0, kw.get("flux", 0), 0.0,
+                    1.0, 0.0, kw.get("rho_init"))
     h = ctypes.c_void_p()
     return N.lib().bclbm_create(ctypes.byref(d), ctypes.byref(h))
 
@@ -88,6 +89,27 @@ def test_create_rejects_bad_descriptor(bclbm, native_lib):
     assert _create_rc(bclbm, case.lat, f0, precision=7) == -1
     assert _create_rc(bclbm, case.lat, f0, precision=2, flags=1) == -1  # exact needs F64
     assert _create_rc(bclbm, case.lat, None) == -1
+
+
+def test_create_rejects_modes_outside_their_range(bclbm, native_lib, capfd):
+    """Descriptor checks made before any device work: the fixed-point FP64 step's
+    parameter ranges and the one-pass two-phase step's requirements."""
+    L = bclbm.lbsolver
+    case = lbcases.Case("box_12x10x8", bclbm)
+    f0 = L.initiate_single(case.lat, np.ones(case.n_nodes))
+    assert _create_rc(bclbm, case.lat, f0, tau=(0.5, 0.5)) == -1
+    assert "tau > 0.5" in capfd.readouterr().err
+    assert _create_rc(bclbm, case.lat, f0, flags=L.FLAG_LAGGED_COLOUR) == -1  # single phase
+    assert "BCLBM_FLAG_LAGGED_COLOUR" in capfd.readouterr().err
+    ones = np.ones(case.n_nodes)
+    f2, rho = L.initiate_twophase(case.lat, ones, 0 * ones, ones)
+    rk = dict(collision=L.RK, rho_init=rho)
+    assert _create_rc(bclbm, case.lat, f2, precision=L.F64, flags=L.FLAG_LAGGED_COLOUR, **rk) == -1
+    assert "BCLBM_FLAG_LAGGED_COLOUR" in capfd.readouterr().err
+    assert _create_rc(bclbm, case.lat, f2, precision=L.F16, flags=L.FLAG_LAGGED_COLOUR, flux=1, **rk) == -1
+    assert "constant body force" in capfd.readouterr().err
+    assert _create_rc(bclbm, case.lat, f2, precision=L.F64, sigma=4.0, **rk) == -1
+    assert "sigma" in capfd.readouterr().err
 
 
 def test_missing_library_fails_loudly(bclbm, tmp_path, monkeypatch):

@@ -243,3 +243,71 @@ def test_two_phase_unequal_viscosities(bclbm, gpu, oracle, lattice, shape, radiu
             assert relerr(r, er) <= 1e-12, mode
             assert relerr(cgb, ecg) <= 1e-12, mode
             assert np.abs(vel - evel).max() <= u_bound(evel, ef, UV_STEPS), mode
+
+
+def _developed(bclbm, size=64, steps=1000):
+    """A 64^3 two-phase pack after `steps` exact FP64 steps (interfaces formed)."""
+    L = bclbm.lbsolver
+    geo, _, _ = bclbm.geometry.sphere_pack((size,) * 3, radius=TP_RADIUS, porosity=POROSITY, seed=SEED)
+    lat = L.Lattice.from_geometry(geo, "D3Q19", "xyz")
+    red = np.random.default_rng(SEED + 1).random(geo.shape) < 0.5
+    rho0 = np.where(geo == 1, red, 0.0)
+    rho1 = np.where(geo == 1, ~red, 0.0).astype(np.float64)
+    f0, rho = L.initiate_twophase(lat, lat.attribute(rho0), lat.attribute(rho1),
+                                  lat.attribute(np.full(geo.shape, 0.5)))
+    with tp_solver(bclbm, lat, f0, rho, exact=True) as s:
+        s.step(steps)
+        f = s.download_f()
+        r, _, _ = s.download_macros()
+    rho_dev = rho.reshape(-1, 2).copy()
+    rho_dev[lat.bulk] = r.reshape(-1, 2)[lat.bulk]
+    return lat, f, rho_dev.reshape(-1)
+
+
+LAG_STEPS = 200
+
+
+def test_two_phase_lagged_colour(bclbm, gpu):
+    """BCLBM_FLAG_LAGGED_COLOUR (one pass per step, the gradient from the previous
+    step's colours) on FP32 storage, from a developed 64^3 state: its first step is
+    the two-pass step bit for bit; after 200 steps the saturation stays within 1e-7
+    of exact FP64, the colour field within a mean of 5e-3 and the phase fluxes within
+    5% (the deviations FP16 storage itself makes over such runs)."""
+    lat, f, rho = _developed(bclbm)
+    b = lat.bulk
+    cx = np.array([1, 0, 0, 1, 1, 1, 1, 0, 0, -1, 0, 0, -1, -1, -1, -1, 0, 0, 0], dtype=np.float64)
+
+    def run(n, **kw):
+        with tp_solver(bclbm, lat, f, rho, **kw) as s:
+            s.step(n)
+            st = s.reduce()
+            g = s.download_f().reshape(-1, 2, 19)[b]
+            _, _, cg = s.download_macros()
+        return st["saturation"], g, cg[b], [(g[:, k, :] * cx[None, :]).sum() for k in range(2)]
+
+    _, g2, _, _ = run(1, precision="f32")
+    _, gl, _, _ = run(1, precision="f32", lagged_colour=True)
+    assert np.array_equal(g2, gl)
+    s_ref, _, cg_ref, fl_ref = run(LAG_STEPS, exact=True)
+    s_lag, g_lag, cg_lag, fl_lag = run(LAG_STEPS, precision="f32", lagged_colour=True)
+    _, g_two, _, _ = run(LAG_STEPS, precision="f32")
+    assert not np.array_equal(g_lag, g_two)  # the one-pass step ran
+    assert abs(s_lag - s_ref) <= 1e-7
+    assert np.abs(cg_lag - cg_ref).mean() <= 5e-3
+    for a, c in zip(fl_lag, fl_ref):
+        assert abs(a - c) <= 0.05 * abs(c)
+
+
+def test_two_phase_lagged_colour_mass(bclbm, gpu):
+    """FP16 storage in one pass per step over 2,000 steps on the 64^3 pack: the
+    lag-aware mass correction keeps the saturation within 1e-6 of its start, 10x
+    closer than the uncorrected run."""
+    lat, f, rho = _developed(bclbm, steps=10)
+    drift = {}
+    for fix in (True, False):
+        with tp_solver(bclbm, lat, f, rho, precision="f16", lagged_colour=True, mass_fix=fix) as s:
+            s0 = s.reduce()["saturation"]
+            s.step(DRIFT_STEPS)
+            drift[fix] = abs(s.reduce()["saturation"] - s0)
+    assert drift[True] <= 1e-6, drift
+    assert drift[False] >= 10 * drift[True], drift
