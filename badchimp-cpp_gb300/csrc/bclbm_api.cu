@@ -993,6 +993,76 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_params), sizeof(DevParams), h->stream));
     CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_partials), (static_cast<size_t>(grid_for(h->nf)) * 6 + 64) * sizeof(double), h->stream));
     CREATE_TRY(pool_malloc(reinterpret_cast<void**>(&h->d_red), 16 * sizeof(double), h->stream));
+    // the step parameters: body force, and for shifted two-phase storage the conserved
+    // totals of the uploaded state
+    auto build_params = [&]() {
+        DevParams prm;
+        std::memset(&prm, 0, sizeof(prm));
+        for (int k = 0; k < 3; ++k) {
+            prm.force[k] = h->force[k];
+            prm.forcef[k] = static_cast<float>(h->force[k]);
+            prm.forcex[k] = fx::param(h->force[k]);
+        }
+        if (h->mass_fix) {
+            // the conserved totals of the uploaded state, sum over bulk nodes of
+            // sum_q (f0 + f1) and sum_q (f0 - f1), in FP64 (fixed order per chunk)
+            const size_t nb = static_cast<size_t>(d->n_bulk), Qs = static_cast<size_t>(h->q);
+            std::vector<double> pt(64, 0.0), pc(64, 0.0);
+            parallel_for(64, [&](size_t c0, size_t c1) {
+                for (size_t c = c0; c < c1; ++c)
+                    for (size_t b = nb * c / 64; b < nb * (c + 1) / 64; ++b) {
+                        const double* fb = d->f_init + static_cast<size_t>(d->bulk[b]) * 2 * Qs;
+                        for (size_t q = 0; q < Qs; ++q) {
+                            pt[c] += fb[q] + fb[Qs + q];
+                            pc[c] += fb[q] - fb[Qs + q];
+                        }
+                    }
+            }, 1);
+            for (int c = 0; c < 64; ++c) {
+                prm.mass_target[0] += pt[c];
+                prm.mass_target[1] += pc[c];
+            }
+        }
+        return prm;
+    };
+    // The common case, a contiguous bulk list whose table is checked on the device: the
+    // populations go up on a second stream while the neighbour rows are copied and checked,
+    // and are converted after the checks; one synchronisation covers both.  The conversion
+    // reads slot i = bulk index i (k_prepare_affine writes that map whatever the checks
+    // find), so it stays in bounds when a check fails; DevParams goes up first, so that
+    // the conversion's range flag is not overwritten.
+    const bool early_pops = affine && h->bulk_contiguous && device_table;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_alloc = nullptr, ev_copied = nullptr;
+    double* early_tmp = nullptr;
+    // releases the second stream's objects (their pending work completes first) and,
+    // stream-ordered, the staging buffer
+    auto end_side = [&]() {
+        if (early_tmp) cudaFreeAsync(early_tmp, h->stream);
+        if (side) cudaStreamDestroy(side);
+        if (ev_alloc) cudaEventDestroy(ev_alloc);
+        if (ev_copied) cudaEventDestroy(ev_copied);
+        early_tmp = nullptr;
+        side = nullptr;
+        ev_alloc = ev_copied = nullptr;
+    };
+    if (early_pops) {
+        const DevParams prm = build_params();
+        const size_t naos = static_cast<size_t>(h->nf) * h->nfields * Q;
+        cudaError_t e = cudaMemcpyAsync(h->d_params, &prm, sizeof(prm), cudaMemcpyHostToDevice, h->stream);
+        if (e == cudaSuccess) e = pool_malloc(reinterpret_cast<void**>(&early_tmp), naos * sizeof(double), h->stream);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_alloc, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_copied, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_alloc, h->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev_alloc, 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(early_tmp, d->f_init + static_cast<size_t>(h->bulk0) * h->nfields * Q,
+                                naos * sizeof(double), cudaMemcpyHostToDevice, side);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_copied, side);
+        if (e != cudaSuccess) end_side();
+        CREATE_TRY(e);
+    }
     if (!affine)
         CREATE_TRY(cudaMemcpyAsync(h->d_slot_bulk, h->slot_bulk.data(), h->nf * sizeof(int32_t),
                                    cudaMemcpyHostToDevice, h->stream));
@@ -1037,6 +1107,19 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
                 k_build_pull_affine<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, dbad + 5, h->d_nbr, h->bulk0,
                                                                                 h->nf, h->nf_pad, Q);
                 launch_counter() += 3;
+                if (early_pops) {  // the populations, once their copy on the second stream is done
+                    e = cudaStreamWaitEvent(h->stream, ev_copied, 0);
+                    if (e == cudaSuccess)
+                        e = cudaMemsetAsync(h->pops[0], 0, static_cast<size_t>(h->nfields) * Q * pad *
+                                                               store_bytes(h->precision), h->stream);
+                    if (e == cudaSuccess) {
+                        const int mode = h->fx_storage ? 1 : (h->precision == BCLBM_F64 ? 0 : 2);
+                        k_upload_aos<<<grid_for(h->nf), kBlock, 0, h->stream>>>(
+                            early_tmp, h->d_slot_bulk, h->pops[0], h->nf, h->nf_pad, Q, h->nfields, mode,
+                            h->precision, h->rho_ref, h->scale, &h->d_params->fx_overflow);
+                        launch_counter()++;
+                    }
+                }
             } else {
                 k_check_links<<<grid_for(h->nf), kBlock, 0, h->stream>>>(rows, dty, h->bulk0, h->nf, Q, dbad);
                 GhostSrc g;
@@ -1047,6 +1130,8 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             }
             e = cudaGetLastError();
         }
+        if (e == cudaSuccess) e = cudaGetLastError();
+        end_side();
         if (e == cudaSuccess) e = cudaMemcpyAsync(bad, dbad, sizeof(bad), cudaMemcpyDeviceToHost, h->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
         // stream-ordered frees: no device-wide synchronisation while other handles run
@@ -1100,34 +1185,10 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         if (affine)
             for (int k = 0; k < R; ++k) h->ghost_src[k] = std::max(bad[5 + k], 0);
     }
-    DevParams prm;
-    std::memset(&prm, 0, sizeof(prm));
-    for (int k = 0; k < 3; ++k) {
-        prm.force[k] = h->force[k];
-        prm.forcef[k] = static_cast<float>(h->force[k]);
-        prm.forcex[k] = fx::param(h->force[k]);
+    if (!early_pops) {
+        const DevParams prm = build_params();
+        CREATE_TRY(cudaMemcpyAsync(h->d_params, &prm, sizeof(prm), cudaMemcpyHostToDevice, h->stream));
     }
-    if (h->mass_fix) {
-        // the conserved totals of the uploaded state, sum over bulk nodes of
-        // sum_q (f0 + f1) and sum_q (f0 - f1), in FP64 (fixed order per chunk)
-        const size_t nb = static_cast<size_t>(d->n_bulk), Qs = static_cast<size_t>(h->q);
-        std::vector<double> pt(64, 0.0), pc(64, 0.0);
-        parallel_for(64, [&](size_t c0, size_t c1) {
-            for (size_t c = c0; c < c1; ++c)
-                for (size_t b = nb * c / 64; b < nb * (c + 1) / 64; ++b) {
-                    const double* fb = d->f_init + static_cast<size_t>(d->bulk[b]) * 2 * Qs;
-                    for (size_t q = 0; q < Qs; ++q) {
-                        pt[c] += fb[q] + fb[Qs + q];
-                        pc[c] += fb[q] - fb[Qs + q];
-                    }
-                }
-        }, 1);
-        for (int c = 0; c < 64; ++c) {
-            prm.mass_target[0] += pt[c];
-            prm.mass_target[1] += pc[c];
-        }
-    }
-    CREATE_TRY(cudaMemcpyAsync(h->d_params, &prm, sizeof(prm), cudaMemcpyHostToDevice, h->stream));
     if (h->collision == BCLBM_LINKS) {
         auto up = [&](auto** dst, const auto& v, size_t n_min) -> cudaError_t {
             using E = typename std::remove_reference<decltype(v)>::type::value_type;
@@ -1195,7 +1256,9 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     // initial populations: reference AoS -> storage format.  The bulk nodes' rows are
     // one contiguous block in the common case (vtklb.py numbers the fluid nodes first):
     // upload it as it is and transpose on the device; otherwise transpose on the host.
-    if (h->bulk_contiguous) {
+    if (early_pops) {
+        // uploaded and converted with the table checks
+    } else if (h->bulk_contiguous) {
         const int es = h->nfields * Q;
         const size_t naos = static_cast<size_t>(h->nf) * es;
         const int mode = h->fx_storage ? 1 : (h->precision == BCLBM_F64 ? 0 : 2);
