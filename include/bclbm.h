@@ -57,10 +57,11 @@ extern "C" {
 #define BCLBM_BGK 0 /* calcOmegaBGK + calcDeltaOmegaF          (src/lbsolver/LBcollision.h:27-46, 194-213) */
 #define BCLBM_TRT 1 /* calcOmegaBGKTRT + calcDeltaOmegaFTRT(phi=1) (LBcollision.h:50-75, 215-236) */
 #define BCLBM_RK 2  /* Rothman-Keller two-phase step of src/twophase/main_TWOPHASE.cpp:238-392;
-                       BCLBM_F64: both colour sets in 64-bit fixed point with the per-node scalars
-                       (relaxation rate of the phase mix, colour gradient, amplitudes) in FP64
-                       (default), the reference's rounding with BCLBM_FLAG_EXACT, FP64 with FMA
-                       under BCLBM_FLAG_FP64_FMA */
+                       BCLBM_F64: both colour sets and the colour field in 64-bit fixed point, every
+                       term of the collision a fixed-point product (default; needs |sigma| < 3.5 and
+                       |beta| < 4), the reference's rounding with BCLBM_FLAG_EXACT, FP64 with FMA
+                       under BCLBM_FLAG_FP64_FMA; BCLBM_F32 / F16 / BF16: shifted storage with FP32
+                       arithmetic (one pass per step with BCLBM_FLAG_LAGGED_COLOUR) */
 #define BCLBM_LINKS 3 /* the std_one_phase step (src/std_one_phase/main.cpp:470-575, D3Q19):
                          BGK + Guo force times the per-node force attribute, interior-domain mass
                          sources (calcDeltaOmegaQ) and the solid-fluid, pressure (anti-bounce-back)
@@ -75,9 +76,10 @@ extern "C" {
                         resolution (finer than an FP64 ulp of any population of a fluid
                         with rho ~ 1; needs sum_q |f_q| < 8 and rho > 0.15 per node,
                         else bclbm_reduce reports BCLBM_ERR_NONFINITE), results rounded
-                        to FP64.  With
+                        to FP64; the single-phase collision needs tau > 0.5 (and
+                        tau_anti > 0.5 for TRT).  With
                         BCLBM_FLAG_EXACT: FP64 in the reference's expression order;
-                        with BCLBM_FLAG_FP64_FMA: FP64 with FMA. */
+                        with BCLBM_FLAG_FP64_FMA: FP64 with FMA (any parameters). */
 #define BCLBM_F32 1  /* FP32 shifted deviations (f - w*rho_ref)/w, FP32 arithmetic */
 #define BCLBM_F16 2  /* FP16 shifted, scaled deviations, FP32 arithmetic */
 #define BCLBM_BF16 3 /* BF16 shifted, scaled deviations, FP32 arithmetic */
