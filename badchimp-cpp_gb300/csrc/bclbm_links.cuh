@@ -31,7 +31,8 @@ struct LinksArgs {
     const uint32_t* info;       // [nf] label | kLinkAdd | kLinkPress
     const int32_t* pidx;        // [nf] u_store index of a pressure-boundary node, else -1
     const int32_t* force_on;    // [nf] force attribute
-    double* ustore;             // [3][npress] velocity of the last step
+    double* ustore;             // [3][npress] velocity of the last step (FP64; the shifted formats keep
+                                // FP32 values in it: their kernels alone read it)
     int npress;
     double rho_w;               // pressure-boundary density
     const int32_t* lab_slot;    // [nlabeled] slots of the labelled bulk nodes, by label, in bulk order
@@ -395,7 +396,7 @@ __device__ __forceinline__ void links_velocity_f(const LinksArgs& A, int i, uint
     if (!LOCAL && (inf & kLinkPress)) {
         const int p = __ldg(A.pidx + i);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) u[d] = static_cast<float>(A.ustore[static_cast<size_t>(d) * A.npress + p]);
+        for (int d = 0; d < 3; ++d) u[d] = reinterpret_cast<const float*>(A.ustore)[static_cast<size_t>(d) * A.npress + p];
     }
 }
 
@@ -499,10 +500,10 @@ __global__ void __launch_bounds__(kBlock, BCLBM_LINKS_MINB) k_links_collide_shif
 #pragma unroll
     for (int q = 0; q < 19; ++q)
         Store<S>::store(out + static_cast<size_t>(q) * pad + i, fd[q] * (sc / static_cast<float>(Lat<19>::w(q))));
-    if (inf & kLinkPress) {
+    if (inf & kLinkPress) {  // FP32 values (no conversion on the FP64 pipe in the many warps with one)
         const int p = __ldg(A.pidx + i);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) A.ustore[static_cast<size_t>(d) * A.npress + p] = vel[d];
+        for (int d = 0; d < 3; ++d) reinterpret_cast<float*>(A.ustore)[static_cast<size_t>(d) * A.npress + p] = vel[d];
     }
     if (A.s.rho_out) {
         A.s.rho_out[i] = A.s.rho_ref + static_cast<double>(dr);
