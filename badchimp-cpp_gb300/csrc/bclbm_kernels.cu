@@ -106,9 +106,9 @@ cudaError_t single_fast_qs(bool trt, bool local, const StepArgs& a, const CUtens
     constexpr bool kStaged = std::is_same<S, double>::value;
     if constexpr (!kStaged) {
         if (!local) {
-            const int gp = grid_for((a.L.nf + 1) / 2);
-            if (trt) k_single_pair<Q, S, true><<<gp, kBlock, 0, s>>>(a);
-            else k_single_pair<Q, S, false><<<gp, kBlock, 0, s>>>(a);
+            const int gp = ((a.L.nf + 1) / 2 + BCLBM_PAIR_BLOCK - 1) / BCLBM_PAIR_BLOCK;
+            if (trt) k_single_pair<Q, S, true><<<gp, BCLBM_PAIR_BLOCK, 0, s>>>(a);
+            else k_single_pair<Q, S, false><<<gp, BCLBM_PAIR_BLOCK, 0, s>>>(a);
             launch_counter()++;
             return cudaGetLastError();
         }
@@ -136,13 +136,13 @@ cudaError_t single_fast_qs(bool trt, bool local, const StepArgs& a, const CUtens
 
 template <int Q>
 cudaError_t single_fixed_q(bool trt, bool local, const StepArgs& a, cudaStream_t s) {
-    const int g = grid_for(a.L.nf);
+    const int g = (a.L.nf + BCLBM_FX_BLOCK - 1) / BCLBM_FX_BLOCK;
     if (trt) {
-        if (local) k_single_fixed<Q, true, true><<<g, kBlock, 0, s>>>(a);
-        else k_single_fixed<Q, true, false><<<g, kBlock, 0, s>>>(a);
+        if (local) k_single_fixed<Q, true, true><<<g, BCLBM_FX_BLOCK, 0, s>>>(a);
+        else k_single_fixed<Q, true, false><<<g, BCLBM_FX_BLOCK, 0, s>>>(a);
     } else {
-        if (local) k_single_fixed<Q, false, true><<<g, kBlock, 0, s>>>(a);
-        else k_single_fixed<Q, false, false><<<g, kBlock, 0, s>>>(a);
+        if (local) k_single_fixed<Q, false, true><<<g, BCLBM_FX_BLOCK, 0, s>>>(a);
+        else k_single_fixed<Q, false, false><<<g, BCLBM_FX_BLOCK, 0, s>>>(a);
     }
     launch_counter()++;
     return cudaGetLastError();
@@ -191,8 +191,9 @@ cudaError_t rk_fx_q(bool local, bool flux, const StepArgs& a, cudaStream_t s, bo
             else k_rk_density<Q, int64_t, false, false><<<g, kBlock, 0, s>>>(a);
         }
     } else {
-        if (local) k_rk_collide_fx<Q, true><<<g, kBlock, 0, s>>>(a);
-        else k_rk_collide_fx<Q, false><<<g, kBlock, 0, s>>>(a);
+        const int gc = (a.L.nf + BCLBM_RK_FX_BLOCK - 1) / BCLBM_RK_FX_BLOCK;
+        if (local) k_rk_collide_fx<Q, true><<<gc, BCLBM_RK_FX_BLOCK, 0, s>>>(a);
+        else k_rk_collide_fx<Q, false><<<gc, BCLBM_RK_FX_BLOCK, 0, s>>>(a);
     }
     launch_counter()++;
     return cudaGetLastError();

@@ -482,15 +482,20 @@ __global__ void __launch_bounds__(kBlock, 1) k_single_staged(StepArgs a, const _
 
 // ---------------------------------------------------------------------------
 // k_single_fixed: one single-phase step on F64 storage with 64-bit fixed-point
-// arithmetic (bclbm_fixed.cuh).  BCLBM_FX_MINB is the minimum number of
-// resident blocks per SM requested from the register allocator: 3 (80
-// registers, 156 B of spills) beats the 2 blocks of the unbounded 115-132
-// registers because the kernel is issue-latency bound (256^3: 8,925 -> 9,410
-// MLUPS); the collision hands each pair to the store as soon as it is known,
-// which keeps the spills small.
+// arithmetic (bclbm_fixed.cuh).  BCLBM_FX_BLOCK threads per block and at least
+// BCLBM_FX_MINB resident blocks per SM asked of the register allocator: 80
+// registers, 24 warps per SM.  Blocks of 256 at 3 per SM measured 14,420
+// MLUPS at 256^3, of 128 at 6-7 14,600, of 64 at 12 or 14 14,650 (the same
+// warps in smaller blocks: finer placement of the work over the SMs), of 32 at
+// 28 14,130.  (Earlier: 3 blocks of 256 at 80 registers beat the 2 blocks of
+// the unbounded 115-132 registers, 8,925 -> 9,410 MLUPS.)
 // ---------------------------------------------------------------------------
 #ifndef BCLBM_FX_MINB
-#define BCLBM_FX_MINB 3
+#define BCLBM_FX_MINB 12
+#endif
+// threads per block of k_single_fixed (the kernel uses no shared memory)
+#ifndef BCLBM_FX_BLOCK
+#define BCLBM_FX_BLOCK 64
 #endif
 
 // one update of slot i from its pulled values X (the int64 state of Store<int64_t>)
@@ -518,7 +523,7 @@ __device__ __forceinline__ void fixed_node(const StepArgs& a, int i) {
 }
 
 template <int Q, bool TRT, bool LOCAL>
-__global__ void __launch_bounds__(kBlock, BCLBM_FX_MINB) k_single_fixed(StepArgs a) {
+__global__ void __launch_bounds__(BCLBM_FX_BLOCK, BCLBM_FX_MINB) k_single_fixed(StepArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.L.nf) fixed_node<Q, TRT, LOCAL>(a, i);
 }
@@ -727,13 +732,16 @@ __device__ __forceinline__ void load_rk(const S* __restrict__ g, const LatticeVi
 // resident blocks per SM asked of the register allocator (256^3, ms per step, one slot
 // per thread / two at 2, 3, 4 blocks: FP16 0.1699 / 0.1797, 0.1579, 0.1556; FP32
 // 0.2212 / 0.2256, 0.2194, 0.2231)
+#ifndef BCLBM_PAIR_BLOCK
+#define BCLBM_PAIR_BLOCK 256
+#endif
 template <class S>
 constexpr int pair_min_blocks() {
-    return sizeof(S) == 2 ? 4 : 3;
+    return (sizeof(S) == 2 ? 4 : 3) * (256 / BCLBM_PAIR_BLOCK);
 }
 
 template <int Q, class S, bool TRT>
-__global__ void __launch_bounds__(kBlock, pair_min_blocks<S>()) k_single_pair(StepArgs a) {
+__global__ void __launch_bounds__(BCLBM_PAIR_BLOCK, pair_min_blocks<S>()) k_single_pair(StepArgs a) {
     constexpr int D = Lat<Q>::D, R = Lat<Q>::REST;
     const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (i >= a.L.nf) return;
@@ -1116,8 +1124,11 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_fused_shift(S
 #ifndef BCLBM_RK_FX_MINB
 #define BCLBM_RK_FX_MINB 2
 #endif
+#ifndef BCLBM_RK_FX_BLOCK
+#define BCLBM_RK_FX_BLOCK 256
+#endif
 template <int Q, bool LOCAL>
-__global__ void __launch_bounds__(kBlock, BCLBM_RK_FX_MINB) k_rk_collide_fx(StepArgs a) {
+__global__ void __launch_bounds__(BCLBM_RK_FX_BLOCK, BCLBM_RK_FX_MINB) k_rk_collide_fx(StepArgs a) {
     const bool MACROS = a.rho_out != nullptr;
     constexpr int D = Lat<Q>::D, R = Lat<Q>::REST, NP = Lat<Q>::NP;
     constexpr int SH1 = Q == 19 ? 1 : 2;  // w_axis / w_diag

@@ -207,9 +207,9 @@ cudaError_t mass_fixed(bool local, const LinksArgs& A, cudaStream_t s) {
 }
 
 cudaError_t collide_fixed(bool local, const LinksArgs& A, cudaStream_t s) {
-    const int n = A.s.L.nf;
-    if (local) k_links_collide_fixed<true><<<grid_for(n), kBlock, 0, s>>>(A);
-    else k_links_collide_fixed<false><<<grid_for(n), kBlock, 0, s>>>(A);
+    const int g = (A.s.L.nf + BCLBM_LINKS_FX_BLOCK - 1) / BCLBM_LINKS_FX_BLOCK;
+    if (local) k_links_collide_fixed<true><<<g, BCLBM_LINKS_FX_BLOCK, 0, s>>>(A);
+    else k_links_collide_fixed<false><<<g, BCLBM_LINKS_FX_BLOCK, 0, s>>>(A);
     launch_counter()++;
     return cudaGetLastError();
 }

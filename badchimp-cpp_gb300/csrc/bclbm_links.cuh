@@ -276,7 +276,14 @@ __global__ void __launch_bounds__(kBlock) k_links_collide(LinksArgs A) {
 // The default BCLBM_F64 arithmetic of the std_one_phase step: GB300's FP64 pipe
 // caps the FP64 forms of the collision at about a tenth of the HBM bandwidth.
 template <bool LOCAL>
-__global__ void __launch_bounds__(kBlock, BCLBM_FX_MINB) k_links_collide_fixed(LinksArgs A) {
+// resident blocks per SM asked of the register allocator by the fixed-point links step
+#ifndef BCLBM_LINKS_FX_MINB
+#define BCLBM_LINKS_FX_MINB 3
+#endif
+#ifndef BCLBM_LINKS_FX_BLOCK
+#define BCLBM_LINKS_FX_BLOCK 256
+#endif
+__global__ void __launch_bounds__(BCLBM_LINKS_FX_BLOCK, BCLBM_LINKS_FX_MINB) k_links_collide_fixed(LinksArgs A) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.s.L.nf) return;
     const uint32_t inf = __ldg(A.info + i);
