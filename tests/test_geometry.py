@@ -80,3 +80,17 @@ def test_native_lattice_builder_rejects_bad_masks(bclbm):
         bclbm.native.lattice_tables(np.full((4, 4, 4), 2, dtype=np.int8), 19, 0)
     with pytest.raises(bclbm.native.BclbmError):
         bclbm.native.lattice_tables(np.ones((4, 4), dtype=np.int8), 19, 0)
+
+
+def test_native_builder_from_concurrent_threads(bclbm):
+    """The library's host loops share one pool of worker threads: calls from several
+    host threads at once (one loop on the pool, the others on their callers' threads)
+    give the same tables as one call at a time."""
+    from concurrent.futures import ThreadPoolExecutor
+    geo, _, _ = bclbm.geometry.sphere_pack((48, 40, 44), radius=5.0, porosity=0.45, seed=11)
+    ref = bclbm.geometry.build_lattice(geo, "D3Q19", "xyz")
+    with ThreadPoolExecutor(6) as ex:
+        outs = list(ex.map(lambda _: bclbm.geometry.build_lattice(geo, "D3Q19", "xyz"), range(12)))
+    for out in outs:
+        for k in ("neigh", "types", "pos"):
+            assert np.array_equal(out[k], ref[k]), k

@@ -292,3 +292,38 @@ def test_destroyed_handles_memory_is_kept_until_trim(bclbm, gpu):
     assert bclbm.native.lib().bclbm_trim() == 0
     free2 = torch.cuda.mem_get_info()[0]
     assert free2 - free1 >= need // 2
+
+
+@pytest.mark.parametrize("name,tag", [("disc_40x32", "rk_200"), ("pack_20", "rk_100")])
+@pytest.mark.parametrize("prec", ["f32", "bf16"])
+def test_lagged_colour_against_two_passes(bclbm, gpu, name, tag, prec):
+    """BCLBM_FLAG_LAGGED_COLOUR on a D2Q9 and a D3Q19 fixture: the first step equals the
+    two-pass step bit for bit, the run stays finite and conserves the saturation about
+    as well as the two-pass run (drift from the start within 3x the two-pass run's, or
+    below 1e-6 in FP32 / 1e-4 in BF16).  From the fixtures' random phases the lag sends
+    the separation down another path (mean colour difference 0.03-0.05 measured; the
+    bounds from a developed state are in test_gpu_headline_parity.py): here the mean
+    stays below 0.1."""
+    case = lbcases.Case(name, bclbm)
+    run = case.runs[tag]
+    b = case.lat.bulk
+    with make_solver(case, run, precision=prec) as s:
+        s.step(1)
+        one = outputs(case, run, s)
+    with make_solver(case, run, precision=prec, lagged_colour=True) as s:
+        s.step(1)
+        one_lag = outputs(case, run, s)
+    assert np.array_equal(one["f"], one_lag["f"])
+    sat = {}
+    cg = {}
+    for lag in (False, True):
+        with make_solver(case, run, precision=prec, lagged_colour=lag) as s:
+            s0 = s.reduce()["saturation"]
+            s.step(run["steps"])
+            st = s.reduce()
+            out = outputs(case, run, s)
+        assert np.isfinite(out["f"]).all() and not st["nonfinite"]
+        sat[lag] = abs(st["saturation"] - s0)
+        cg[lag] = out["cg"][b]
+    assert sat[True] <= max(3 * sat[False], {"f32": 1e-6, "bf16": 1e-4}[prec]), sat
+    assert np.abs(cg[True] - cg[False]).mean() <= 0.1
