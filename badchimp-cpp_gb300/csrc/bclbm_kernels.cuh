@@ -1095,8 +1095,14 @@ __global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_collide_shift
 // One pass per step (BCLBM_FLAG_LAGGED_COLOUR), after a step of both passes; SUMS
 // writes the per-block sums that k_rk_fix turns into the next step's force and
 // mass correction.
+// resident blocks per SM asked of the register allocator (192^3, MLUPS at 3 / 4 / 5
+// blocks: FP16 14,750 / 15,413 / 13,436, FP32 12,974 / 12,474 / 10,659)
+template <class S>
+constexpr int fused_min_blocks() {
+    return sizeof(S) == 2 ? 4 : 3;
+}
 template <int Q, class S, bool SUMS>
-__global__ void __launch_bounds__(kBlock, BCLBM_RK_COLL_MINB) k_rk_fused_shift(StepArgs a) {
+__global__ void __launch_bounds__(kBlock, fused_min_blocks<S>()) k_rk_fused_shift(StepArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float sums[3] = {0.f, 0.f, 0.f};
     if (i < a.L.nf) rk_collide_shift_node<Q, S, false, true>(a, i, sums);
