@@ -77,6 +77,30 @@ cudaError_t pool_malloc(void** p, size_t bytes, cudaStream_t s) {
     return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
+// The caller's large host arrays page-locked for the length of one copy.  On the
+// Grace host the device reads pageable memory through the host's page tables, and
+// a range whose translations it has not walked yet copies at ~20-25 GB/s (1 GiB:
+// 42-51 ms in a process that had just built its arrays) instead of ~190; locking
+// the range costs 2-6 ms per GiB and the copy then runs at the link's rate.  A
+// range that cannot be locked (already registered, a mapping the driver refuses)
+// is copied as it is.  unlock() only after the copies that use the range have
+// completed.
+struct HostLock {
+    void* p = nullptr;
+    void lock(const void* ptr, size_t bytes) {
+        if (p || !ptr || bytes < (size_t(64) << 20)) return;
+        if (cudaHostRegister(const_cast<void*>(ptr), bytes, cudaHostRegisterDefault) == cudaSuccess)
+            p = const_cast<void*>(ptr);
+        else
+            cudaGetLastError();  // the copy falls back to the pageable path
+    }
+    void unlock() {
+        if (p) cudaHostUnregister(p);
+        cudaGetLastError();
+        p = nullptr;
+    }
+};
+
 size_t store_bytes(int precision) {
     switch (precision) {
         case BCLBM_F64: return 8;
@@ -1035,6 +1059,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_alloc = nullptr, ev_copied = nullptr;
     double* early_tmp = nullptr;
+    HostLock lock_f, lock_rows;
     // releases the second stream's objects (their pending work completes first) and,
     // stream-ordered, the staging buffer
     auto end_side = [&]() {
@@ -1056,11 +1081,17 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_copied, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventRecord(ev_alloc, h->stream);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev_alloc, 0);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(early_tmp, d->f_init + static_cast<size_t>(h->bulk0) * h->nfields * Q,
-                                naos * sizeof(double), cudaMemcpyHostToDevice, side);
+        if (e == cudaSuccess) {
+            const double* src = d->f_init + static_cast<size_t>(h->bulk0) * h->nfields * Q;
+            lock_f.lock(src, naos * sizeof(double));
+            e = cudaMemcpyAsync(early_tmp, src, naos * sizeof(double), cudaMemcpyHostToDevice, side);
+        }
         if (e == cudaSuccess) e = cudaEventRecord(ev_copied, side);
-        if (e != cudaSuccess) end_side();
+        if (e != cudaSuccess) {
+            if (side) cudaStreamSynchronize(side);
+            lock_f.unlock();
+            end_side();
+        }
         CREATE_TRY(e);
     }
     if (!affine)
@@ -1083,9 +1114,11 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         if (e == cudaSuccess && !affine)
             e = pool_malloc(reinterpret_cast<void**>(&dext), static_cast<size_t>(d->n_nodes) * sizeof(int32_t), h->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(h->d_nbr, 0, ntab * sizeof(int32_t), h->stream);
-        if (e == cudaSuccess)
+        if (e == cudaSuccess) {
+            lock_rows.lock(d->neigh + static_cast<size_t>(h->bulk0) * Q, nrow * sizeof(int32_t));
             e = cudaMemcpyAsync(rows, d->neigh + static_cast<size_t>(h->bulk0) * Q, nrow * sizeof(int32_t),
                                 cudaMemcpyHostToDevice, h->stream);
+        }
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(dty, d->types, static_cast<size_t>(d->n_nodes) * sizeof(int16_t),
                                 cudaMemcpyHostToDevice, h->stream);
@@ -1134,6 +1167,9 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         end_side();
         if (e == cudaSuccess) e = cudaMemcpyAsync(bad, dbad, sizeof(bad), cudaMemcpyDeviceToHost, h->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        else cudaStreamSynchronize(h->stream);  // the copies from the locked ranges are done either way
+        lock_rows.unlock();
+        lock_f.unlock();
         // stream-ordered frees: no device-wide synchronisation while other handles run
         if (rows) cudaFreeAsync(rows, h->stream);
         if (dty) cudaFreeAsync(dty, h->stream);
@@ -1457,9 +1493,14 @@ int bclbm_download_f(bclbm_handle* h, double* f) {
     const int es = h->nfields * h->q;
     const size_t n = static_cast<size_t>(h->nf) * es;
     if (h->bulk_contiguous) {
-        CUDA_TRY(h, cudaMemcpyAsync(f + static_cast<size_t>(h->bulk0) * es, h->d_gather, n * sizeof(double),
-                                    cudaMemcpyDeviceToHost, h->stream));
-        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        HostLock lk;
+        lk.lock(f + static_cast<size_t>(h->bulk0) * es, n * sizeof(double));
+        cudaError_t e = cudaMemcpyAsync(f + static_cast<size_t>(h->bulk0) * es, h->d_gather, n * sizeof(double),
+                                        cudaMemcpyDeviceToHost, h->stream);
+        const cudaError_t es2 = cudaStreamSynchronize(h->stream);
+        lk.unlock();
+        if (e == cudaSuccess) e = es2;
+        CUDA_TRY(h, e);
     } else {
         std::vector<double> tmp(n);
         CUDA_TRY(h, cudaMemcpyAsync(tmp.data(), h->d_gather, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
