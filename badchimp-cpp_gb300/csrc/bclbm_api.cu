@@ -99,6 +99,13 @@ struct HostLock {
         cudaGetLastError();
         p = nullptr;
     }
+    // still locked on an error path: a copy may be in flight
+    ~HostLock() {
+        if (p) {
+            cudaDeviceSynchronize();
+            unlock();
+        }
+    }
 };
 
 size_t store_bytes(int precision) {
@@ -1098,8 +1105,12 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         CREATE_TRY(cudaMemcpyAsync(h->d_slot_bulk, h->slot_bulk.data(), h->nf * sizeof(int32_t),
                                    cudaMemcpyHostToDevice, h->stream));
     if (!device_table) {
+        HostLock lk;
+        lk.lock(tab.data(), tab.size() * sizeof(int32_t));
         CREATE_TRY(cudaMemcpyAsync(h->d_nbr, tab.data(), tab.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
                                    h->stream));
+        CREATE_TRY(cudaStreamSynchronize(h->stream));
+        lk.unlock();
     } else {
         // the bulk nodes' neighbour rows and the node types go up as they are (and, for
         // a plan with explicit maps, the node -> slot map); the table is checked and
@@ -1328,6 +1339,8 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
                             d->f_init[n * es + static_cast<size_t>(k) * Q + q];
             }
         });
+        HostLock lk;
+        lk.lock(soa.data(), nsoa * sizeof(double));
         if (h->precision == BCLBM_F64 && !h->fx_storage) {
             CREATE_TRY(cudaMemcpyAsync(h->pops[0], soa.data(), nsoa * sizeof(double), cudaMemcpyHostToDevice, h->stream));
             CREATE_TRY(cudaStreamSynchronize(h->stream));
@@ -1358,6 +1371,7 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
             cudaFreeAsync(tmp, h->stream);
             CREATE_TRY(e);
         }
+        lk.unlock();  // every branch above ends with the stream synchronised
     }
 #undef CREATE_TRY
     h->cur = 0;
