@@ -487,13 +487,18 @@ __global__ void __launch_bounds__(kBlock) k_links_mass_shift(LinksArgs A) {
 
 // resident blocks per SM asked of the register allocator for the shifted step (192^3
 // tagged pack, F32 / F16 MLUPS: 3 blocks 15.7k / 17.1k, 4: 17.6k / 18.7k, 5: 18.3k / 20.4k,
-// 6: 17.4k / 18.7k)
+// 6: 17.4k / 18.7k; after the later changes 4: 20.9k / 24.0k, 5: 20.4k / 24.9k, 6: 17.6k /
+// 21.5k): 5 for the 2-byte formats, 4 for FP32
 #ifndef BCLBM_LINKS_MINB
 #define BCLBM_LINKS_MINB 5
 #endif
+template <class S>
+constexpr int links_min_blocks() {
+    return sizeof(S) == 2 ? BCLBM_LINKS_MINB : 4;
+}
 
 template <class S, bool LOCAL>
-__global__ void __launch_bounds__(kBlock, BCLBM_LINKS_MINB) k_links_collide_shift(LinksArgs A) {
+__global__ void __launch_bounds__(kBlock, links_min_blocks<S>()) k_links_collide_shift(LinksArgs A) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= A.s.L.nf) return;
     const uint32_t inf = __ldg(A.info + i);
