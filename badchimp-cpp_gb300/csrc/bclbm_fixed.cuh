@@ -372,6 +372,47 @@ inline Consts make_consts(bool trt, double tau, double tau_anti, const double* F
     return K;
 }
 
+// The colour gradient's norm and direction for the two-phase collision, from the
+// integer gradient T (G = T / 3, |T_d| < 6): cgn = |G| and n = G / |G| in fixed
+// point, or n = G where |G| < 2^-52 (the reference's gs = 1 / (|G| + (|G| < eps))
+// gives G / (|G| + 1), equal to G to 2^-104).  T is scaled by a power of two so that
+// its largest component t_d is in [1/2, 1); x = |t|^2 in [1/4, 3); y = 1/sqrt(x) from
+// an FP32 estimate and two Newton steps y (3 - x y^2) / 2 in fixed point; n = t y and
+// |G| = x y / 3 scaled back.  third = 1/3 in fixed point.
+__host__ __device__ __forceinline__ float rsqrt_estimate(float x) {
+#ifdef __CUDA_ARCH__
+    return rsqrtf(x);
+#else
+    return 1.0f / __builtin_sqrtf(x);
+#endif
+}
+
+template <int D>
+__host__ __device__ __forceinline__ void unit_normal(const int64_t* T, int64_t third, int64_t* n, int64_t& cgn) {
+    auto mag = [](int64_t v) { return static_cast<uint64_t>(v < 0 ? -v : v); };
+    uint64_t mx = mag(T[0]) > mag(T[1]) ? mag(T[0]) : mag(T[1]);
+    if (D == 3 && mag(T[2]) > mx) mx = mag(T[2]);
+    n[0] = n[1] = n[2] = 0;
+    cgn = 0;
+    if (mx == 0) return;
+    const int sh = clz64(mx) - 4;  // mx < 2^63: sh >= -3
+    int64_t t[3] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) t[d] = sh >= 0 ? static_cast<int64_t>(static_cast<uint64_t>(T[d]) << sh) : (T[d] >> -sh);
+    int64_t x = mul_ss(t[0], t[0]) + mul_ss(t[1], t[1]);
+    if (D == 3) x += mul_ss(t[2], t[2]);
+    const float xf = static_cast<float>(static_cast<int>(x >> 32)) * 3.7252902984619140625e-9f;  // 2^-28
+    const float ys = rsqrt_estimate(xf) * 536870912.0f;                                       // 2^29
+    int64_t y = static_cast<int64_t>(static_cast<int>(ys + 0.5f)) << 31;
+    for (int it = 0; it < 2; ++it) y = mul_uu(y, 3 * ONE - mul_uu(x, mul_uu(y, y))) >> 1;
+    const int64_t r3 = mul_uu(mul_uu(x, y), third);  // |t| / 3
+    cgn = sh >= 0 ? r3 >> sh : static_cast<int64_t>(static_cast<uint64_t>(r3) << -sh);
+    if (cgn >= 256) {  // |G| >= 2^-52
+        for (int d = 0; d < D; ++d) n[d] = mul_su(t[d], y);
+    } else {
+        for (int d = 0; d < D; ++d) n[d] = mul_su(T[d], third);
+    }
+}
+
 // Constants of the two-phase (Rothman-Keller) collision in fixed point: the
 // lattice weights and B coefficients by weight class (0 rest, 1 axis, 2 diagonal).
 struct RkConsts {

@@ -1214,35 +1214,7 @@ __global__ void __launch_bounds__(BCLBM_RK_FX_BLOCK, BCLBM_RK_FX_MINB) k_rk_coll
     }
     // |G| and n = G / |G| (the reference's gs = 1 / (|G| + (|G| < eps)))
     int64_t n[3] = {0, 0, 0}, cgn = 0;
-    {
-        auto mag = [](int64_t v) { return static_cast<uint64_t>(v < 0 ? -v : v); };
-        uint64_t mx = max(mag(T[0]), mag(T[1]));
-        if (D == 3) mx = max(mx, mag(T[2]));
-        if (mx != 0) {
-            // |T_d| < 6 (|sc| < 1/2): mx < 2^63, and t = T 2^sh has max |t_d| in [1/2, 1)
-            const int sh = __clzll(static_cast<long long>(mx)) - 4;
-            int64_t t[3] = {0, 0, 0};
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                t[d] = sh >= 0 ? static_cast<int64_t>(static_cast<uint64_t>(T[d]) << sh) : (T[d] >> -sh);
-            int64_t x = fx::mul_ss(t[0], t[0]) + fx::mul_ss(t[1], t[1]);  // |t|^2 in [1/4, 3)
-            if (D == 3) x += fx::mul_ss(t[2], t[2]);
-            const float xf = static_cast<float>(static_cast<int>(x >> 32)) * 3.7252902984619140625e-9f;  // 2^-28
-            int64_t y = static_cast<int64_t>(__float2int_rn(rsqrtf(xf) * 536870912.0f)) << 31;  // 2^29
-#pragma unroll
-            for (int it = 0; it < 2; ++it)  // y (3 - x y^2) / 2
-                y = fx::mul_uu(y, 3 * fx::ONE - fx::mul_uu(x, fx::mul_uu(y, y))) >> 1;
-            const int64_t r3 = fx::mul_uu(fx::mul_uu(x, y), K.third);  // |t| / 3
-            cgn = sh >= 0 ? r3 >> sh : static_cast<int64_t>(static_cast<uint64_t>(r3) << -sh);
-            if (cgn >= 256) {  // |G| >= 2^-52
-#pragma unroll
-                for (int d = 0; d < D; ++d) n[d] = fx::mul_su(t[d], y);
-            } else {
-#pragma unroll
-                for (int d = 0; d < D; ++d) n[d] = fx::mul_su(T[d], K.third);
-            }
-        }
-    }
+    fx::unit_normal<D>(T, K.third, n, cgn);
     // relaxation rate and the products that carry it
     int64_t oms, omsw2, k45, K3, tf3w2, sto;
     if (K.uniform) {

@@ -130,4 +130,51 @@ int fx_primitives(const double* a, const double* b, int n) {
     return bad;
 }
 
+// fx::unit_normal against long-double norms over n integer gradients T with
+// |T_d| < 6 (in fixed point) spread over 60 binary orders of magnitude (every 7th in
+// two dimensions); worst[0] = max |n_d - T_d / |T||, worst[1] = max ||G| - |T| / 3|,
+// worst[2] = max over |G| < 2^-52 of |n_d - T_d / 3|
+void fx_unit_normal_check(int n, unsigned seed, double* worst) {
+    uint64_t st = 0x9E3779B97F4A7C15ull ^ seed;
+    auto next = [&st]() {  // splitmix64
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    const int64_t third = fx::param(1.0 / 3.0);
+    const long double one = static_cast<long double>(fx::ONE);
+    worst[0] = worst[1] = worst[2] = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const int scale = static_cast<int>(next() % 61);
+        int64_t T[3];
+        for (int d = 0; d < 3; ++d) {
+            int64_t v = static_cast<int64_t>(next() % (uint64_t(6) << 60)) >> scale;
+            if (next() & 1) v = -v;
+            T[d] = v;
+        }
+        const bool two = k % 7 == 0;
+        if (two) T[2] = 0;
+        int64_t nv[3], cgn;
+        if (two) fx::unit_normal<2>(T, third, nv, cgn);
+        else fx::unit_normal<3>(T, third, nv, cgn);
+        long double t2 = 0;
+        for (int d = 0; d < 3; ++d) t2 += (static_cast<long double>(T[d]) / one) * (static_cast<long double>(T[d]) / one);
+        const long double tn = std::sqrt(t2);
+        if (tn == 0) continue;
+        const double eg = static_cast<double>(std::fabs(static_cast<long double>(cgn) / one - tn / 3));
+        if (eg > worst[1]) worst[1] = eg;
+        for (int d = 0; d < 3; ++d) {
+            const long double nd = static_cast<long double>(nv[d]) / one;
+            if (tn / 3 >= 2.220446049250313e-16L) {
+                const double e = static_cast<double>(std::fabs(nd - (static_cast<long double>(T[d]) / one) / tn));
+                if (e > worst[0]) worst[0] = e;
+            } else {
+                const double e = static_cast<double>(std::fabs(nd - static_cast<long double>(T[d]) / one / 3));
+                if (e > worst[2]) worst[2] = e;
+            }
+        }
+    }
+}
+
 }  // extern "C"

@@ -34,6 +34,8 @@ def fxlib(tmp_path_factory):
                            ctypes.c_double, ctypes.c_double, vp, vp, vp, vp]
     lib.fx_primitives.argtypes = [vp, vp, ctypes.c_int]
     lib.fx_collide_ovf.argtypes = [ctypes.c_double]
+    lib.fx_unit_normal_check.argtypes = [ctypes.c_int, ctypes.c_uint, vp]
+    lib.fx_unit_normal_check.restype = None
     return lib
 
 
@@ -51,6 +53,18 @@ def test_primitives_against_128bit_reference(fxlib):
     a = np.concatenate([a, rng.uniform(-7.9, 7.9, 20000), [-7.999, 7.999, 0.0, -1e-18, 1e-18]])
     b = np.concatenate([b, rng.uniform(0.0, 1.0, 20000), [0.999999999, 0.0, 0.5, 1e-18, 0.999999999]])
     assert fxlib.fx_primitives(_p(a), _p(b), a.size) == 0
+
+
+def test_colour_gradient_normal(fxlib):
+    """The two-phase collision's |G| and G / |G| from the integer colour gradient
+    (fx::unit_normal, the device code compiled for the host): the direction within
+    2^-56 and |G| within 2^-51 of long-double norms, over 60 binary orders of
+    magnitude of the gradient; below |G| = 2^-52 the reference's G / (|G| + 1) = G."""
+    worst = np.zeros(3)
+    fxlib.fx_unit_normal_check(400000, 7, _p(worst))
+    assert worst[0] <= 2.0 ** -56, worst
+    assert worst[1] <= 2.0 ** -51, worst
+    assert worst[2] <= 2.0 ** -58, worst
 
 
 def test_range_guard(fxlib):
