@@ -696,6 +696,24 @@ __device__ __forceinline__ void load_field2(const S* __restrict__ g, const Latti
     }
 }
 
+// load_field2 from the table entries e[q] = nbr[q][i] already in registers (the
+// colour gradient reads the same entries: the pull along c_q takes e[rev q])
+template <int Q, class S, bool LOCAL>
+__device__ __forceinline__ void load_field2_e(const S* __restrict__ g, const LatticeView& L, int i, const int* e,
+                                              typename Store<S>::T* v0, typename Store<S>::T* v1) {
+    constexpr int R = Lat<Q>::REST;
+    using V = typename Pair<S>::V;
+    const V* gp = reinterpret_cast<const V*>(g);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const size_t el = (q == R || LOCAL) ? static_cast<size_t>(q) * L.nf_pad + i
+                                            : pull_elem<Q>(L, q, e[Lat<Q>::rev(q)], i);
+        const V p = gp[el];
+        v0[q] = static_cast<typename Store<S>::T>(p.x);
+        v1[q] = static_cast<typename Store<S>::T>(p.y);
+    }
+}
+
 template <int Q, class S, bool LOCAL>
 __device__ __forceinline__ void load_rk(const S* __restrict__ g, const LatticeView& L, int i, double* f0,
                                         double* f1, double rho_ref, double inv_scale) {
@@ -1000,11 +1018,14 @@ __device__ __forceinline__ void rk_collide_shift_node(const StepArgs& a, int i, 
     constexpr int D = Lat<Q>::D, R = Lat<Q>::REST;
     using T = typename Store<S>::T;
     const S* g = static_cast<const S*>(a.src);
+    int e[Q - 1];  // each table entry once, for the pull and the colour gradient
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) e[q] = ld_table(a.L.nbr + static_cast<size_t>(q) * a.L.nf_pad + i);
     T v0[Q], v1[Q];
-    load_field2<Q, S, LOCAL>(g, a.L, i, v0, v1);
+    load_field2_e<Q, S, LOCAL>(g, a.L, i, e, v0, v1);
     float sc[Q];
 #pragma unroll
-    for (int q = 0; q < Q - 1; ++q) sc[q] = a.cgf[__ldg(a.L.nbr + static_cast<size_t>(q) * a.L.nf_pad + i)];
+    for (int q = 0; q < Q - 1; ++q) sc[q] = a.cgf[e[q]];
     sc[R] = 0.f;
     const float isc = a.f_inv_scale;
     float ft[Q], dc[Q];
@@ -1148,13 +1169,16 @@ __global__ void __launch_bounds__(BCLBM_RK_FX_BLOCK, BCLBM_RK_FX_MINB) k_rk_coll
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.L.nf) return;
     const size_t pad = static_cast<size_t>(a.L.nf_pad);
+    int e[Q - 1];  // each table entry once, for the pull and the colour gradient
+#pragma unroll
+    for (int q = 0; q < Q - 1; ++q) e[q] = ld_table(a.L.nbr + static_cast<size_t>(q) * pad + i);
     int64_t X0[Q], X1[Q];
-    load_field2<Q, int64_t, LOCAL>(static_cast<const int64_t*>(a.src), a.L, i, X0, X1);
+    load_field2_e<Q, int64_t, LOCAL>(static_cast<const int64_t*>(a.src), a.L, i, e, X0, X1);
     // colour at the downstream neighbours (grad, LButilities.h:12-22), a quarter
     // of it so that the gradient sums stay inside the range (|colour| < 2)
     int64_t sc[Q - 1];
 #pragma unroll
-    for (int q = 0; q < Q - 1; ++q) sc[q] = a.cgx[ld_table(a.L.nbr + static_cast<size_t>(q) * pad + i)] >> 2;
+    for (int q = 0; q < Q - 1; ++q) sc[q] = a.cgx[e[q]] >> 2;
     int ovf = 0;
     int64_t rho0 = 0, rho1 = 0, ft[Q];
 #pragma unroll
