@@ -582,6 +582,24 @@ __device__ __forceinline__ void block_reduce_store_f32(float* vals, double* part
     }
 }
 
+// The block's sums of NV values per thread held in shared memory as sh[NV][kBlock]
+// (written by each thread, read after the barrier): warp k adds row k, lane l the
+// entries l, l + 32, ... in order, then a shuffle tree.  Deterministic.
+template <int NV>
+__device__ __forceinline__ void block_sums_from_shared(const float* sh, double* partials) {
+    static_assert(NV <= kBlock / 32, "one warp per value");
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp < NV) {
+        float v = sh[warp * kBlock + lane];
+#pragma unroll
+        for (int m = 1; m < kBlock / 32; ++m) v += sh[warp * kBlock + m * 32 + lane];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) partials[static_cast<size_t>(blockIdx.x) * NV + warp] = static_cast<double>(v);
+    }
+}
+
 // Final sum of nrows rows of NV partials by one block of kFinalThreads threads,
 // in a fixed order: thread t takes rows t, t + kFinalThreads, ... (loads issued
 // four at a time, added in row order), then a fixed pairwise tree over the
@@ -665,6 +683,24 @@ template <>
 struct Pair<int64_t> {
     using V = longlong2;
 };
+
+// Two FP32 values rounded to nearest into one stored pair: for the 2-byte formats
+// one packed conversion (cvt.rn.f16x2.f32 / cvt.rn.bf16x2.f32), the same bits as
+// two separate round-to-nearest conversions.
+template <class S>
+__device__ __forceinline__ typename Pair<S>::V pack2(float a, float b);
+template <>
+__device__ __forceinline__ float2 pack2<float>(float a, float b) {
+    return make_float2(a, b);
+}
+template <>
+__device__ __forceinline__ __half2 pack2<__half>(float a, float b) {
+    return __floats2half2_rn(a, b);
+}
+template <>
+__device__ __forceinline__ __nv_bfloat162 pack2<__nv_bfloat16>(float a, float b) {
+    return __floats2bfloat162_rn(a, b);
+}
 
 template <class S>
 __device__ __forceinline__ void store_pair(S* out, size_t elem, S a, S b) {
@@ -802,13 +838,7 @@ __global__ void __launch_bounds__(BCLBM_PAIR_BLOCK, pair_min_blocks<S>()) k_sing
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const float s = scale / static_cast<float>(Lat<Q>::w(q));
-        S x, y;
-        Store<S>::store(&x, fa[q] * s);
-        Store<S>::store(&y, fb[q] * s);
-        V p;
-        p.x = x;
-        p.y = y;
-        *reinterpret_cast<V*>(out + static_cast<size_t>(q) * pad + i) = p;
+        *reinterpret_cast<V*>(out + static_cast<size_t>(q) * pad + i) = pack2<S>(fa[q] * s, fb[q] * s);
     }
 }
 
@@ -1010,8 +1040,11 @@ __global__ void __launch_bounds__(kBlock) k_rk_collide_f64(StepArgs a) {
 // dc_post = (c0 - c1) X + 2 RC.
 // FUSED (BCLBM_FLAG_LAGGED_COLOUR): PASS 1 and PASS 2 in one: the neighbours'
 // colours come from the previous step's field (a.cgf), the node's own colour goes
-// to this step's (a.cgf_out), and sums receives the PASS 1 sums of the node
-// (flux, total deviation, colour difference).
+// to this step's (a.cgf_out), and sums (when not null) receives the PASS 1 sums of
+// the node (flux, total deviation, colour difference) at sums[0], sums[kBlock],
+// sums[2 kBlock]: a shared-memory column, written as soon as they are known
+// (192^3, MLUPS with the sums in registers to the end / in shared memory: FP16
+// 16,291 / 16,615, BF16 16,095 / 16,457, FP32 13,230 / 13,813).
 template <int Q, class S, bool LOCAL, bool FUSED>
 __device__ __forceinline__ void rk_collide_shift_node(const StepArgs& a, int i, float* sums) {
     const bool MACROS = a.rho_out != nullptr;
@@ -1040,6 +1073,14 @@ __device__ __forceinline__ void rk_collide_shift_node(const StepArgs& a, int i, 
         j[0] += Lat<Q>::cx(q) * ft[q];
         j[1] += Lat<Q>::cy(q) * ft[q];
         j[2] += Lat<Q>::cz(q) * ft[q];
+    }
+    if constexpr (FUSED) {
+        // to shared memory at once (stride kBlock), so they hold no registers below
+        if (sums != nullptr) {
+            sums[0] = j[0];
+            sums[kBlock] = rs;
+            sums[2 * kBlock] = dr;
+        }
     }
     const float F[3] = {a.params->forcef[0], a.params->forcef[1], a.params->forcef[2]};
     const float rho_ref = a.f_rho_ref;
@@ -1087,10 +1128,8 @@ __device__ __forceinline__ void rk_collide_shift_node(const StepArgs& a, int i, 
         const float dRC = (q == R) ? 0.f : rfb * w * cn * (Lat<Q>::wclass(q) == 1 ? 1.f : 0.70710678118654752f);
         const float X = Xd + w * rho_ref;
         const float s = sc_out / w;
-        S st, sd;
-        Store<S>::store(&st, Xd * s + fix_t);
-        Store<S>::store(&sd, (dcf * X + 2.f * dRC) * s + fix_c);
-        store_pair(out, static_cast<size_t>(q) * a.L.nf_pad + i, st, sd);
+        reinterpret_cast<typename Pair<S>::V*>(out)[static_cast<size_t>(q) * a.L.nf_pad + i] =
+            pack2<S>(Xd * s + fix_t, (dcf * X + 2.f * dRC) * s + fix_c);
     }
     if (MACROS) {
         a.rho_out[i] = rho0;
@@ -1100,9 +1139,6 @@ __device__ __forceinline__ void rk_collide_shift_node(const StepArgs& a, int i, 
     }
     if constexpr (FUSED) {
         a.cgf_out[i] = dcf;
-        sums[0] = j[0];
-        sums[1] = rs;
-        sums[2] = dr;
     }
 }
 
@@ -1132,9 +1168,19 @@ constexpr int fused_min_blocks() {
 template <int Q, class S, bool SUMS>
 __global__ void __launch_bounds__(kBlock, fused_min_blocks<S>()) k_rk_fused_shift(StepArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    float sums[3] = {0.f, 0.f, 0.f};
-    if (i < a.L.nf) rk_collide_shift_node<Q, S, false, true>(a, i, sums);
-    if constexpr (SUMS) block_reduce_store_f32<3>(sums, a.partials);
+    if constexpr (SUMS) {
+        // the node's flux, total deviation and colour difference, [3][kBlock]
+        __shared__ float sh[3 * kBlock];
+        float* mine = sh + threadIdx.x;
+        if (i < a.L.nf) {
+            rk_collide_shift_node<Q, S, false, true>(a, i, mine);
+        } else {
+            mine[0] = mine[kBlock] = mine[2 * kBlock] = 0.f;
+        }
+        block_sums_from_shared<3>(sh, a.partials);
+    } else {
+        if (i < a.L.nf) rk_collide_shift_node<Q, S, false, true>(a, i, nullptr);
+    }
 }
 
 // PASS 2 of the default FP64 two-phase step, on the int64 fixed-point state
