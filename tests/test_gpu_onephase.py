@@ -156,3 +156,36 @@ def test_generated_pack_matches_oracle(bclbm, gpu, labels_on):
     assert np.array_equal(f.reshape(-1, 19)[b], fe.reshape(-1, 19)[b])
     assert np.array_equal(rho[b], rhoe[b]) and np.array_equal(vel.reshape(-1, 3)[b], vele.reshape(-1, 3)[b])
     assert np.array_equal(flux, fluxe)
+
+
+@pytest.mark.parametrize("prec,tol_f,tol_u,tol_q", [("f32", 1e-6, 1e-5, 1e-5), ("f16", 1e-4, 1e-3, 1e-3)])
+@pytest.mark.parametrize("seed,n_bulk", [(7, 29767), (8, 29406)], ids=["odd", "even"])
+def test_generated_pack_shifted(bclbm, gpu, seed, n_bulk, prec, tol_f, tol_u, tol_q):
+    """Shifted storage on generated tagged packs (interior domains, pressure ghosts
+    on both z faces) with an odd and an even number of fluid slots: within the
+    tolerances of test_shifted_storage of the oracle's FP64 run after 120 steps."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parent.parent / "oracle"))
+    import oracle
+    L = bclbm.lbsolver
+    mask, attrs = bclbm.geometry.tagged_pack((40, 36, 48), 5.0, 0.45, seed, blob_radius=3.5, blob_spacing=12)
+    lat = L.Lattice.from_geometry(mask, "D3Q19", "xy")
+    assert lat.n_bulk == n_bulk
+    tags, labels, fon = (lat.attribute(attrs[k]).astype(np.int32) for k in ("nodetags", "interior_domains", "force"))
+    f0 = L.initiate_single(lat, np.ones(lat.n_nodes))
+    force = (2e-6, 1e-6, 1e-5)
+    g = oracle.OracleGrid(19, lat.neigh, lat.types, lat.bulk)
+    fe, _, vele, fluxe = oracle.links_run(g, f0, 120, 0.9, force, tags, labels, fon, nthreads=4)
+    with L.Solver(lat, f0, collision=L.LINKS, tau=(0.9, 0.9), force=force, tags=tags, labels=labels,
+                  force_on=fon, precision=prec) as s:
+        s.step(120)
+        f = s.download_f()
+        _, vel, _ = s.download_macros()
+        flux = s.pressure_flux()
+    b = lat.bulk
+    ef = relerr(f.reshape(-1, 19)[b], fe.reshape(-1, 19)[b])
+    ve = vele.reshape(-1, 3)[b]
+    eu = np.abs(vel.reshape(-1, 3)[b] - ve).max() / np.abs(ve).max()
+    eq = np.abs(np.asarray(flux) - np.asarray(fluxe)).max() / np.abs(np.asarray(fluxe)).max()
+    assert ef <= tol_f and eu <= tol_u and eq <= tol_q, (ef, eu, eq)
