@@ -968,6 +968,13 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         h->nflux = static_cast<int>(lp.flux_slot.size());
         h->force_on_sum = lp.force_on_sum;
     } else if (h->collision == BCLBM_RK) {
+        // the pull's element indices (row * pad + slot) are 32-bit
+        if (static_cast<size_t>(Q) * pad > static_cast<size_t>(INT32_MAX)) {
+            std::fprintf(stderr, "bclbm_create: %d fluid nodes exceed the int32 element index\n", h->nf);
+            free_all(h);
+            delete h;
+            return BCLBM_ERR_UNSUPPORTED;
+        }
         // extended neighbour table in device numbering (pull + colour gradient)
         tab.assign(static_cast<size_t>(R) * pad, static_cast<int32_t>(h->nf + h->ns));
         parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {

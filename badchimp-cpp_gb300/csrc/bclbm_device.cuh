@@ -137,9 +137,14 @@ struct LatticeView {
 };
 
 // Element index (row * nf_pad + slot) of the population arriving at slot i along
-// c_q from extended neighbour y, in post-collision storage.
+// c_q from extended neighbour y, in post-collision storage.  32-bit arithmetic
+// (bclbm_create keeps Q nf_pad <= INT32_MAX), so that the address is one wide
+// multiply-add and the index one register (192^3 two-phase, MLUPS with 64-bit /
+// 32-bit indices: one pass FP16 16,557 / 17,460, BF16 16,418 / 17,179; two
+// passes BF16 11,293 / 12,109; FP64 and FP32 unchanged).
+using elem_t = uint32_t;
 template <int Q>
-__device__ __forceinline__ size_t pull_elem(const LatticeView& L, int q, int y, int i) {
+__device__ __forceinline__ elem_t pull_elem(const LatticeView& L, int q, int y, int i) {
     const int rq = Lat<Q>::rev(q);
     int slot, row;
     if (y < L.nf) {
@@ -149,7 +154,7 @@ __device__ __forceinline__ size_t pull_elem(const LatticeView& L, int q, int y, 
         row = rq;
         slot = (y == L.nf + L.ns) ? L.ghost_src[rq] : i;
     }
-    return static_cast<size_t>(row) * L.nf_pad + slot;
+    return static_cast<elem_t>(row) * static_cast<elem_t>(L.nf_pad) + static_cast<elem_t>(slot);
 }
 
 // Population arriving at slot i along c_q, read from post-collision storage g
@@ -166,7 +171,7 @@ __device__ __forceinline__ typename Store<S>::T pull_raw(const S* __restrict__ g
         row = rq;
         slot = (y == L.nf + L.ns) ? L.ghost_src[rq] : i;
     }
-    return g[static_cast<size_t>(row) * L.nf_pad + slot];
+    return g[static_cast<elem_t>(row) * static_cast<elem_t>(L.nf_pad) + static_cast<elem_t>(slot)];
 }
 
 }  // namespace bclbm

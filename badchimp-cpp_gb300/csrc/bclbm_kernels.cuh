@@ -719,9 +719,9 @@ __device__ __forceinline__ void load_field2(const S* __restrict__ g, const Latti
     const V* gp = reinterpret_cast<const V*>(g);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        size_t e;
+        elem_t e;
         if (q == R || LOCAL) {
-            e = static_cast<size_t>(q) * L.nf_pad + i;
+            e = static_cast<elem_t>(q) * static_cast<elem_t>(L.nf_pad) + static_cast<elem_t>(i);
         } else {
             const int y = ld_table(L.nbr + static_cast<size_t>(Lat<Q>::rev(q)) * L.nf_pad + i);
             e = pull_elem<Q>(L, q, y, i);
@@ -742,8 +742,9 @@ __device__ __forceinline__ void load_field2_e(const S* __restrict__ g, const Lat
     const V* gp = reinterpret_cast<const V*>(g);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const size_t el = (q == R || LOCAL) ? static_cast<size_t>(q) * L.nf_pad + i
-                                            : pull_elem<Q>(L, q, e[Lat<Q>::rev(q)], i);
+        const elem_t el = (q == R || LOCAL)
+                              ? static_cast<elem_t>(q) * static_cast<elem_t>(L.nf_pad) + static_cast<elem_t>(i)
+                              : pull_elem<Q>(L, q, e[Lat<Q>::rev(q)], i);
         const V p = gp[el];
         v0[q] = static_cast<typename Store<S>::T>(p.x);
         v1[q] = static_cast<typename Store<S>::T>(p.y);

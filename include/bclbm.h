@@ -110,7 +110,10 @@ typedef struct {
     int32_t n_nodes;          /* N = Grid::size() */
     const int32_t* neigh;     /* [N*Q] */
     const int16_t* types;     /* [N] */
-    int32_t n_bulk;           /* number of bulk (own-rank fluid) nodes */
+    int32_t n_bulk;           /* number of bulk (own-rank fluid) nodes; the steps index the
+                                 populations with 32-bit element numbers, so Q times n_bulk
+                                 (rounded up to a multiple of 64) must stay below 2^31
+                                 (D3Q19: 113 M nodes), else BCLBM_ERR_UNSUPPORTED */
     const int32_t* bulk;      /* [n_bulk], increasing; every listed node has type > 1 */
     const int32_t* pos;       /* [N*nD] Grid positions, needed for BCLBM_FLAG_SFC_ORDER, else NULL */
     int32_t collision;        /* BCLBM_BGK | BCLBM_TRT | BCLBM_RK */
