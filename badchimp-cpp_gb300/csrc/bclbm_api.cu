@@ -175,6 +175,12 @@ int validate_descriptor(const bclbm_desc* d, std::string& err) {
     }
     if ((d->flags & BCLBM_FLAG_SFC_ORDER) && !d->pos) { err = "BCLBM_FLAG_SFC_ORDER needs pos"; return BCLBM_ERR_INVALID; }
     if (d->n_bulk >= d->n_nodes) { err = "n_bulk must be smaller than n_nodes"; return BCLBM_ERR_INVALID; }
+    if (static_cast<int64_t>(Q) * ((static_cast<int64_t>(d->n_bulk) + 63) / 64 * 64) > INT32_MAX) {
+        // element numbers (row * nf_pad + slot) are 32-bit in the pull table and the two-phase pull
+        err = "Q times n_bulk (rounded up to a multiple of 64) exceeds the int32 element numbers "
+              "(D3Q19: 113 M fluid nodes per instance)";
+        return BCLBM_ERR_UNSUPPORTED;
+    }
     const bool fixed = d->precision == BCLBM_F64 && !(d->flags & (BCLBM_FLAG_EXACT | BCLBM_FLAG_FP64_FMA));
     if ((d->flags & BCLBM_FLAG_LAGGED_COLOUR) && !(d->collision == BCLBM_RK && d->precision != BCLBM_F64)) {
         err = "BCLBM_FLAG_LAGGED_COLOUR needs BCLBM_RK with shifted storage (F32, F16 or BF16)";
@@ -968,13 +974,6 @@ int bclbm_create(const bclbm_desc* d, bclbm_handle** out) {
         h->nflux = static_cast<int>(lp.flux_slot.size());
         h->force_on_sum = lp.force_on_sum;
     } else if (h->collision == BCLBM_RK) {
-        // the pull's element indices (row * pad + slot) are 32-bit
-        if (static_cast<size_t>(Q) * pad > static_cast<size_t>(INT32_MAX)) {
-            std::fprintf(stderr, "bclbm_create: %d fluid nodes exceed the int32 element index\n", h->nf);
-            free_all(h);
-            delete h;
-            return BCLBM_ERR_UNSUPPORTED;
-        }
         // extended neighbour table in device numbering (pull + colour gradient)
         tab.assign(static_cast<size_t>(R) * pad, static_cast<int32_t>(h->nf + h->ns));
         parallel_for(static_cast<size_t>(h->nf), [&](size_t s0, size_t s1) {

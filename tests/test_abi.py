@@ -112,6 +112,24 @@ def test_create_rejects_modes_outside_their_range(bclbm, native_lib, capfd):
     assert "sigma" in capfd.readouterr().err
 
 
+def test_create_rejects_element_numbers_past_int32(bclbm, native_lib, capfd):
+    """Q x n_bulk rounded up to 64 must stay at most 2^31 - 1 (the 32-bit element
+    numbers of the pull): checked on the descriptor before any array is read, so
+    the sizes alone are enough (two-phase, whose create reads no array before it)."""
+    N = bclbm.native
+    L = bclbm.lbsolver
+    case = lbcases.Case("box_12x10x8", bclbm)
+    ones = np.ones(case.n_nodes)
+    f2, rho = L.initiate_twophase(case.lat, ones, 0 * ones, ones)
+    d = N.make_desc(case.lat, f2, L.RK, L.F16, 0, (0.8, 0.8), (0.0, 0.0, 0.0), 0.0, 0.0, 0, 0.0, 1.0, 0.0, rho)
+    d.n_bulk = 113_025_409  # rounded up: 113,025,472 x 19 = 2,147,483,968
+    d.n_nodes = d.n_bulk + 1
+    h = ctypes.c_void_p()
+    assert N.lib().bclbm_create(ctypes.byref(d), ctypes.byref(h)) == -5
+    assert "int32 element numbers" in capfd.readouterr().err
+    assert not h.value
+
+
 def test_missing_library_fails_loudly(bclbm, tmp_path, monkeypatch):
     N = bclbm.native
     monkeypatch.setattr(N, "_lib", None)
