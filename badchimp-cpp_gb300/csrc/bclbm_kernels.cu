@@ -172,8 +172,9 @@ cudaError_t rk_shift_qs(bool local, bool flux, const StepArgs& a, cudaStream_t s
             else k_rk_density<Q, S, false, false><<<g, kBlock, 0, s>>>(a);
         }
     } else {
-        if (local) k_rk_collide_shift<Q, S, true><<<g, kBlock, 0, s>>>(a);
-        else k_rk_collide_shift<Q, S, false><<<g, kBlock, 0, s>>>(a);
+        const int gc = (a.L.nf + BCLBM_RK_COLL_BLOCK - 1) / BCLBM_RK_COLL_BLOCK;
+        if (local) k_rk_collide_shift<Q, S, true><<<gc, BCLBM_RK_COLL_BLOCK, 0, s>>>(a);
+        else k_rk_collide_shift<Q, S, false><<<gc, BCLBM_RK_COLL_BLOCK, 0, s>>>(a);
     }
     launch_counter()++;
     return cudaGetLastError();

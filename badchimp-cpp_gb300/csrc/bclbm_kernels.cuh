@@ -1145,13 +1145,18 @@ __device__ __forceinline__ void rk_collide_shift_node(const StepArgs& a, int i, 
 
 // FP32 storage takes 3 resident blocks per SM (192^3: 8,908 -> 9,284 MLUPS against 4;
 // FP16 11,615 at 4, 11,078 at 3, 10,738 at 5)
+// threads per block (192^3, MLUPS at 256 / 128 / 64 with the same resident warps:
+// FP16 11,914 / 11,894 / 11,825, BF16 12,096 / 11,807 / 11,710, FP32 9,521 / 9,588 / 9,586)
+#ifndef BCLBM_RK_COLL_BLOCK
+#define BCLBM_RK_COLL_BLOCK 256
+#endif
 template <class S>
 constexpr int rk_collide_min_blocks() {
-    return sizeof(S) == 2 ? BCLBM_RK_COLL_MINB : 3;
+    return (sizeof(S) == 2 ? BCLBM_RK_COLL_MINB : 3) * (256 / BCLBM_RK_COLL_BLOCK);
 }
 
 template <int Q, class S, bool LOCAL>
-__global__ void __launch_bounds__(kBlock, rk_collide_min_blocks<S>()) k_rk_collide_shift(StepArgs a) {
+__global__ void __launch_bounds__(BCLBM_RK_COLL_BLOCK, rk_collide_min_blocks<S>()) k_rk_collide_shift(StepArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.L.nf) return;
     rk_collide_shift_node<Q, S, LOCAL, false>(a, i, nullptr);
@@ -1162,9 +1167,13 @@ __global__ void __launch_bounds__(kBlock, rk_collide_min_blocks<S>()) k_rk_colli
 // mass correction.
 // resident blocks per SM asked of the register allocator (192^3, MLUPS at 3 / 4 / 5
 // blocks: FP16 14,750 / 15,413 / 13,436, FP32 12,974 / 12,474 / 10,659)
+// (FP32 after the shared-memory sums and 32-bit element numbers: 13,835 at 3, 12,990 at 4)
+#ifndef BCLBM_RK_FUSED_MINB_F32
+#define BCLBM_RK_FUSED_MINB_F32 3
+#endif
 template <class S>
 constexpr int fused_min_blocks() {
-    return sizeof(S) == 2 ? 4 : 3;
+    return sizeof(S) == 2 ? 4 : BCLBM_RK_FUSED_MINB_F32;
 }
 template <int Q, class S, bool SUMS>
 __global__ void __launch_bounds__(kBlock, fused_min_blocks<S>()) k_rk_fused_shift(StepArgs a) {
